@@ -1,0 +1,749 @@
+// C entry points of the hot path: solvers.rs, cg.rs, lora_helpers.rs,
+// lora_drivers.rs and sketch_and_precondition.rs, orchestrated on the GPU.
+#include "rnla_abi.h"
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace rnla {
+
+// Stage timer on the call's stream (device-timed).
+struct StageTimer {
+    cudaStream_t s;
+    cudaEvent_t e[5];
+    int n = 0;
+    explicit StageTimer(cudaStream_t st) : s(st) {
+        for (auto& x : e) RNLA_CUDA(cudaEventCreate(&x));
+    }
+    ~StageTimer() {
+        for (auto& x : e) cudaEventDestroy(x);
+    }
+    void mark() {
+        if (n < 5) RNLA_CUDA(cudaEventRecord(e[n++], s));
+    }
+    double ms(int a, int b) {
+        if (b >= n) return 0.0;
+        float t = 0.f;
+        RNLA_CUDA(cudaEventSynchronize(e[b]));
+        RNLA_CUDA(cudaEventElapsedTime(&t, e[a], e[b]));
+        return t;
+    }
+};
+
+static rnla_options opts_or_default(const rnla_options* o) {
+    rnla_options d;
+    rnla_options_default(&d);
+    return o ? *o : d;
+}
+
+static void check_mat(int64_t m, int64_t n, int64_t ld) {
+    if (m < 0 || n < 0) fail(RNLA_ERR_NEGATIVE_DIMENSIONS, "negative dimension");
+    if (ld < (m > 0 ? m : 1)) fail(RNLA_ERR_INVALID_PARAMETERS, "leading dimension smaller than rows");
+}
+
+// ---------------------------------------------------------------------------
+// Reference-mode range finder (lora_helpers.rs:17-105)
+// ---------------------------------------------------------------------------
+struct DMat {
+    DevBuf<double> buf;
+    int64_t rows = 0, cols = 0;
+    double* p() const { return buf.get(); }
+};
+
+static void stabilize(Ctx& ctx, DMat& X) {
+    const int64_t c = X.rows < X.cols ? X.rows : X.cols;
+    DMat L;
+    L.buf.alloc((size_t)X.rows * c, ctx.stream);
+    L.rows = X.rows;
+    L.cols = c;
+    full_piv_lu_l(ctx, X.p(), X.rows, X.cols, X.rows, L.p(), X.rows);
+    X = std::move(L);
+}
+
+// product with the zero S1 of lora_helpers.rs:63: exactly zero for finite A;
+// with non-finite entries the FP64 GEMM reproduces the NaNs the reference gets.
+static void times_zero(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, int64_t k,
+                       bool finite, DMat& out) {
+    out.buf.alloc((size_t)m * k, ctx.stream);
+    out.rows = m;
+    out.cols = k;
+    if (finite) {
+        fill_zero(ctx, m, k, out.p(), m);
+    } else {
+        DevBuf<double> Z((size_t)n * k, ctx.stream);
+        fill_zero(ctx, n, k, Z, n);
+        gemm_f64(ctx, 'N', 'N', m, k, n, 1.0, A, lda, Z, n, 0.0, out.p(), m);
+    }
+}
+
+static DMat tsog1_ref(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, int64_t k,
+                      int num_passes, int passes_per_stab, bool finite) {
+    if (passes_per_stab == 0) fail(RNLA_ERR_INVALID_PARAMETERS, "passes_per_stab must be nonzero");
+    int passes_done = 0;
+    DMat S;                 // current S (lora_helpers.rs:67)
+    bool s1_zero = true;    // S1 is the zero n x k matrix of line 63 unless replaced
+    DMat S1;
+    RngKey key0{GEN_PHILOX4X32, 0, 0};
+    if (num_passes % 2 == 0) {
+        S.buf.alloc((size_t)n * k, ctx.stream);
+        S.rows = n;
+        S.cols = k;
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key0, n, k, S.p(), n);   // line 71
+    } else {
+        DMat G;
+        G.buf.alloc((size_t)m * k, ctx.stream);
+        G.rows = m;
+        G.cols = k;
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key0, m, k, G.p(), m);   // line 74
+        S1.buf.alloc((size_t)n * k, ctx.stream);
+        S1.rows = n;
+        S1.cols = k;
+        gemm_f64(ctx, 'T', 'N', n, k, m, 1.0, A, lda, G.p(), m, 0.0, S1.p(), n);   // line 76
+        s1_zero = false;
+        passes_done += 1;
+        // line 78-81: the stabilised copy _S2 is never used
+    }
+    int diff = num_passes - passes_done;
+    while (diff >= 2) {
+        if (s1_zero) times_zero(ctx, A, m, n, lda, k, finite, S);      // line 89
+        else {
+            S.buf.alloc((size_t)m * S1.cols, ctx.stream);
+            S.rows = m;
+            S.cols = S1.cols;
+            gemm_f64(ctx, 'N', 'N', m, S1.cols, n, 1.0, A, lda, S1.p(), n, 0.0, S.p(), m);
+        }
+        passes_done += 1;
+        if (passes_done % passes_per_stab == 0) stabilize(ctx, S);      // line 93
+        DMat T;
+        T.buf.alloc((size_t)n * S.cols, ctx.stream);
+        T.rows = n;
+        T.cols = S.cols;
+        gemm_f64(ctx, 'T', 'N', n, S.cols, m, 1.0, A, lda, S.p(), m, 0.0, T.p(), n);   // line 95
+        S = std::move(T);
+        passes_done += 1;
+        if (passes_done % passes_per_stab == 0) stabilize(ctx, S);      // line 99
+        diff -= 2;
+    }
+    return S;
+}
+
+static DMat orth_of(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx) {
+    // lora_helpers.rs:131-133: Householder QR, thin Q m x min(m,n)
+    const int64_t c = m < n ? m : n;
+    DMat Q;
+    Q.rows = m;
+    Q.cols = c;
+    Q.buf.alloc((size_t)m * (c ? c : 1), ctx.stream);
+    if (c == 0) return Q;
+    DevBuf<double> W((size_t)m * n, ctx.stream), tau(c, ctx.stream);
+    copy_matrix(ctx, m, n, X, ldx, W, m);
+    // only the first c columns are factored (m < n: the trailing columns do not change Q)
+    householder_qr(ctx, W, m, c, c, m, tau);
+    householder_form_q(ctx, W, m, c, m, tau, Q.p(), m);
+    return Q;
+}
+
+static DMat rf1_ref(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, int64_t k,
+                    bool finite) {
+    DMat S = tsog1_ref(ctx, A, m, n, lda, k, 2, 1, finite);          // line 40
+    DevBuf<double> Y((size_t)m * S.cols, ctx.stream);
+    gemm_f64(ctx, 'N', 'N', m, S.cols, n, 1.0, A, lda, S.p(), S.rows, 0.0, Y, m);   // line 41
+    return orth_of(ctx, Y, m, S.cols, m);                                            // line 42
+}
+
+// ---------------------------------------------------------------------------
+// Shared helpers for the randomized drivers
+// ---------------------------------------------------------------------------
+// C (MM x NN) = X^T Y with X (K x MM), Y (K x NN) in the requested precision.
+static void product_tn(Ctx& ctx, int prec, const double* X, int64_t K, int64_t MM, int64_t ldx,
+                       const double* Y, int64_t NN, int64_t ldy, int dx, int dy, double* C,
+                       int64_t ldc) {
+    if (prec == RNLA_PREC_FP64) gemm_f64(ctx, 'T', 'N', MM, NN, K, 1.0, X, ldx, Y, ldy, 0.0, C, ldc);
+    else tc_gemm_tn(ctx, X, K, MM, ldx, Y, NN, ldy, dx, dy, C, ldc);
+}
+
+struct SvdOut {
+    int64_t r = 0;
+};
+
+// SVD finish of lora_drivers.rs:51-68 from Q (m x cq) and B (cq x n).
+static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_t cq, const double* B,
+                          int64_t n, int64_t k, double* U, int64_t ldu, double* sig, double* Vt,
+                          int64_t ldvt) {
+    const int64_t r = k < cq ? k : cq;
+    const int64_t t = cq < n ? cq : n;
+    DevBuf<double> UB((size_t)cq * t, ctx.stream), VB((size_t)n * t, ctx.stream), sg(t, ctx.stream);
+    small_svd(ctx, B, cq, n, cq, UB, cq, sg, VB, n);
+    // U = Q U_B[:, :r]
+    gemm_f64(ctx, 'N', 'N', m, r, cq, 1.0, Q, m, UB, cq, 0.0, U, ldu);
+    (void)prec;
+    RNLA_CUDA(cudaMemcpyAsync(sig, sg.get(), r * sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
+    transpose(ctx, n, r, VB, n, Vt, ldvt);
+    return r;
+}
+
+static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
+                             int64_t k, double epsilon, int64_t s, const rnla_options& o, double* U,
+                             int64_t ldu, double* sig, double* Vt, int64_t ldvt, rnla_stats* st) {
+    if (k == 0) {
+        char b[96];
+        snprintf(b, sizeof b, "Rank k must be positive, current input is %lld", (long long)k);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (!(epsilon > 0.0)) {
+        char b[96];
+        snprintf(b, sizeof b, "Epsilon must be positive, current input is %g", epsilon);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (s == 0) {
+        char b[112];
+        snprintf(b, sizeof b, "Oversampling parameter s must be positive, current input is %lld",
+                 (long long)s);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (k < 0 || s < 0) fail(RNLA_ERR_NEGATIVE_DIMENSIONS, "k and s must be non-negative");
+    if (m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    StageTimer tm(ctx.stream);
+    tm.mark();
+    // A as double (stored-FP32 inputs are widened once for the FP64 products)
+    DevBuf<double> Aw;
+    const double* A = static_cast<const double*>(Av);
+    int64_t ld = lda;
+    if (a_f32) {
+        Aw.alloc((size_t)m * n, ctx.stream);
+        copy_matrix_f32_to_f64(ctx, m, n, static_cast<const float*>(Av), lda, Aw, m);
+        A = Aw.get();
+        ld = m;
+    }
+    int64_t r = 0;
+    int fallbacks = 0;
+    if (o.mode == RNLA_MODE_REFERENCE) {
+        if (o.precision != RNLA_PREC_FP64)
+            fail(RNLA_ERR_UNSUPPORTED, "reference mode runs in FP64 only");
+        const bool finite = all_finite(ctx, m, n, A, ld);
+        DMat Q = rf1_ref(ctx, A, m, n, ld, k + s, finite);                 // QB1 line 20
+        tm.mark();
+        const int64_t cq = Q.cols;
+        DevBuf<double> B((size_t)cq * n, ctx.stream);
+        gemm_f64(ctx, 'T', 'N', cq, n, m, 1.0, Q.p(), m, A, ld, 0.0, B, cq);   // QB1 line 21
+        tm.mark();
+        r = svd_finish(ctx, o.precision, Q.p(), m, cq, B, n, k, U, ldu, sig, Vt, ldvt);
+    } else {
+        // Gaussian range finder, q power iterations, re-orthonormalised after every product
+        int64_t l = k + s;
+        const int64_t mn = m < n ? m : n;
+        if (l > mn) l = mn;
+        const int prec = o.precision;
+        if (prec != RNLA_PREC_FP64 && !tc_available(ctx))
+            fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
+        const RngKey key = key_of(&o.rng);
+        DevBuf<double> Y((size_t)m * l, ctx.stream), Z((size_t)n * l, ctx.stream);
+        const bool force_hh = (o.orth == 1);
+        if (prec == RNLA_PREC_FP64) {
+            DevBuf<double> Om((size_t)n * l, ctx.stream);
+            sketch_fill_f64(ctx, DIST_GAUSSIAN, key, n, l, Om, n);
+            gemm_f64(ctx, 'N', 'N', m, l, n, 1.0, A, ld, Om, n, 0.0, Y, m);
+        } else {
+            // Y = A Omega = (Omega^T A^T)^T: the sketch kernel applies Omega^T (l x n) to A^T
+            DevBuf<double> At((size_t)n * m, ctx.stream), Yt((size_t)l * m, ctx.stream);
+            transpose(ctx, m, n, A, ld, At, n);
+            tc_sketch_apply(ctx, key, At, false, n, m, n, l, o.digits_a, Yt, l);
+            transpose(ctx, l, m, Yt, l, Y, m);
+        }
+        fallbacks += orthonormalize(ctx, Y, m, l, m, force_hh);
+        for (int it = 0; it < o.power_iters; ++it) {
+            product_tn(ctx, prec, A, m, n, ld, Y, l, m, o.digits_a, o.digits_b, Z, n);   // Z = A^T Q
+            fallbacks += orthonormalize(ctx, Z, n, l, n, force_hh);
+            if (prec == RNLA_PREC_FP64) gemm_f64(ctx, 'N', 'N', m, l, n, 1.0, A, ld, Z, n, 0.0, Y, m);
+            else {
+                DevBuf<double> At((size_t)n * m, ctx.stream), Yt((size_t)l * m, ctx.stream);
+                transpose(ctx, m, n, A, ld, At, n);
+                product_tn(ctx, prec, Z, n, l, n, At, m, n, o.digits_b, o.digits_a, Yt, l);
+                transpose(ctx, l, m, Yt, l, Y, m);
+            }
+            fallbacks += orthonormalize(ctx, Y, m, l, m, force_hh);
+        }
+        tm.mark();
+        DevBuf<double> B((size_t)l * n, ctx.stream);
+        product_tn(ctx, prec, Y, m, l, m, A, n, ld, o.digits_b, o.digits_a, B, l);   // B = Q^T A
+        tm.mark();
+        r = svd_finish(ctx, prec, Y, m, l, B, n, k, U, ldu, sig, Vt, ldvt);
+    }
+    tm.mark();
+    if (st) {
+        st->rank = r;
+        st->orth_fallbacks = fallbacks;
+        st->precision_used = o.precision;
+        st->ms_sketch = tm.ms(0, 1);
+        st->ms_factor = tm.ms(1, 2);
+        st->ms_solve = tm.ms(2, 3);
+        st->ms_total = tm.ms(0, 3);
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// blendenpik (sketch_and_precondition.rs:26-59)
+// ---------------------------------------------------------------------------
+static int64_t sketch_rows(int64_t m, int64_t n, double sf) {
+    return (sf * (double)n > (double)m) ? m : (int64_t)std::floor(sf * (double)n);   // line 49
+}
+
+static void blendenpik_validate(int64_t m, int64_t n, double epsilon, int64_t l, double sf) {
+    char b[160];
+    if (m < n) {
+        snprintf(b, sizeof b, "Need more columns than rows, found %lld rows and %lld columns",
+                 (long long)m, (long long)n);
+        fail(RNLA_ERR_NOT_OVERDETERMINED, b);
+    }
+    if (sf < 1.0) {
+        snprintf(b, sizeof b, "Sampling factor must be greater than 1, current input is %g", sf);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (!(epsilon > 0.0)) {
+        snprintf(b, sizeof b, "Epsilon must be positive, current input is %g", epsilon);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (l == 0) {
+        snprintf(b, sizeof b, "Number of iterations must be positive, current input is %lld",
+                 (long long)l);
+        fail(RNLA_ERR_INVALID_PARAMETERS, b);
+    }
+    if (l < 0) fail(RNLA_ERR_NEGATIVE_DIMENSIONS, "l must be positive");
+    if (n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must have at least one column");
+}
+
+static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
+                            const double* b, double epsilon, int64_t l, double sf,
+                            const rnla_options& o, double* x, rnla_stats* st) {
+    blendenpik_validate(m, n, epsilon, l, sf);
+    const int64_t d = sketch_rows(m, n, sf);
+    if (d < n) fail(RNLA_ERR_SINGULAR_MATRIX, "sketch has fewer rows than columns");
+    StageTimer tm(ctx.stream);
+    tm.mark();
+    const RngKey key = key_of(&o.rng);
+    const int64_t nc = n + 1;
+    DevBuf<double> SK((size_t)d * nc, ctx.stream);
+    if (o.precision == RNLA_PREC_FP64) {
+        // the reference's data flow: dense S (line 50), S a and S b (lines 51-52)
+        DevBuf<double> S((size_t)d * m, ctx.stream);
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key, d, m, S, d);
+        DevBuf<double> Aw;
+        const double* A = static_cast<const double*>(Av);
+        int64_t ld = lda;
+        if (a_f32) {
+            Aw.alloc((size_t)m * n, ctx.stream);
+            copy_matrix_f32_to_f64(ctx, m, n, static_cast<const float*>(Av), lda, Aw, m);
+            A = Aw.get();
+            ld = m;
+        }
+        gemm_f64(ctx, 'N', 'N', d, n, m, 1.0, S, d, A, ld, 0.0, SK, d);
+        gemm_f64(ctx, 'N', 'N', d, 1, m, 1.0, S, d, b, m, 0.0, SK.get() + n * d, d);
+    } else {
+        if (!tc_available(ctx))
+            fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, d, o.digits_a, SK, d);
+        tc_sketch_apply(ctx, key, b, false, m, 1, m, d, 0, SK.get() + n * d, d);
+    }
+    tm.mark();
+    // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
+    DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
+    householder_qr(ctx, SK, d, n, nc, d, tau);
+    if (!upper_inverse(ctx, SK, n, d, Mi, n))                       // line 55
+        fail(RNLA_ERR_SINGULAR_MATRIX, "the R factor of the sketch is singular");
+    tm.mark();
+    const double* z0 = SK.get() + n * d;
+    DevBuf<double> z(n, ctx.stream);
+    const double* a64 = a_f32 ? nullptr : static_cast<const double*>(Av);
+    const float* a32 = a_f32 ? static_cast<const float*>(Av) : nullptr;
+    int64_t iters = 0, istop = 0;
+    LsqrResult lr;
+    if (o.inner_solver == RNLA_SOLVER_CGLS) {
+        bool conv = false;
+        iters = cgls_solve(ctx, a64, a32, m, n, lda, Mi, b, z0, epsilon, l, z, &conv);   // line 57
+        istop = conv ? 1 : 0;
+    } else {
+        LsqrParams p;
+        p.atol = o.atol;
+        p.btol = o.btol;
+        p.conlim = o.conlim > 0 ? o.conlim : 1e8;
+        p.iter_lim = l;
+        if (o.atol == 0.0 && o.btol == 0.0) p.abs_arnorm_tol = epsilon;
+        lr = lsqr_solve(ctx, a64, a32, m, n, lda, Mi, b, z0, p, z, nullptr, nullptr,
+                        o.precision != RNLA_PREC_FP64);
+        iters = lr.itn;
+        istop = lr.istop;
+    }
+    trmv_upper(ctx, Mi, n, n, z, x);                                // line 58
+    tm.mark();
+    if (st) {
+        st->iterations = iters;
+        st->istop = istop;
+        st->r1norm = lr.r1norm;
+        st->r2norm = lr.r2norm;
+        st->anorm = lr.anorm;
+        st->acond = lr.acond;
+        st->arnorm = lr.arnorm;
+        st->xnorm = lr.xnorm;
+        st->sketch_rows = d;
+        st->precision_used = o.precision;
+        st->ms_sketch = tm.ms(0, 1);
+        st->ms_factor = tm.ms(1, 2);
+        st->ms_solve = tm.ms(2, 3);
+        st->ms_total = tm.ms(0, 3);
+    }
+}
+
+}  // namespace rnla
+
+using namespace rnla;
+
+extern "C" {
+
+// ---- solvers.rs ----
+int rnla_solve_upper_triangular_system_dev(const double* u, int64_t n, int64_t ldu, const double* y,
+                                           double* x, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(n, n, ldu);
+    Ctx ctx((cudaStream_t)stream);
+    upper_solve_skip_zero(ctx, u, n, ldu, y, x);
+    RNLA_API_END
+}
+
+int rnla_solve_upper_triangular_system(const double* u, int64_t n, int64_t ldu, const double* y,
+                                       double* x) {
+    RNLA_API_BEGIN
+    check_mat(n, n, ldu);
+    if (n == 0) return abi_ok();
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> U((size_t)n * n, s), Y(n, s), X(n, s);
+    h2d_matrix(U, n, u, ldu, n, n, s);
+    RNLA_CUDA(cudaMemcpyAsync(Y.get(), y, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    upper_solve_skip_zero(ctx, U, n, n, Y, X);
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_lsqr_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda, const double* b_dev,
+                  double damp, double atol, double btol, double conlim, int64_t iter_lim,
+                  int32_t calc_var, const double* x0_dev, double* x_dev, rnla_lsqr_result* result,
+                  double* arnorms_host, double* var_dev, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    Ctx ctx((cudaStream_t)stream);
+    LsqrParams p;
+    p.damp = damp;
+    p.atol = atol;
+    p.btol = btol;
+    p.conlim = conlim;
+    p.iter_lim = iter_lim < 0 ? 2 * n : iter_lim;
+    p.calc_var = calc_var != 0;
+    DevBuf<double> arn(p.iter_lim > 0 ? p.iter_lim : 1, ctx.stream);
+    LsqrResult r = lsqr_solve(ctx, a_dev, nullptr, m, n, lda, nullptr, b_dev, x0_dev, p, x_dev,
+                              var_dev, arn, false);
+    if (result) {
+        result->istop = r.istop;
+        result->itn = r.itn;
+        result->r1norm = r.r1norm;
+        result->r2norm = r.r2norm;
+        result->anorm = r.anorm;
+        result->acond = r.acond;
+        result->xnorm = r.xnorm;
+    }
+    if (arnorms_host) {
+        const int64_t cnt = r.itn > 0 ? r.itn : 1;
+        RNLA_CUDA(cudaMemcpyAsync(arnorms_host, arn.get(), cnt * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx.stream));
+        RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    }
+    RNLA_API_END
+}
+
+int rnla_lsqr(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double damp,
+              double atol, double btol, double conlim, int64_t iter_lim, int32_t calc_var,
+              const double* x0, double* x, rnla_lsqr_result* result, double* arnorms, double* var) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), B(m, s), X0(n, s), X(n, s), V(n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (x0) RNLA_CUDA(cudaMemcpyAsync(X0.get(), x0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int rc = rnla_lsqr_dev(A, m, n, m, B, damp, atol, btol, conlim, iter_lim, calc_var,
+                           x0 ? X0.get() : nullptr, X, result, arnorms, (calc_var && var) ? V.get() : nullptr, s);
+    if (rc != RNLA_OK) return rc;
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (calc_var && var) RNLA_CUDA(cudaMemcpyAsync(var, V.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+// ---- cg.rs ----
+int rnla_cgls_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda, const double* b_dev,
+                  double tolerance, int64_t num_iterations, const double* x0_dev, double* x_dev,
+                  int64_t* iterations_out, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    if (num_iterations < 0) fail(RNLA_ERR_NEGATIVE_DIMENSIONS, "num_iterations must be >= 0");
+    Ctx ctx((cudaStream_t)stream);
+    bool conv = false;
+    const int64_t it = cgls_solve(ctx, a_dev, nullptr, m, n, lda, nullptr, b_dev, x0_dev, tolerance,
+                                  num_iterations, x_dev, &conv);
+    if (iterations_out) *iterations_out = it;
+    RNLA_API_END
+}
+
+int rnla_cgls(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double tolerance,
+              int64_t num_iterations, const double* x0, double* x, int64_t* iterations_out) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), B(m, s), X0(n, s), X(n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (x0) RNLA_CUDA(cudaMemcpyAsync(X0.get(), x0, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    int rc = rnla_cgls_dev(A, m, n, m, B, tolerance, num_iterations, x0 ? X0.get() : nullptr, X,
+                           iterations_out, s);
+    if (rc != RNLA_OK) return rc;
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+// ---- lora_helpers.rs ----
+int rnla_orth(const double* x, int64_t m, int64_t n, int64_t ldx, double* q, int64_t ldq) {
+    RNLA_API_BEGIN
+    check_mat(m, n, ldx);
+    const int64_t c = m < n ? m : n;
+    if (c == 0) return abi_ok();
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> X((size_t)m * n, s);
+    h2d_matrix(X, m, x, ldx, m, n, s);
+    DMat Q = orth_of(ctx, X, m, n, m);
+    d2h_matrix(q, ldq, Q.p(), m, m, c, s);
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_stabilizer(const double* x, int64_t m, int64_t n, int64_t ldx, double* l, int64_t ldl) {
+    RNLA_API_BEGIN
+    check_mat(m, n, ldx);
+    const int64_t c = m < n ? m : n;
+    if (c == 0) return abi_ok();
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> X((size_t)m * n, s), L((size_t)m * c, s);
+    h2d_matrix(X, m, x, ldx, m, n, s);
+    full_piv_lu_l(ctx, X, m, n, m, L, m);
+    d2h_matrix(l, ldl, L, m, m, c, s);
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_tsog1(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, int32_t num_passes,
+               int32_t passes_per_stab, double* sk, int64_t lds, int64_t* cols_out) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0 || k <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty input");
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> A((size_t)m * n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    const bool finite = all_finite(ctx, m, n, A, m);
+    DMat S = tsog1_ref(ctx, A, m, n, m, k, num_passes, passes_per_stab, finite);
+    d2h_matrix(sk, lds, S.p(), S.rows, S.rows, S.cols, s);
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    if (cols_out) *cols_out = S.cols;
+    RNLA_API_END
+}
+
+int rnla_rf1(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double* q, int64_t ldq,
+             int64_t* cols_out) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0 || k <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty input");
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> A((size_t)m * n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    const bool finite = all_finite(ctx, m, n, A, m);
+    DMat Q = rf1_ref(ctx, A, m, n, m, k, finite);
+    d2h_matrix(q, ldq, Q.p(), m, m, Q.cols, s);
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    if (cols_out) *cols_out = Q.cols;
+    RNLA_API_END
+}
+
+int rnla_qb1(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double epsilon, double* q,
+             int64_t ldq, double* bq, int64_t ldb, int64_t* cols_out) {
+    RNLA_API_BEGIN
+    (void)epsilon;   // lora_helpers.rs:18
+    check_mat(m, n, lda);
+    if (m == 0 || n == 0 || k <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty input");
+    cudaStream_t s = host_stream();
+    Ctx ctx(s);
+    DevBuf<double> A((size_t)m * n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    const bool finite = all_finite(ctx, m, n, A, m);
+    DMat Q = rf1_ref(ctx, A, m, n, m, k, finite);
+    const int64_t c = Q.cols;
+    DevBuf<double> B((size_t)c * n, s);
+    gemm_f64(ctx, 'T', 'N', c, n, m, 1.0, Q.p(), m, A, m, 0.0, B, c);
+    d2h_matrix(q, ldq, Q.p(), m, m, c, s);
+    d2h_matrix(bq, ldb, B, c, c, n, s);
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    if (cols_out) *cols_out = c;
+    RNLA_API_END
+}
+
+// ---- lora_drivers.rs ----
+int64_t rnla_rand_svd_rank(int64_t m, int64_t n, int64_t k, int64_t s, int32_t mode) {
+    if (k <= 0 || s < 0 || m <= 0 || n <= 0) return 0;
+    int64_t l = k + s;
+    int64_t c = m < n ? m : n;
+    if (l < c) c = l;
+    (void)mode;
+    return k < c ? k : c;
+}
+
+int rnla_rand_svd_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n, int64_t lda,
+                      int64_t k, double epsilon, int64_t s, const rnla_options* opt, double* u_dev,
+                      int64_t ldu, double* singular_values_dev, double* vt_dev, int64_t ldvt,
+                      int64_t* r_out, rnla_stats* stats, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    Ctx ctx((cudaStream_t)stream);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    const int64_t r = rand_svd_impl(ctx, a_dev, a_is_f32 != 0, m, n, lda, k, epsilon, s, o, u_dev, ldu,
+                                    singular_values_dev, vt_dev, ldvt, stats);
+    if (r_out) *r_out = r;
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_API_END
+}
+
+int rnla_rand_svd_ex(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double epsilon,
+                     int64_t s, const rnla_options* opt, double* u, int64_t ldu, double* sigma,
+                     int64_t lds, double* vt, int64_t ldvt, int64_t* r_out, rnla_stats* stats) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    cudaStream_t st = host_stream();
+    Ctx ctx(st);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    const int64_t rmax = rnla_rand_svd_rank(m, n, k, s, o.mode);
+    DevBuf<double> A((size_t)m * n, st), U((size_t)m * (rmax ? rmax : 1), st),
+        Sg(rmax ? rmax : 1, st), Vt((size_t)(rmax ? rmax : 1) * n, st);
+    h2d_matrix(A, m, a, lda, m, n, st);
+    const int64_t r = rand_svd_impl(ctx, A, false, m, n, m, k, epsilon, s, o, U, m, Sg, Vt,
+                                    rmax ? rmax : 1, stats);
+    std::vector<double> sg(r > 0 ? r : 1);
+    d2h_matrix(u, ldu, U, m, m, r, st);
+    d2h_matrix(vt, ldvt, Vt, rmax ? rmax : 1, r, n, st);
+    if (r > 0) RNLA_CUDA(cudaMemcpyAsync(sg.data(), Sg.get(), r * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RNLA_CUDA(cudaStreamSynchronize(st));
+    // S is the r x r diagonal matrix of lora_drivers.rs:64
+    for (int64_t j = 0; j < r; ++j)
+        for (int64_t i = 0; i < r; ++i) sigma[i + j * lds] = (i == j) ? sg[i] : 0.0;
+    if (r_out) *r_out = r;
+    RNLA_API_END
+}
+
+int rnla_rand_svd(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double epsilon,
+                  int64_t s, double* u, int64_t ldu, double* sigma, int64_t lds, double* vt,
+                  int64_t ldvt, int64_t* r_out) {
+    return rnla_rand_svd_ex(a, m, n, lda, k, epsilon, s, nullptr, u, ldu, sigma, lds, vt, ldvt, r_out,
+                            nullptr);
+}
+
+// ---- sketch_and_precondition.rs ----
+int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n,
+                                       int64_t lda, const double* b_dev, double epsilon, int64_t l,
+                                       double sampling_factor, const rnla_options* opt,
+                                       double* x_dev, rnla_stats* stats, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    Ctx ctx((cudaStream_t)stream);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    blendenpik_impl(ctx, a_dev, a_is_f32 != 0, m, n, lda, b_dev, epsilon, l, sampling_factor, o, x_dev,
+                    stats);
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_API_END
+}
+
+int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda,
+                                      const double* b, double epsilon, int64_t l,
+                                      double sampling_factor, const rnla_options* opt, double* x,
+                                      rnla_stats* stats) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    blendenpik_validate(m, n, epsilon, l, sampling_factor);
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    int rc = rnla_blendenpik_overdetermined_dev(A, 0, m, n, m, B, epsilon, l, sampling_factor, opt, X,
+                                                stats, s);
+    if (rc != RNLA_OK) return rc;
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_blendenpik_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                                   double epsilon, int64_t l, double sampling_factor, double* x) {
+    return rnla_blendenpik_overdetermined_ex(a, m, n, lda, b, epsilon, l, sampling_factor, nullptr, x,
+                                             nullptr);
+}
+
+// ---- building blocks ----
+int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
+                          int64_t d, const rnla_rng* rng, int32_t precision, int32_t digits,
+                          double* y_dev, int64_t ldy, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, ldx);
+    if (d <= 0 || m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty sketch product");
+    Ctx ctx((cudaStream_t)stream);
+    const RngKey key = key_of(rng);
+    if (precision == RNLA_PREC_FP64) {
+        DevBuf<double> S((size_t)d * m, ctx.stream);
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key, d, m, S, d);
+        DevBuf<double> Xw;
+        const double* X = static_cast<const double*>(x_dev);
+        int64_t ld = ldx;
+        if (x_is_f32) {
+            Xw.alloc((size_t)m * n, ctx.stream);
+            copy_matrix_f32_to_f64(ctx, m, n, static_cast<const float*>(x_dev), ldx, Xw, m);
+            X = Xw.get();
+            ld = m;
+        }
+        gemm_f64(ctx, 'N', 'N', d, n, m, 1.0, S, d, X, ld, 0.0, y_dev, ldy);
+    } else {
+        if (!tc_available(ctx)) fail(RNLA_ERR_UNSUPPORTED, "sm_103a tensor-core kernels unavailable");
+        tc_sketch_apply(ctx, key, x_dev, x_is_f32 != 0, m, n, ldx, d, digits, y_dev, ldy);
+    }
+    RNLA_API_END
+}
+
+int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, const double* y_dev,
+                     int64_t nn, int64_t ldy, int32_t precision, int32_t digits_x, int32_t digits_y,
+                     double* c_dev, int64_t ldc, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(k, mm, ldx);
+    check_mat(k, nn, ldy);
+    Ctx ctx((cudaStream_t)stream);
+    if (precision != RNLA_PREC_FP64 && !tc_available(ctx))
+        fail(RNLA_ERR_UNSUPPORTED, "sm_103a tensor-core kernels unavailable");
+    product_tn(ctx, precision, x_dev, k, mm, ldx, y_dev, nn, ldy, digits_x, digits_y, c_dev, ldc);
+    RNLA_API_END
+}
+
+}  // extern "C"

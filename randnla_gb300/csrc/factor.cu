@@ -1,0 +1,530 @@
+// Dense FP64 factorizations used by the hot path:
+//   * Householder QR (lora_helpers.rs:132 `qr().q()`; sketch_and_precondition.rs:53)
+//   * triangular inverse / solves (sketch_and_precondition.rs:55; solvers.rs:22-41)
+//   * Cholesky and CholeskyQR2 with a Householder fallback (range basis)
+//   * complete-pivoting LU, L factor only (lora_helpers.rs:144-146)
+//   * one-sided Jacobi SVD of a small matrix (lora_drivers.rs:53 `B.svd`)
+// All run on the GPU in FP64.
+#include "rnla_internal.h"
+#include <vector>
+
+namespace rnla {
+
+// ---------------------------------------------------------------------------
+// Householder QR, one launch per column.  Launch t applies reflector t-1 to
+// every column j >= t and, in the CTA that owns column t, builds reflector t
+// (LAPACK dlarfg convention: tau = 0 when the sub-column is exactly zero).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) hh_step_kernel(double* __restrict__ X, int64_t m, int64_t n,
+                                                      int64_t ld, int64_t t, int64_t jfirst,
+                                                      double* __restrict__ tau) {
+    __shared__ double red[8];
+    const int64_t j = jfirst + blockIdx.x;
+    double* col = X + j * ld;
+    if (t > 0) {
+        const int64_t p = t - 1;
+        const double tp = tau[p];
+        if (tp != 0.0) {
+            const double* v = X + p * ld;
+            double s = 0.0;
+            for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) s = fma(v[i], col[i], s);
+            s = block_sum(s, red) + col[p];
+            const double f = tp * s;
+            if (threadIdx.x == 0) col[p] -= f;
+            for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] = fma(-f, v[i], col[i]);
+        }
+    }
+    if (j == t && t < n) {
+        __syncthreads();
+        double s = 0.0;
+        for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) s = fma(col[i], col[i], s);
+        const double xn2 = block_sum(s, red);
+        const double alpha = col[t];
+        if (xn2 == 0.0) {
+            if (threadIdx.x == 0) tau[t] = 0.0;
+        } else {
+            const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+            const double scale = 1.0 / (alpha - beta);
+            for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] *= scale;
+            if (threadIdx.x == 0) {
+                tau[t] = (beta - alpha) / beta;
+                col[t] = beta;
+            }
+        }
+    }
+}
+
+void householder_qr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld, double* tau) {
+    if (n <= 0) return;
+    if (m < n) fail(RNLA_ERR_INVALID_DIMENSIONS, "householder_qr needs m >= n");
+    for (int64_t t = 0; t <= n; ++t) {
+        const int64_t jfirst = (t < n) ? t : n;
+        const int64_t cnt = nc - jfirst;
+        if (cnt <= 0) break;
+        hh_step_kernel<<<(unsigned)cnt, 256, 0, ctx.stream>>>(X, m, n, ld, t, jfirst, tau);
+        RNLA_LAUNCH_CHECK();
+    }
+}
+
+// Applies reflector t (stored in V) to columns j >= t of Q.
+__global__ void __launch_bounds__(256) hh_apply_kernel(const double* __restrict__ V, int64_t ldv,
+                                                       const double* __restrict__ tau, int64_t m,
+                                                       int64_t t, double* __restrict__ Q, int64_t ldq) {
+    __shared__ double red[8];
+    const double tp = tau[t];
+    if (tp == 0.0) return;
+    const int64_t j = t + blockIdx.x;
+    double* q = Q + j * ldq;
+    const double* v = V + t * ldv;
+    double s = 0.0;
+    for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) s = fma(v[i], q[i], s);
+    s = block_sum(s, red) + q[t];
+    const double f = tp * s;
+    if (threadIdx.x == 0) q[t] -= f;
+    for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) q[i] = fma(-f, v[i], q[i]);
+}
+
+void householder_form_q(Ctx& ctx, const double* V, int64_t m, int64_t n, int64_t ldv,
+                        const double* tau, double* Q, int64_t ldq) {
+    fill_identity(ctx, m, n, Q, ldq);
+    for (int64_t t = n - 1; t >= 0; --t) {
+        hh_apply_kernel<<<(unsigned)(n - t), 256, 0, ctx.stream>>>(V, ldv, tau, m, t, Q, ldq);
+        RNLA_LAUNCH_CHECK();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Triangular inverse and solves (column-oriented back substitution)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) upper_inverse_kernel(const double* __restrict__ R, int64_t n,
+                                                            int64_t ldr, double* __restrict__ Ri,
+                                                            int64_t ldi, unsigned int* status) {
+    extern __shared__ double b[];
+    const int64_t j = blockIdx.x;
+    for (int64_t i = threadIdx.x; i <= j; i += blockDim.x) b[i] = (i == j) ? 1.0 : 0.0;
+    __shared__ double xi_s;
+    __syncthreads();
+    for (int64_t i = j; i >= 0; --i) {
+        if (threadIdx.x == 0) {
+            const double d = R[i + i * ldr];
+            if (d == 0.0) atomicCAS(status, 0u, (unsigned int)KSTATUS_SINGULAR);
+            xi_s = b[i] / d;
+            b[i] = xi_s;
+        }
+        __syncthreads();
+        const double xi = xi_s;
+        const double* rc = R + i * ldr;
+        for (int64_t r = threadIdx.x; r < i; r += blockDim.x) b[r] = fma(-xi, rc[r], b[r]);
+        __syncthreads();
+    }
+    double* out = Ri + j * ldi;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) out[i] = (i <= j) ? b[i] : 0.0;
+}
+
+bool upper_inverse(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi) {
+    if (n <= 0) return true;
+    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+    const size_t smem = (size_t)n * sizeof(double);
+    if (smem > 48 * 1024)
+        RNLA_CUDA(cudaFuncSetAttribute(upper_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    upper_inverse_kernel<<<(unsigned)n, 256, smem, ctx.stream>>>(R, n, ldr, Rinv, ldi, ctx.status);
+    RNLA_LAUNCH_CHECK();
+    unsigned int h = 0;
+    RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+    return h == 0;
+}
+
+// solvers.rs:22-41: x_i = (y_i - sum_{j>i} u_ij x_j) / u_ii, skipped (x_i = 0) when u_ii == 0.
+__global__ void __launch_bounds__(256) upper_solve_skip_kernel(const double* __restrict__ U, int64_t n,
+                                                               int64_t ldu, const double* __restrict__ y,
+                                                               double* __restrict__ x) {
+    extern __shared__ double b[];
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) b[i] = y[i];
+    __shared__ double xi_s;
+    __syncthreads();
+    for (int64_t i = n - 1; i >= 0; --i) {
+        if (threadIdx.x == 0) {
+            const double d = U[i + i * ldu];
+            xi_s = (d != 0.0) ? b[i] / d : 0.0;
+            b[i] = xi_s;
+        }
+        __syncthreads();
+        const double xi = xi_s;
+        if (xi != 0.0) {
+            const double* uc = U + i * ldu;
+            for (int64_t r = threadIdx.x; r < i; r += blockDim.x) b[r] = fma(-xi, uc[r], b[r]);
+        }
+        __syncthreads();
+    }
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) x[i] = b[i];
+}
+
+void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, const double* y,
+                           double* x) {
+    if (n <= 0) return;
+    const size_t smem = (size_t)n * sizeof(double);
+    if (smem > 48 * 1024)
+        RNLA_CUDA(cudaFuncSetAttribute(upper_solve_skip_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    upper_solve_skip_kernel<<<1, 256, smem, ctx.stream>>>(U, n, ldu, y, x);
+    RNLA_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Cholesky (right-looking, one CTA): G = R^T R, R upper, written in place.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) cholesky_kernel(double* __restrict__ G, int64_t n, int64_t ld,
+                                                        unsigned int* status) {
+    __shared__ double rkk_s;
+    __shared__ int bad_s;
+    if (threadIdx.x == 0) bad_s = 0;
+    for (int64_t k = 0; k < n; ++k) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double d = G[k + k * ld];
+            if (!(d > 0.0)) {
+                bad_s = 1;
+                atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);
+            }
+            rkk_s = sqrt(d);
+            G[k + k * ld] = rkk_s;
+        }
+        __syncthreads();
+        if (bad_s) return;
+        const double rkk = rkk_s;
+        for (int64_t j = k + 1 + threadIdx.x; j < n; j += blockDim.x) G[k + j * ld] /= rkk;
+        __syncthreads();
+        // trailing update of the upper triangle: G[i][j] -= R[k][i] R[k][j], k < i <= j
+        const int64_t w = n - k - 1;
+        const int64_t tot = w * w;
+        for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int64_t ii = k + 1 + e % w, jj = k + 1 + e / w;
+            if (ii <= jj) G[ii + jj * ld] = fma(-G[k + ii * ld], G[k + jj * ld], G[ii + jj * ld]);
+        }
+    }
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < n * n; e += blockDim.x) {
+        const int64_t i = e % n, j = e / n;
+        if (i > j) G[i + j * ld] = 0.0;
+    }
+}
+
+bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld) {
+    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+    cholesky_kernel<<<1, 1024, 0, ctx.stream>>>(G, n, ld, ctx.status);
+    RNLA_LAUNCH_CHECK();
+    unsigned int h = 0;
+    RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+    return h == 0;
+}
+
+// ---------------------------------------------------------------------------
+// Orthonormal basis: CholeskyQR2, Householder fallback
+// ---------------------------------------------------------------------------
+static void householder_orth_inplace(Ctx& ctx, double* Y, int64_t m, int64_t n, int64_t ld) {
+    DevBuf<double> tau(n, ctx.stream), Q((size_t)m * n, ctx.stream);
+    householder_qr(ctx, Y, m, n, n, ld, tau);
+    householder_form_q(ctx, Y, m, n, ld, tau, Q, m);
+    copy_matrix(ctx, m, n, Q, m, Y, ld);
+}
+
+int orthonormalize(Ctx& ctx, double* Y, int64_t m, int64_t n, int64_t ld, bool force_householder) {
+    if (m <= 0 || n <= 0) return 0;
+    if (force_householder || m < n) {
+        householder_orth_inplace(ctx, Y, m, n, ld);
+        return 0;
+    }
+    DevBuf<double> G((size_t)n * n, ctx.stream), Ri((size_t)n * n, ctx.stream),
+        T((size_t)m * n, ctx.stream);
+    for (int pass = 0; pass < 2; ++pass) {
+        gemm_f64(ctx, 'T', 'N', n, n, m, 1.0, Y, ld, Y, ld, 0.0, G, n);
+        if (!cholesky_upper(ctx, G, n, n) || !upper_inverse(ctx, G, n, n, Ri, n)) {
+            householder_orth_inplace(ctx, Y, m, n, ld);
+            return 1;
+        }
+        gemm_f64(ctx, 'N', 'N', m, n, n, 1.0, Y, ld, Ri, n, 0.0, T, m);
+        copy_matrix(ctx, m, n, T, m, Y, ld);
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Complete-pivoting LU (one CTA), L only.  Arithmetic uses explicitly
+// rounded operations (no contraction) so the pivot sequence is exactly that
+// of a scalar restatement of the same algorithm.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) full_piv_lu_kernel(double* __restrict__ W, int64_t m, int64_t n,
+                                                           int64_t ld) {
+    __shared__ double bv[32];
+    __shared__ long long bi[32];
+    __shared__ long long piv_s;
+    __shared__ double pval_s;
+    const int64_t p = m < n ? m : n;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t k = 0; k < p; ++k) {
+        const int64_t rows = m - k, cols = n - k, tot = rows * cols;
+        double best = -1.0;
+        long long bidx = 0x7fffffffffffffffLL;
+        for (int64_t e = threadIdx.x; e < tot; e += blockDim.x) {
+            const int64_t i = k + e % rows, j = k + e / rows;
+            const double a = fabs(W[i + j * ld]);
+            if (a > best) { best = a; bidx = e; }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+            const long long oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+            if (ov > best || (ov == best && oi < bidx)) { best = ov; bidx = oi; }
+        }
+        if (lane == 0) { bv[wid] = best; bi[wid] = bidx; }
+        __syncthreads();
+        if (wid == 0) {
+            best = lane < nw ? bv[lane] : -1.0;
+            bidx = lane < nw ? bi[lane] : 0x7fffffffffffffffLL;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+                const long long oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+                if (ov > best || (ov == best && oi < bidx)) { best = ov; bidx = oi; }
+            }
+            if (lane == 0) { piv_s = bidx; pval_s = best; }
+        }
+        __syncthreads();
+        if (pval_s == 0.0) break;   // remaining block is zero: L keeps identity columns
+        const int64_t r = k + piv_s % rows, c = k + piv_s / rows;
+        if (r != k)
+            for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+                const double t = W[k + j * ld];
+                W[k + j * ld] = W[r + j * ld];
+                W[r + j * ld] = t;
+            }
+        __syncthreads();   // the column swap below touches rows k and r too
+        if (c != k)
+            for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+                const double t = W[i + k * ld];
+                W[i + k * ld] = W[i + c * ld];
+                W[i + c * ld] = t;
+            }
+        __syncthreads();
+        const double pv = W[k + k * ld];
+        for (int64_t i = k + 1 + threadIdx.x; i < m; i += blockDim.x)
+            W[i + k * ld] = __ddiv_rn(W[i + k * ld], pv);
+        __syncthreads();
+        const int64_t tr = m - k - 1, tc = n - k - 1;
+        for (int64_t e = threadIdx.x; e < tr * tc; e += blockDim.x) {
+            const int64_t i = k + 1 + e % tr, j = k + 1 + e / tr;
+            W[i + j * ld] = __dsub_rn(W[i + j * ld], __dmul_rn(W[i + k * ld], W[k + j * ld]));
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void extract_unit_lower_kernel(const double* __restrict__ W, int64_t m, int64_t p,
+                                          int64_t ldw, double* __restrict__ L, int64_t ldl) {
+    const int64_t tot = m * p;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % m, c = e / m;
+        L[i + c * ldl] = (i > c) ? W[i + c * ldw] : (i == c ? 1.0 : 0.0);
+    }
+}
+
+void full_piv_lu_l(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx, double* L,
+                   int64_t ldl) {
+    if (m <= 0 || n <= 0) return;
+    DevBuf<double> W((size_t)m * n, ctx.stream);
+    copy_matrix(ctx, m, n, X, ldx, W, m);
+    full_piv_lu_kernel<<<1, 1024, 0, ctx.stream>>>(W, m, n, m);
+    RNLA_LAUNCH_CHECK();
+    const int64_t p = m < n ? m : n;
+    int g = div_up(m * p, 256);
+    if (g > 4096) g = 4096;
+    extract_unit_lower_kernel<<<g, 256, 0, ctx.stream>>>(W, m, p, m, L, ldl);
+    RNLA_LAUNCH_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// One-sided (Hestenes) Jacobi on a small s x s matrix W, rotations
+// accumulated into V.  One CTA; each warp takes pairs of a round-robin
+// tournament round, so the pairs of a round touch disjoint columns.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) jacobi_kernel(double* __restrict__ W, double* __restrict__ V,
+                                                      int s, int max_sweeps) {
+    __shared__ int rot_s;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int sp = (s + 1) & ~1;     // players, padded to even (a bye when s is odd)
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) rot_s = 0;
+        __syncthreads();
+        for (int round = 0; round < sp - 1; ++round) {
+            for (int pr = wid; pr < sp / 2; pr += nw) {
+                // circle method: player 0 fixed, the others rotate
+                int a, b;
+                if (pr == 0) { a = 0; b = 1 + (round % (sp - 1)); }
+                else {
+                    a = 1 + ((round + pr) % (sp - 1));
+                    b = 1 + ((round + sp - 1 - pr) % (sp - 1));
+                }
+                if (a >= s || b >= s) continue;
+                if (a > b) { const int t = a; a = b; b = t; }
+                double* wa = W + (int64_t)a * s;
+                double* wb = W + (int64_t)b * s;
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int i = lane; i < s; i += 32) {
+                    const double x = wa[i], y = wb[i];
+                    al = fma(x, x, al);
+                    be = fma(y, y, be);
+                    ga = fma(x, y, ga);
+                }
+                al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+                if (ga == 0.0 || fabs(ga) <= tol * sqrt(al * be)) continue;
+                const double zeta = (be - al) / (2.0 * ga);
+                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
+                const double c = 1.0 / sqrt(fma(t, t, 1.0));
+                const double sn = c * t;
+                for (int i = lane; i < s; i += 32) {
+                    const double x = wa[i], y = wb[i];
+                    wa[i] = c * x - sn * y;
+                    wb[i] = sn * x + c * y;
+                }
+                double* va = V + (int64_t)a * s;
+                double* vb = V + (int64_t)b * s;
+                for (int i = lane; i < s; i += 32) {
+                    const double x = va[i], y = vb[i];
+                    va[i] = c * x - sn * y;
+                    vb[i] = sn * x + c * y;
+                }
+                if (lane == 0) atomicAdd(&rot_s, 1);
+            }
+            __syncthreads();
+        }
+        if (rot_s == 0) break;
+        __syncthreads();
+    }
+}
+
+// sigma_i = ||W_i||, descending order; U_R = W_i / sigma_i (zero columns
+// completed with the first coordinate vectors orthogonal to the others);
+// V columns permuted alike.  One CTA.
+__global__ void __launch_bounds__(256) jacobi_finish_kernel(const double* __restrict__ W,
+                                                            const double* __restrict__ V, int s,
+                                                            double* __restrict__ UR,
+                                                            double* __restrict__ VS,
+                                                            double* __restrict__ sigma, int* order) {
+    __shared__ double red[8];
+    extern __shared__ double nrm[];
+    for (int c = 0; c < s; ++c) {
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < s; i += blockDim.x) acc = fma(W[i + (int64_t)c * s], W[i + (int64_t)c * s], acc);
+        acc = block_sum(acc, red);
+        if (threadIdx.x == 0) nrm[c] = sqrt(acc);
+    }
+    __syncthreads();
+    // stable descending rank
+    for (int c = threadIdx.x; c < s; c += blockDim.x) {
+        int rank = 0;
+        for (int d = 0; d < s; ++d)
+            if (nrm[d] > nrm[c] || (nrm[d] == nrm[c] && d < c)) ++rank;
+        order[rank] = c;
+    }
+    __syncthreads();
+    for (int r = 0; r < s; ++r) {
+        const int c = order[r];
+        const double sg = nrm[c];
+        if (threadIdx.x == 0) sigma[r] = sg;
+        for (int i = threadIdx.x; i < s; i += blockDim.x) {
+            UR[i + (int64_t)r * s] = (sg > 0.0) ? W[i + (int64_t)c * s] / sg : 0.0;
+            VS[i + (int64_t)r * s] = V[i + (int64_t)c * s];
+        }
+    }
+    __syncthreads();
+    // complete the zero-sigma columns of UR with coordinate vectors
+    int cand = 0;
+    for (int r = 0; r < s; ++r) {
+        if (nrm[order[r]] > 0.0) continue;
+        while (cand < s) {
+            // u = e_cand - sum_q (UR_q . e_cand) UR_q over the columns already set
+            for (int i = threadIdx.x; i < s; i += blockDim.x) UR[i + (int64_t)r * s] = (i == cand) ? 1.0 : 0.0;
+            __syncthreads();
+            for (int q = 0; q < s; ++q) {
+                if (q == r) continue;
+                const bool set = (nrm[order[q]] > 0.0) || (q < r);
+                if (!set) continue;
+                double d = 0.0;
+                for (int i = threadIdx.x; i < s; i += blockDim.x)
+                    d = fma(UR[i + (int64_t)q * s], UR[i + (int64_t)r * s], d);
+                d = block_sum(d, red);
+                for (int i = threadIdx.x; i < s; i += blockDim.x)
+                    UR[i + (int64_t)r * s] = fma(-d, UR[i + (int64_t)q * s], UR[i + (int64_t)r * s]);
+                __syncthreads();
+            }
+            double nn = 0.0;
+            for (int i = threadIdx.x; i < s; i += blockDim.x)
+                nn = fma(UR[i + (int64_t)r * s], UR[i + (int64_t)r * s], nn);
+            nn = sqrt(block_sum(nn, red));
+            ++cand;
+            if (nn > 0.5) {
+                for (int i = threadIdx.x; i < s; i += blockDim.x) UR[i + (int64_t)r * s] /= nn;
+                __syncthreads();
+                break;
+            }
+        }
+    }
+}
+
+__global__ void triu_copy_kernel(const double* __restrict__ src, int64_t lds, int64_t s,
+                                 double* __restrict__ dst) {
+    const int64_t tot = s * s;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % s, j = e / s;
+        dst[e] = (i <= j) ? src[i + j * lds] : 0.0;
+    }
+}
+
+void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
+               double* sigma, double* V, int64_t ldv) {
+    const int64_t s = p < q ? p : q;
+    if (s <= 0) return;
+    const bool wide = p <= q;
+    const int64_t big = wide ? q : p;      // rows of G = B^T (wide) or B (tall)
+    DevBuf<double> G((size_t)big * s, ctx.stream), tau(s, ctx.stream), QG((size_t)big * s, ctx.stream);
+    if (wide) transpose(ctx, p, q, B, ldb, G, big);
+    else copy_matrix(ctx, p, q, B, ldb, G, big);
+    householder_qr(ctx, G, big, s, s, big, tau);
+    householder_form_q(ctx, G, big, s, big, tau, QG, big);
+    DevBuf<double> W((size_t)s * s, ctx.stream), VR((size_t)s * s, ctx.stream);
+    int g = div_up(s * s, 256);
+    if (g > 1024) g = 1024;
+    triu_copy_kernel<<<g, 256, 0, ctx.stream>>>(G, big, s, W);
+    RNLA_LAUNCH_CHECK();
+    fill_identity(ctx, s, s, VR, s);
+    // R VR = W with orthogonal columns -> R = UR diag(sigma) VR^T
+    jacobi_kernel<<<1, 1024, 0, ctx.stream>>>(W, VR, (int)s, 60);
+    RNLA_LAUNCH_CHECK();
+    DevBuf<double> UR((size_t)s * s, ctx.stream), VS((size_t)s * s, ctx.stream);
+    DevBuf<int> order(s, ctx.stream);
+    const size_t smem = (size_t)s * sizeof(double);
+    if (smem > 48 * 1024)
+        RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+    jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, VR, (int)s, UR, VS, sigma, order);
+    RNLA_LAUNCH_CHECK();
+    // G = QG R = (QG UR) diag(sigma) VS^T
+    if (wide) {
+        // B = G^T = VS diag(sigma) (QG UR)^T: U_B = VS (p x s), V_B = QG UR (q x s)
+        copy_matrix(ctx, s, s, VS, s, U, ldu);
+        gemm_f64(ctx, 'N', 'N', q, s, s, 1.0, QG, big, UR, s, 0.0, V, ldv);
+    } else {
+        gemm_f64(ctx, 'N', 'N', p, s, s, 1.0, QG, big, UR, s, 0.0, U, ldu);
+        copy_matrix(ctx, s, s, VS, s, V, ldv);
+    }
+}
+
+}  // namespace rnla

@@ -1,0 +1,185 @@
+// Shared runtime pieces of librandnla_gb300: status codes and exceptions,
+// CUDA error checks, stream-ordered device buffers, a bounded grid barrier
+// for cooperative persistent kernels, and small reduction helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <stdexcept>
+#include "../../include/randnla_gb300.h"
+
+namespace rnla {
+
+// C++ exception carried up to the C ABI, where it becomes an rnla_status
+// plus the thread-local message returned by rnla_last_error_message().
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const std::string& msg) { throw Error(code, msg); }
+
+inline void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+    if (e != cudaSuccess) {
+        char buf[512];
+        snprintf(buf, sizeof buf, "CUDA error in %s (%s:%d): %s", what, file, line,
+                 cudaGetErrorString(e));
+        throw Error(RNLA_ERR_CUDA, buf);
+    }
+}
+#define RNLA_CUDA(x) ::rnla::cuda_check((x), #x, __FILE__, __LINE__)
+#define RNLA_LAUNCH_CHECK() ::rnla::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+
+// Per-call context: stream plus device facts used for grid sizing.
+struct Ctx {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int sm_count = 0;
+    unsigned int* status = nullptr;   // device word: nonzero = kernel-side failure code
+    explicit Ctx(cudaStream_t s);
+    ~Ctx();
+    Ctx(const Ctx&) = delete;
+    Ctx& operator=(const Ctx&) = delete;
+    // Reads the device status word (synchronises the stream).
+    void check_status(const char* where);
+};
+
+// Device buffer allocated from the library's stream-ordered pool and freed
+// on the same stream when it goes out of scope.
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    DevBuf() = default;
+    DevBuf(size_t count, cudaStream_t stream) { alloc(count, stream); }
+    void alloc(size_t count, cudaStream_t stream);
+    ~DevBuf() { release(); }
+    void release();
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p; n = o.n; s = o.s;
+            o.p = nullptr; o.n = 0;
+        }
+        return *this;
+    }
+    T* get() const { return p; }
+    operator T*() const { return p; }
+};
+
+void* pool_alloc(size_t bytes, cudaStream_t s);
+void pool_free(void* p, cudaStream_t s);
+
+template <typename T>
+void DevBuf<T>::alloc(size_t count, cudaStream_t stream) {
+    release();
+    s = stream;
+    n = count;
+    p = count ? static_cast<T*>(pool_alloc(count * sizeof(T), stream)) : nullptr;
+}
+template <typename T>
+void DevBuf<T>::release() {
+    if (p) pool_free(p, s);
+    p = nullptr;
+    n = 0;
+}
+
+// Kernel-side failure codes written to Ctx::status.
+enum : unsigned int {
+    KSTATUS_OK = 0,
+    KSTATUS_BARRIER_TIMEOUT = 1,   // a grid barrier waited longer than its limit
+    KSTATUS_MBAR_TIMEOUT = 2,      // an mbarrier wait gave up
+    KSTATUS_SINGULAR = 3,          // zero pivot where the algorithm needs a nonzero one
+    KSTATUS_NOT_PD = 4,            // Cholesky met a non-positive pivot
+};
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+#ifdef __CUDACC__
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum; `red` must hold blockDim.x/32 doubles.  All threads get the result.
+__device__ __forceinline__ double block_sum(double v, double* red) {
+    v = warp_sum(v);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = (threadIdx.x < nw) ? red[threadIdx.x] : 0.0;
+    if (w == 0) t = warp_sum(t);
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    t = red[0];
+    __syncthreads();
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier for cooperative launches (all CTAs co-resident by contract
+// of cudaLaunchCooperativeKernel).  The wait is bounded: after `limit_ns`
+// it records KSTATUS_BARRIER_TIMEOUT in *status and returns false, and the
+// caller leaves the kernel.  count/gen live in device memory zeroed before
+// the launch.
+struct GridBarrier {
+    unsigned int* count;
+    unsigned int* gen;
+    unsigned int* status;
+};
+
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned long long limit_ns = 2000000000ull) {
+    __syncthreads();
+    __shared__ int ok_s;
+    if (threadIdx.x == 0) {
+        ok_s = 1;
+        const unsigned int nblocks = gridDim.x * gridDim.y * gridDim.z;
+        volatile unsigned int* vgen = b.gen;
+        const unsigned int my_gen = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(b.count, 1u);
+        if (arrived == nblocks - 1) {
+            *b.count = 0;
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int spins = 0;
+            while (*vgen == my_gen) {
+                if (*((volatile unsigned int*)b.status) != 0u) { ok_s = 0; break; }
+                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > limit_ns) {
+                    atomicCAS(b.status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+                    ok_s = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+#endif
+
+}  // namespace rnla

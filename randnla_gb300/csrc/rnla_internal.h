@@ -1,0 +1,100 @@
+// Internal interfaces between the translation units of librandnla_gb300.
+// Everything here works on device pointers, column-major storage, and is
+// enqueued on ctx.stream.
+#pragma once
+#include "rnla_common.cuh"
+#include "rnla_rng.cuh"
+
+namespace rnla {
+
+// ---- generators (rng.cu) ----
+void rng_words(Ctx& ctx, const RngKey& key, uint64_t first_word, int64_t n, uint32_t* out);
+void sketch_fill_f64(Ctx& ctx, int dist, const RngKey& key, int64_t rows, int64_t cols,
+                     double* out, int64_t ld);
+void sketch_fill_f32(Ctx& ctx, int dist, const RngKey& key, int64_t rows, int64_t cols,
+                     bool quantized, float* out, int64_t ld);
+
+// ---- dense FP64 kernels (dense.cu) ----
+// C = alpha op(A) op(B) + beta C, op(X) = X ('N') or X^T ('T'); M x N result.
+void gemm_f64(Ctx& ctx, char ta, char tb, int64_t M, int64_t N, int64_t K, double alpha,
+              const double* A, int64_t lda, const double* B, int64_t ldb, double beta,
+              double* C, int64_t ldc);
+void copy_matrix(Ctx& ctx, int64_t rows, int64_t cols, const double* src, int64_t lds,
+                 double* dst, int64_t ldd);
+void copy_matrix_f32_to_f64(Ctx& ctx, int64_t rows, int64_t cols, const float* src, int64_t lds,
+                            double* dst, int64_t ldd);
+// dst (cols x rows) = src^T
+void transpose(Ctx& ctx, int64_t rows, int64_t cols, const double* src, int64_t lds, double* dst,
+               int64_t ldd);
+void fill_identity(Ctx& ctx, int64_t rows, int64_t cols, double* dst, int64_t ld);
+void fill_zero(Ctx& ctx, int64_t rows, int64_t cols, double* dst, int64_t ld);
+// returns false if any entry is NaN or infinite (synchronises)
+bool all_finite(Ctx& ctx, int64_t rows, int64_t cols, const double* a, int64_t lda);
+
+// ---- factorizations (factor.cu) ----
+// Householder QR of the first n columns of X (m x nc, m >= n), LAPACK
+// convention (tau = 0 when the sub-column is zero).  R in the upper
+// triangle, reflectors below; columns n..nc-1 receive Q^T.  tau: n values.
+void householder_qr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld, double* tau);
+// Thin Q (m x n) from the reflectors stored in V (m x n, ld) and tau.
+void householder_form_q(Ctx& ctx, const double* V, int64_t m, int64_t n, int64_t ldv,
+                        const double* tau, double* Q, int64_t ldq);
+// Rinv (n x n, upper) = R^-1; returns false on an exactly zero pivot (synchronises).
+bool upper_inverse(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi);
+// back substitution with the reference's zero-pivot rule (solvers.rs:22-41)
+void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, const double* y,
+                           double* x);
+// Cholesky G = R^T R (upper R written to the upper triangle of G, n x n);
+// returns false if a pivot is not positive (synchronises).
+bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld);
+// Thin orthonormal basis of Y (m x n, m >= n) in place: CholeskyQR2, with a
+// Householder fallback when a Cholesky pivot fails.  Returns 1 if the
+// fallback was taken.
+int orthonormalize(Ctx& ctx, double* Y, int64_t m, int64_t n, int64_t ld, bool force_householder);
+// Unit-lower L (m x min(m,n)) of complete-pivoting LU, without P.
+void full_piv_lu_l(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx, double* L,
+                   int64_t ldl);
+// Thin SVD of B (p x q): U (p x t), sigma (t), V (q x t), t = min(p, q),
+// singular values descending; exactly-zero singular directions get the
+// first unused coordinate vectors (so SVD(0) = (I, 0, I)).
+void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U,
+               int64_t ldu, double* sigma, double* V, int64_t ldv);
+
+// ---- iterative solvers (iterative.cu) ----
+struct LsqrParams {
+    double damp = 0.0, atol = 1e-8, btol = 1e-8, conlim = 1e8;
+    int64_t iter_lim = -1;
+    bool calc_var = false;
+    double abs_arnorm_tol = 0.0;   // > 0: also stop when the ||A^T r|| estimate < this (CGLS rule)
+};
+struct LsqrResult {
+    int64_t istop = 0, itn = 0;
+    double r1norm = 0, r2norm = 0, anorm = 0, acond = 0, xnorm = 0, arnorm = 0;
+};
+// LSQR on the operator A M (M upper-triangular n x n, or identity if
+// Minv_rowmajor == nullptr).  A is double (a64) or float (a32), m x n, lda.
+// x0 nullable; x receives z (the solution of the preconditioned problem,
+// i.e. the caller applies M afterwards).  arnorms_dev nullable (iter_lim values).
+LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
+                      int64_t lda, const double* M, const double* b, const double* x0,
+                      const LsqrParams& prm, double* x, double* var, double* arnorms_dev,
+                      bool ffp);
+// CGLS (cg.rs:18-61) on A M, same conventions; returns iterations used.
+int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
+                   int64_t lda, const double* M, const double* b, const double* x0,
+                   double tolerance, int64_t num_iterations, double* x, bool* converged);
+// y = M x for upper-triangular M (n x n)
+void trmv_upper(Ctx& ctx, const double* M, int64_t n, int64_t ldm, const double* x, double* y);
+
+// ---- tensor-core digit-sliced products (sketch_tc.cu) ----
+// Returns true if the sm_103a tensor-core kernels are usable on this device.
+bool tc_available(Ctx& ctx);
+// C (M x N, ldc, FP64) = S X where S (M x K) is the quantised Gaussian
+// sketch of `key` (entry (i,k) = word i + k*round_up(M,4)), X (K x N).
+void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
+                     int64_t ldx, int64_t M, int digits, double* C, int64_t ldc);
+// C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.
+void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y,
+                int64_t NN, int64_t ldy, int dx, int dy, double* C, int64_t ldc);
+
+}  // namespace rnla

@@ -1,0 +1,69 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares.
+No compute entry point is called here (this suite also runs without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        with open(h) as f:
+            txt = f.read()
+        names |= set(re.findall(r"^RNLA_API\s+[\w\s\*]+?\b(rnla_\w+)\s*\(", txt, re.M))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("rnla_sketching_operator", "rnla_rand_svd", "rnla_blendenpik_overdetermined",
+                 "rnla_cgls", "rnla_lsqr", "rnla_solve_upper_triangular_system", "rnla_qb1",
+                 "rnla_rf1", "rnla_tsog1", "rnla_orth", "rnla_stabilizer"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from randnla_gb300 import _lib
+    assert os.path.exists(_lib.LIB_PATH), "library not built"
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s+(rnla_\w+)", out))
+    missing = declared_symbols() - exported
+    assert not missing, missing
+    bound = {name for name, _, _ in _lib.SIGNATURES}
+    assert bound == declared_symbols()
+
+
+def test_library_loads_and_answers_host_queries():
+    import randnla_gb300 as R
+    lib = R.lib()
+    assert lib.rnla_version().decode().endswith("sm_103a")
+    assert lib.rnla_device_count() >= 0
+    o = R.options()
+    assert o.precision == 0 and o.conlim == 1e8 and o.power_iters == 2
+    # rank rule of lora_drivers.rs:51 with the reference shapes
+    assert lib.rnla_rand_svd_rank(100, 50, 45, 2, 0) == 45
+    assert lib.rnla_rand_svd_rank(5, 20, 3, 2, 0) == 3
+    assert lib.rnla_rand_svd_rank(10, 2, 3, 2, 0) == 2
+
+
+def test_struct_layouts_match_header():
+    from randnla_gb300 import _lib
+    assert ctypes.sizeof(_lib.Rng) == 24
+    assert ctypes.sizeof(_lib.Options) == 16 + 24 + 24 + 16
+    assert ctypes.sizeof(_lib.LsqrResult) == 16 + 5 * 8
+
+
+def test_no_oracle_in_product():
+    """The product package never imports or loads the oracle."""
+    for path in glob.glob(os.path.join(ROOT, "randnla_gb300", "**", "*"), recursive=True):
+        if path.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+            with open(path) as f:
+                txt = f.read()
+            assert "oracle" not in txt.lower(), path

@@ -1,0 +1,79 @@
+"""The oracle's generators against the reference's own known-answer vectors
+(rust-random123/src/philox.rs:242-363, threefry.rs:97-127)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def test_philox_kats(golden):
+    k = golden["rng"]
+    s1, s2 = k["philox_key_seed1"], k["philox_key_seed2"]
+    for i in range(10):
+        assert O.philox4x32([i, 0, 0, 0], [s1, s2]) == k["philox4x32"][4 * i:4 * i + 4]
+        assert O.philox2x32([i, 0], [s1]) == k["philox2x32"][2 * i:2 * i + 2]
+        assert O.philox2x64([i, 0], [s1]) == k["philox2x64"][2 * i:2 * i + 2]
+        assert O.philox4x64([i, 0, 0, 0], [s1, s2]) == k["philox4x64"][4 * i:4 * i + 4]
+
+
+def test_threefry_kat(golden):
+    k = golden["rng"]
+    for i in range(10):
+        assert O.threefry2x64([i, 0], [k["threefry_key0"], k["threefry_key1"]]) == \
+            k["threefry2x64"][2 * i:2 * i + 2]
+
+
+def test_word_stream_is_block_sequence(golden):
+    """Word t = word t%4 of block t//4 (philox.rs:87-99 counter order)."""
+    k = golden["rng"]
+    key = k["philox_key_seed1"] | (k["philox_key_seed2"] << 32)
+    w = O.word_stream(O.GEN_PHILOX4X32, key, 0, 0, 40)
+    assert list(w) == k["philox4x32"]
+    w = O.word_stream(O.GEN_THREEFRY2X64, k["threefry_key0"], k["threefry_key1"], 0, 40)
+    joined = [int(w[2 * i]) | (int(w[2 * i + 1]) << 32) for i in range(20)]
+    assert joined == k["threefry2x64"]
+    # offsets: a window equals the slice of a longer stream
+    full = O.word_stream(O.GEN_PHILOX4X32, 7, 0, 0, 1000)
+    part = O.word_stream(O.GEN_PHILOX4X32, 7, 0, 333, 101)
+    assert np.array_equal(full[333:434], part)
+
+
+def test_counter_carry():
+    """Block 2^32 carries into the second counter word (philox.rs:89-91)."""
+    w = O.word_stream(O.GEN_PHILOX4X32, 5, 0, 4 * (1 << 32), 4)
+    assert list(w) == O.philox4x32([0, 1, 0, 0], [5, 0])
+
+
+def test_transforms_accuracy():
+    lib = O.lib()
+    import ctypes
+    lib.oracle_log_unit.restype = ctypes.c_float
+    lib.oracle_log_unit.argtypes = [ctypes.c_float]
+    us = np.random.default_rng(0).integers(1, 2 ** 24 + 1, 5000) * 2.0 ** -24
+    err = max(abs(lib.oracle_log_unit(float(u)) - np.log(u)) / max(1.0, abs(np.log(u))) for u in us)
+    assert err < 4e-7
+
+
+def test_gaussian_statistics():
+    S = O.sketch(O.DIST_GAUSSIAN, 256, 1000, key0=42)
+    assert abs(S.mean()) < 0.01 and abs(S.var() - 1.0) < 0.01
+    kurt = ((S - S.mean()) ** 4).mean() / S.var() ** 2
+    assert abs(kurt - 3.0) < 0.05
+    U = O.sketch(O.DIST_UNIFORM, 256, 1000, key0=42)
+    assert U.min() > -1 and U.max() < 1 and abs(U.var() - 1 / 3) < 0.01
+    R = O.sketch(O.DIST_RADEMACHER, 256, 1000, key0=42)
+    assert set(np.unique(R)) == {-1.0, 1.0} and abs(R.mean()) < 0.01
+
+
+def test_quantized_sketch_grid():
+    Q = O.sketch(O.DIST_GAUSSIAN, 64, 500, key0=1, quantized=True)
+    assert np.all(np.abs(Q * 8 - np.rint(Q * 8)) == 0) and np.abs(Q).max() <= 63 / 8
+    G = O.sketch(O.DIST_GAUSSIAN, 64, 500, key0=1)
+    assert np.abs(Q - G).max() <= 1 / 16 + 1e-7
+
+
+def test_sketch_shape_errors():
+    with pytest.raises(ValueError):
+        O.sketch(O.DIST_GAUSSIAN, 0, 5)
+    with pytest.raises(ValueError):
+        O.sketch(O.DIST_GAUSSIAN, 5, 0)
