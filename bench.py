@@ -1,0 +1,409 @@
+#!/usr/bin/env python3
+"""Benchmark of the sketch-and-precondition least-squares hot path.
+
+Workload (the configuration the headline metric is quoted on): overdetermined
+least squares with A of 100000 x 500, A = U diag(sigma) V^T, sigma log-spaced
+from 1 to 1e-8 (kappa = 1e8), b = A x* + 1e-6 N(0,1), Gaussian sketch
+d = 4n = 2000, preconditioned LSQR to relative tolerance 1e-12.  Inputs are
+seeded synthetic data generated on the GPU (torch CUDA generator); A (400 MB)
+is larger than L2, so no flush is needed between steps.
+
+One step = one blendenpik solve (sketch S [A b], QR of the sketch, R^-1,
+preconditioned LSQR, x = R^-1 z) through the library's device-pointer entry
+point.  `value` is solves/s with inputs resident in HBM; `e2e` is the same
+metric through the host-pointer entry point with pinned host buffers (A and b
+copied in, x copied out inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun) every rank solves its own replica (the path has no
+exchange step); value = all ranks' solves / max-over-ranks time.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rand_svd & sketch-LS solves/sec on 1 GB300: BF16-sketch vs plain FP64 at stated error"
+UNIT = "solves/s"
+CFG = dict(m=100000, n=500, kappa=1e8, noise=1e-6, sampling_factor=4.0, tol=1e-12)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--m", type=int, default=CFG["m"])
+    p.add_argument("--n", type=int, default=CFG["n"])
+    p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison path")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas)
+# ---------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, local, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# problem generation (seeded, on the GPU)
+# ---------------------------------------------------------------------------
+def make_problem(m, n, kappa, noise, dev, dtype_a=None):
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(1)
+    U = torch.linalg.qr(torch.randn(m, n, generator=g, device=dev, dtype=torch.float64))[0]
+    g.manual_seed(2)
+    V = torch.linalg.qr(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64))[0]
+    sig = torch.logspace(0, -math.log10(kappa), n, dtype=torch.float64, device=dev)
+    A = (U * sig) @ V.T
+    del U
+    A = A.t().contiguous().t()                    # column-major, ld = m
+    g.manual_seed(3)
+    xs = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
+    g.manual_seed(4)
+    b = A @ xs + noise * torch.randn(m, generator=g, device=dev, dtype=torch.float64)
+    return A, b
+
+
+def rel_residual(A, x, b):
+    import torch
+    return float(torch.linalg.norm(A @ x - b) / torch.linalg.norm(b))
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, local, ws):
+    import torch
+    import numpy as np
+    import randnla_gb300 as R
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = R.lib()
+    m, n = args.m, args.n
+    A, b = make_problem(m, n, CFG["kappa"], CFG["noise"], dev)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    tol = CFG["tol"]
+    sf = CFG["sampling_factor"]
+    l = 10 * n
+
+    tc = True
+    o_fast = R.options(precision=R.Precision.BF16X, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol,
+                       seed=42)
+    try:
+        R.blendenpik_dev(A, b, x, tol, l, sf, o_fast)
+    except R.Unsupported:
+        tc = False
+    o_fp64 = R.options(precision=R.Precision.FP64, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol,
+                       seed=42)
+    o = o_fast if tc else o_fp64
+
+    # accuracy of the timed path against the plain FP64 path and LAPACK (cuSOLVER QR)
+    st = R.blendenpik_dev(A, b, x, tol, l, sf, o)
+    torch.cuda.synchronize()
+    rr = rel_residual(A, x, b)
+    x64 = torch.zeros_like(x)
+    st64 = R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
+    torch.cuda.synchronize()
+    rr64 = rel_residual(A, x64, b)
+    xl = torch.linalg.lstsq(A, b.unsqueeze(1), driver="gels").solution.squeeze(1)
+    rrl = rel_residual(A, xl, b)
+
+    for _ in range(args.warmup):
+        R.blendenpik_dev(A, b, x, tol, l, sf, o)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.rnla_kernel_launches()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    solve_ms = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        s_ = R.blendenpik_dev(A, b, x, tol, l, sf, o)
+        solve_ms.append((s_["ms_solve"], s_["iterations"], s_["ms_sketch"], s_["ms_factor"]))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = lib.rnla_kernel_launches() - launches0
+    clk = clocks.stop()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(ms, ws)
+    value = ws * args.steps / (ms_max / 1e3)
+
+    # plain FP64 GPU path throughput (same problem, same solver settings)
+    fp64 = None
+    if not args.no_fp64 and tc:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
+        reps = 2
+        t0.record(stream)
+        for _ in range(reps):
+            R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        fp64 = {"value": reps / (t0.elapsed_time(t1) / 1e3), "unit": UNIT,
+                "rel_residual": rr64, "iterations": st64["iterations"]}
+
+    # end to end through the host-pointer entry point with pinned buffers
+    Ah = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()   # column-major host
+    Ah.copy_(A.cpu())
+    bh = torch.empty(m, dtype=torch.float64, pin_memory=True)
+    bh.copy_(b.cpu())
+    xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    st_e = R.Stats()
+    o_c = o
+
+    def e2e_call():
+        rc = lib.rnla_blendenpik_overdetermined_ex(
+            ctypes.c_void_p(Ah.data_ptr()), m, n, m, ctypes.c_void_p(bh.data_ptr()), tol, l, sf,
+            ctypes.byref(o_c), ctypes.c_void_p(xh.data_ptr()), ctypes.byref(st_e))
+        if rc != 0:
+            raise RuntimeError(lib.rnla_last_error_message().decode())
+
+    for _ in range(2):
+        e2e_call()
+    barrier(ws)
+    t_start = time.perf_counter()
+    ke = max(2, args.steps // 2)
+    for _ in range(ke):
+        e2e_call()
+    t_e2e = time.perf_counter() - t_start
+    t_e2e = max_over_ranks(t_e2e, ws)
+    e2e_val = ws * ke / t_e2e
+
+    # roofline of the dominant kernel
+    ms_solve = sum(s[0] for s in solve_ms) / len(solve_ms)
+    ms_sketch = sum(s[2] for s in solve_ms) / len(solve_ms)
+    ms_factor = sum(s[3] for s in solve_ms) / len(solve_ms)
+    iters = solve_ms[-1][1]
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            peaks = json.load(f)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    elem = m * n * 8
+    lsqr_bytes = (iters + 1) * elem + 4 * m * 8 * (iters + 1)
+    lsqr_gbs = lsqr_bytes / (ms_solve / 1e3) / 1e9
+    sketch_flops = 2.0 * int(CFG["sampling_factor"] * n) * m * (n + 1)   # S [A b]
+    sketch_tflops = sketch_flops / (ms_sketch / 1e3) / 1e12
+    stages = {"sketch_ms": ms_sketch, "qr_rinv_ms": ms_factor, "lsqr_ms": ms_solve,
+              "lsqr_iterations": iters}
+    if ms_solve >= ms_sketch or not tc:
+        roof = {"bound": "hbm", "kernel": "lsqr_kernel (fused A y / A^T u pass per iteration)",
+                "achieved": lsqr_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": lsqr_gbs / hbm_peak,
+                "traffic": None, "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": lsqr_bytes}
+    else:
+        roof = {"bound": "tensor", "kernel": "sketch_tc (digit-sliced bf16 S [A b])",
+                "achieved": sketch_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": sketch_tflops / bf16_peak, "traffic": None, "peak_source": peak_src,
+                "algorithmic_flops_per_launch": sketch_flops}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16-digit-sliced sketch + f64" if tc else "f64",
+        "data": "synthetic (seeded torch CUDA generator)",
+        "config": {"workload": "blendenpik_overdetermined %dx%d kappa=1e8 d=%d lsqr tol=1e-12"
+                               % (m, n, int(CFG["sampling_factor"] * n)),
+                   "m": m, "n": n, "d": int(CFG["sampling_factor"] * n), "kappa": CFG["kappa"],
+                   "precision": "BF16X" if tc else "FP64", "inner_solver": "LSQR",
+                   "l2": "inputs larger than L2 (A is %d MB)" % (elem >> 20),
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "accuracy": {"rel_residual": rr, "rel_residual_fp64_path": rr64, "rel_residual_lapack": rrl,
+                     "abs_diff_vs_fp64": abs(rr - rr64), "abs_diff_vs_lapack": abs(rr - rrl)},
+        "stages": stages,
+        "fp64_path": fp64,
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": elem + m * 8,
+                "d2h_bytes_per_step": n * 8},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "clocks": clk,
+    }
+    return line
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle's restatement of the reference algorithm
+# ---------------------------------------------------------------------------
+def cpu_sample(m_full, n, iters, sample_rows):
+    """Reference blendenpik (sketch_and_precondition.rs:26-59: dense Gaussian
+    S, S a, QR, R^-1, explicit a R^-1, CGLS) on a row-subsampled problem with
+    the same n, kappa and d; CGLS runs `iters` iterations.  Returns
+    (seconds for the sample, full-size solves/s by linear scaling in m)."""
+    import numpy as np
+    from oracle import oracle as O
+    ms = sample_rows
+    d = int(CFG["sampling_factor"] * n)
+    rng = np.random.default_rng(0)
+    U = np.linalg.qr(rng.standard_normal((ms, n)))[0]
+    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    A = (U * np.logspace(0, -8, n)) @ V.T
+    b = A @ rng.standard_normal(n) + 1e-6 * rng.standard_normal(ms)
+    S = O.sketch(O.DIST_GAUSSIAN, d, ms)
+    t0 = time.perf_counter()
+    O.blendenpik_overdetermined(A, b, 1e-300, iters, CFG["sampling_factor"], S=S)
+    t = time.perf_counter() - t0
+    # the sketch generation is part of the reference call (sketch.rs:102-130); time it too
+    t1 = time.perf_counter()
+    O.sketch(O.DIST_GAUSSIAN, d, min(ms, 20000))
+    tg = (time.perf_counter() - t1) * ms / min(ms, 20000)
+    total = t + tg
+    return total, 1.0 / (total * m_full / ms)
+
+
+def run_reference(args, rank, ws):
+    """The reference arm: the oracle's CPU restatement of the reference's
+    path on the host cores, rank 0 only."""
+    if rank != 0:
+        return None
+    import numpy as np
+    iters = 40
+    rows = max(2 * int(CFG["sampling_factor"] * args.n), 10000)
+    samples = []
+    for _ in range(args.warmup):
+        cpu_sample(args.m, args.n, iters, rows)
+    for _ in range(args.steps):
+        samples.append(cpu_sample(args.m, args.n, iters, rows)[1])
+    v = float(np.median(samples))
+    cores = os.cpu_count()
+    return {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy generator)",
+        "impl": "reference",
+        "config": {"workload": "blendenpik_overdetermined %dx%d kappa=1e8 d=%d" %
+                               (args.m, args.n, int(CFG["sampling_factor"] * args.n)),
+                   "m": args.m, "n": args.n},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "oracle restatement of sketch_and_precondition.rs:26-59 "
+                                   "(numpy/LAPACK on all host threads, C sketch generator) on "
+                                   "%d x %d rows with %d CGLS iterations, scaled linearly in m "
+                                   "to %d rows" % (rows, args.n, iters, args.m)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    rank, local, ws = dist_init()
+    if args.impl == "reference":
+        line = run_reference(args, rank, ws)
+        if line is not None:
+            print(json.dumps(line))
+        return
+    line = run_ours(args, rank, local, ws)
+    if rank == 0 and not args.no_cpu:
+        iters = line["stages"]["lsqr_iterations"]
+        rows = max(2 * int(CFG["sampling_factor"] * args.n), 10000)
+        t, v = cpu_sample(args.m, args.n, max(iters, 1), rows)
+        line["cpu_baseline"] = {
+            "value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "oracle restatement of sketch_and_precondition.rs:26-59 (numpy/LAPACK on all "
+                      "host threads, C sketch generator) on %d x %d rows, %d CGLS iterations "
+                      "(the GPU's iteration count), %.2f s, scaled linearly in m to %d rows"
+                      % (rows, args.n, iters, t, args.m)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -63,6 +63,9 @@ RNLA_API const char* rnla_last_error_message(void);
 RNLA_API const char* rnla_version(void);
 /* Number of usable CUDA devices (0 on a machine without a GPU; no error). */
 RNLA_API int rnla_device_count(void);
+/* Number of kernels this library has launched in the process so far (a
+ * diagnostic counter; bench.py reports launches inside its timed region). */
+RNLA_API uint64_t rnla_kernel_launches(void);
 
 /* ---- sketch distributions: src/sketch.rs:9-13 ---- */
 typedef enum { RNLA_GAUSSIAN = 0, RNLA_UNIFORM = 1, RNLA_RADEMACHER = 2 } rnla_distribution;

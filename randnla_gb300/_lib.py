@@ -47,6 +47,7 @@ SIGNATURES = [
     ("rnla_last_error_message", ctypes.c_char_p, []),
     ("rnla_version", ctypes.c_char_p, []),
     ("rnla_device_count", ctypes.c_int, []),
+    ("rnla_kernel_launches", c_u64, []),
     ("rnla_rng_words", ctypes.c_int, [ctypes.POINTER(Rng), c_u64, c_i64, c_vp]),
     ("rnla_rng_words_dev", ctypes.c_int, [ctypes.POINTER(Rng), c_u64, c_i64, c_vp, c_vp]),
     ("rnla_sketching_operator", ctypes.c_int, [c_i32, c_i64, c_i64, c_vp, c_i64]),

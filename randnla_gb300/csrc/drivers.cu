@@ -247,7 +247,7 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
             // Y = A Omega = (Omega^T A^T)^T: the sketch kernel applies Omega^T (l x n) to A^T
             DevBuf<double> At((size_t)n * m, ctx.stream), Yt((size_t)l * m, ctx.stream);
             transpose(ctx, m, n, A, ld, At, n);
-            tc_sketch_apply(ctx, key, At, false, n, m, n, l, o.digits_a, Yt, l);
+            tc_sketch_apply(ctx, key, At, false, n, m, n, nullptr, l, o.digits_a, Yt, l);
             transpose(ctx, l, m, Yt, l, Y, m);
         }
         fallbacks += orthonormalize(ctx, Y, m, l, m, force_hh);
@@ -342,8 +342,8 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     } else {
         if (!tc_available(ctx))
             fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
-        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, d, o.digits_a, SK, d);
-        tc_sketch_apply(ctx, key, b, false, m, 1, m, d, 0, SK.get() + n * d, d);
+        // S [a b] in one pass: b rides along as column n of the digit planes
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d);
     }
     tm.mark();
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
@@ -728,7 +728,7 @@ int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_
         gemm_f64(ctx, 'N', 'N', d, n, m, 1.0, S, d, X, ld, 0.0, y_dev, ldy);
     } else {
         if (!tc_available(ctx)) fail(RNLA_ERR_UNSUPPORTED, "sm_103a tensor-core kernels unavailable");
-        tc_sketch_apply(ctx, key, x_dev, x_is_f32 != 0, m, n, ldx, d, digits, y_dev, ldy);
+        tc_sketch_apply(ctx, key, x_dev, x_is_f32 != 0, m, n, ldx, nullptr, d, digits, y_dev, ldy);
     }
     RNLA_API_END
 }

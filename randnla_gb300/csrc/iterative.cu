@@ -545,6 +545,7 @@ static void* cgls_kernel_for(int64_t n) {
 static void launch_coop(Ctx& ctx, void* kernel, int G, size_t smem, IterArgs& a) {
     void* params[] = {&a};
     RNLA_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(IT_THREADS), params, smem, ctx.stream));
+    count_launch();
 }
 
 LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,

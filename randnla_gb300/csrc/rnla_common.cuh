@@ -29,7 +29,14 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
     }
 }
 #define RNLA_CUDA(x) ::rnla::cuda_check((x), #x, __FILE__, __LINE__)
-#define RNLA_LAUNCH_CHECK() ::rnla::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+// Every kernel launch of the library is followed by RNLA_LAUNCH_CHECK(),
+// which also counts it (rnla_kernel_launches()).
+void count_launch();
+#define RNLA_LAUNCH_CHECK()                                                          \
+    do {                                                                             \
+        ::rnla::count_launch();                                                      \
+        ::rnla::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__); \
+    } while (0)
 
 // Per-call context: stream plus device facts used for grid sizing.
 struct Ctx {

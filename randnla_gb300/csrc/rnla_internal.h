@@ -89,10 +89,11 @@ void trmv_upper(Ctx& ctx, const double* M, int64_t n, int64_t ldm, const double*
 // ---- tensor-core digit-sliced products (sketch_tc.cu) ----
 // Returns true if the sm_103a tensor-core kernels are usable on this device.
 bool tc_available(Ctx& ctx);
-// C (M x N, ldc, FP64) = S X where S (M x K) is the quantised Gaussian
-// sketch of `key` (entry (i,k) = word i + k*round_up(M,4)), X (K x N).
+// C (M x N', ldc, FP64) = S [X extra] where S (M x K) is the quantised
+// Gaussian sketch of `key` (entry (i,k) = word i + k*round_up(M,4)), X (K x N)
+// and the optional double column `extra` (K values) appended as column N.
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
-                     int64_t ldx, int64_t M, int digits, double* C, int64_t ldc);
+                     int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc);
 // C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.
 void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                 int64_t NN, int64_t ldy, int dx, int dy, double* C, int64_t ldc);

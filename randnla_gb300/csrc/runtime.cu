@@ -5,8 +5,12 @@
 #include <mutex>
 #include <map>
 #include <cstring>
+#include <atomic>
 
 namespace rnla {
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
 // Stream-ordered pool (one per device, never shrinks between calls)
@@ -217,6 +221,8 @@ extern "C" {
 const char* rnla_last_error_message(void) { return t_last_error.c_str(); }
 
 const char* rnla_version(void) { return "0.1.0 sm_103a"; }
+
+uint64_t rnla_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int rnla_device_count(void) {
     int n = 0;
