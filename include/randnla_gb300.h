@@ -189,6 +189,23 @@ RNLA_API int rnla_lsqr_dev(const double* a_dev, int64_t m, int64_t n, int64_t ld
                   int32_t calc_var, const double* x0_dev, double* x_dev, rnla_lsqr_result* result,
                   double* arnorms_host, double* var_dev, void* stream);  /* synchronises */
 
+/* Allocation-free LSQR (no counterpart in the reference).  For callers that
+ * cannot let a library allocate device memory: applications running under a
+ * fixed memory budget managed by their own allocator, where a cudaMalloc can
+ * fail or synchronise the device at an uncontrolled moment, and tight loops
+ * that must not pay cudaMalloc/cudaFree per call.  Same algorithm as
+ * rnla_lsqr_dev without the variance and history outputs; FP64 arithmetic.
+ * All scratch lives in a fixed 32 MiB device array inside the library (held
+ * by every GPU that loads it until the process exits); a problem needs
+ * 8 * (10 + 4G + m + 5n + G n) bytes, G <= 4 x (number of SMs), and larger
+ * problems return RNLA_ERR_INVALID_DIMENSIONS.  Calls share that array, so
+ * calls that overlap on the GPU race; the first call on a device looks up the
+ * array's address and should come before any stream capture.  Synchronises. */
+RNLA_API int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda,
+                                   const double* b_dev, double damp, double atol, double btol,
+                                   double conlim, int64_t iter_lim, const double* x0_dev,
+                                   double* x_dev, rnla_lsqr_result* result, void* stream);
+
 /* ---- cg.rs ---- */
 
 /* cg::cgls (src/cg.rs:18-61): CGLS from x0 (NULL -> zeros); stops when

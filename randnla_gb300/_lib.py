@@ -65,6 +65,9 @@ SIGNATURES = [
     ("rnla_lsqr_dev", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_dbl, c_dbl, c_dbl, c_i64, c_i32, c_vp, c_vp,
       ctypes.POINTER(LsqrResult), c_vp, c_vp, c_vp]),
+    ("rnla_lsqr_noalloc_dev", ctypes.c_int,
+     [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_dbl, c_dbl, c_dbl, c_i64, c_vp, c_vp,
+      ctypes.POINTER(LsqrResult), c_vp]),
     ("rnla_cgls", ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_vp, c_vp, P_i64]),
     ("rnla_cgls_dev", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_vp, c_vp, P_i64, c_vp]),

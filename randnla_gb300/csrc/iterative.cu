@@ -921,6 +921,88 @@ int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int
     return (int64_t)out[1];
 }
 
+// Bytes of caller-provided workspace lsqr_run_in_workspace needs for an
+// m x n problem on a device with `sm_count` SMs (FP64 arithmetic, no
+// preconditioner).  Sets *grid to the cooperative grid it will use.
+size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem_out,
+                            const void** kernel_out) {
+    const int mode = (n <= STREAM_MAX_N) ? 1 : 0;
+    const void* k = select_kernel<true>(false, mode, n);
+    int64_t red_off = 0;
+    const size_t smem = iter_smem(mode, n, pick_R(n), red_off);
+    if (smem > 48 * 1024)
+        RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int nb = 0;
+    RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, IT_THREADS, smem));
+    if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "iterative kernel does not fit on an SM");
+    if (nb > 4) nb = 4;
+    const int G = nb * sm_count;
+    if (grid) *grid = G;
+    if (smem_out) *smem_out = smem;
+    if (kernel_out) *kernel_out = k;
+    // words (status, barrier) | out[8] | sp[G*4] | u[m] | v, vun, w, y, g [5n] | part[G*n]
+    return sizeof(double) * (size_t)(2 + 8 + 4 * (int64_t)G + m + 5 * n + (int64_t)G * n);
+}
+
+// LSQR (FP64 arithmetic, no preconditioner) with every scratch buffer carved
+// out of `ws` (lsqr_workspace_bytes bytes, 256-byte aligned).  Performs no
+// allocation: the status word, barrier words and result record inside `ws`
+// are cleared with cudaMemsetAsync, everything else is written by the
+// kernel before it is read.
+LsqrResult lsqr_run_in_workspace(cudaStream_t stream, int sm_count, void* ws, size_t ws_bytes,
+                                 const double* a64, int64_t m, int64_t n, int64_t lda, const double* b,
+                                 const double* x0, const LsqrParams& prm, double* x) {
+    int G = 0;
+    size_t smem = 0;
+    const void* k = nullptr;
+    const size_t need = lsqr_workspace_bytes(m, n, sm_count, &G, &smem, &k);
+    if (need > ws_bytes) fail(RNLA_ERR_INVALID_DIMENSIONS, "workspace too small");
+    double* d = static_cast<double*>(ws);
+    unsigned int* words = reinterpret_cast<unsigned int*>(d);   // [0] status, [1] count, [2] gen
+    double* out = d + 2;
+    double* sp = out + 8;
+    double* u = sp + 4 * (int64_t)G;
+    double* v = u + m;
+    double* vun = v + n;
+    double* w = vun + n;
+    double* y = w + n;
+    double* g = y + n;
+    double* part = g + n;
+    RNLA_CUDA(cudaMemsetAsync(d, 0, sizeof(double) * 10, stream));
+    IterArgs a;
+    a.A = a64; a.m = m; a.n = n; a.lda = lda;
+    a.M = nullptr; a.Mt = nullptr;
+    a.b = b; a.x0 = x0;
+    a.u = u; a.ap = u; a.v = v; a.vun = vun; a.w = w; a.x = x; a.y = y; a.g = g;
+    a.part = part; a.sp = sp; a.var = nullptr; a.arn = nullptr; a.out = out;
+    a.damp = prm.damp; a.atol = prm.atol; a.btol = prm.btol; a.conlim = prm.conlim;
+    a.abs_tol = prm.abs_arnorm_tol;
+    a.iter_lim = prm.iter_lim < 0 ? 2 * n : prm.iter_lim;
+    a.calc_var = 0;
+    a.bar.status = words;
+    a.bar.count = words + 1;
+    a.bar.gen = words + 2;
+    a.R = pick_R(n);
+    const int mode = (n <= STREAM_MAX_N) ? 1 : 0;
+    int64_t red_off = 0;
+    iter_smem(mode, n, a.R, red_off);
+    a.red_off = red_off;
+    void* params[] = {&a};
+    RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(IT_THREADS), params, smem, stream));
+    count_launch();
+    double h[8];
+    unsigned int st = 0;
+    RNLA_CUDA(cudaMemcpyAsync(h, out, sizeof h, cudaMemcpyDeviceToHost, stream));
+    RNLA_CUDA(cudaMemcpyAsync(&st, words, sizeof st, cudaMemcpyDeviceToHost, stream));
+    RNLA_CUDA(cudaStreamSynchronize(stream));
+    if (st == KSTATUS_BARRIER_TIMEOUT) fail(RNLA_ERR_TIMEOUT, "lsqr: a grid barrier exceeded its limit");
+    if (st != 0) fail(RNLA_ERR_COMPUTATION, "lsqr: device status set");
+    LsqrResult r;
+    r.istop = (int64_t)h[0]; r.itn = (int64_t)h[1];
+    r.r1norm = h[2]; r.r2norm = h[3]; r.anorm = h[4]; r.acond = h[5]; r.xnorm = h[6]; r.arnorm = h[7];
+    return r;
+}
+
 __global__ void trmv_upper_kernel(const double* __restrict__ M, int64_t n, int64_t ldm,
                                   const double* __restrict__ x, double* __restrict__ y) {
     const int lane = threadIdx.x & 31;

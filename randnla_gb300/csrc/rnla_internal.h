@@ -83,6 +83,12 @@ LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, 
 int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                    int64_t lda, const double* M, const double* b, const double* x0,
                    double tolerance, int64_t num_iterations, double* x, bool* converged);
+// Workspace-based LSQR used by the allocation-free entry point (noalloc.cu).
+size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem,
+                            const void** kernel);
+LsqrResult lsqr_run_in_workspace(cudaStream_t stream, int sm_count, void* ws, size_t ws_bytes,
+                                 const double* a64, int64_t m, int64_t n, int64_t lda, const double* b,
+                                 const double* x0, const LsqrParams& prm, double* x);
 // y = M x for upper-triangular M (n x n)
 void trmv_upper(Ctx& ctx, const double* M, int64_t n, int64_t ldm, const double* x, double* y);
 
