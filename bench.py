@@ -136,17 +136,22 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # problem generation (seeded, on the GPU)
 # ---------------------------------------------------------------------------
-def make_problem(m, n, kappa, noise, dev, dtype_a=None):
+def make_problem(m, n, kappa, noise, dev):
+    """A = U diag(sigma) V^T with U, V the orthonormal factors (this library's
+    Householder Orth) of seeded Gaussian matrices; b = A x* + noise."""
+    import numpy as np
     import torch
+    import randnla_gb300 as R
     g = torch.Generator(device=dev)
     g.manual_seed(1)
-    U = torch.linalg.qr(torch.randn(m, n, generator=g, device=dev, dtype=torch.float64))[0]
+    U = R.Orth(torch.randn(n, m, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
     g.manual_seed(2)
-    V = torch.linalg.qr(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64))[0]
-    sig = torch.logspace(0, -math.log10(kappa), n, dtype=torch.float64, device=dev)
-    A = (U * sig) @ V.T
-    del U
-    A = A.t().contiguous().t()                    # column-major, ld = m
+    V = R.Orth(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
+    sig = np.logspace(0, -math.log10(kappa), n)
+    Ut = torch.from_numpy(np.asfortranarray(U)).to(dev)
+    Vt = torch.from_numpy(np.ascontiguousarray(V.T * sig[:, None])).to(dev)   # diag(sigma) V^T
+    A = (Ut @ Vt).t().contiguous().t()            # column-major, ld = m
+    del Ut
     g.manual_seed(3)
     xs = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
     g.manual_seed(4)
@@ -155,8 +160,16 @@ def make_problem(m, n, kappa, noise, dev, dtype_a=None):
 
 
 def rel_residual(A, x, b):
-    import torch
-    return float(torch.linalg.norm(A @ x - b) / torch.linalg.norm(b))
+    return float((A @ x - b).norm() / b.norm())
+
+
+def lapack_rel_residual(A, b):
+    """Relative residual of numpy/LAPACK least squares (host, FP64)."""
+    import numpy as np
+    Ah = A.cpu().numpy()
+    bh = b.cpu().numpy()
+    xl = np.linalg.lstsq(Ah, bh, rcond=None)[0]
+    return float(np.linalg.norm(Ah @ xl - bh) / np.linalg.norm(bh))
 
 
 # ---------------------------------------------------------------------------
@@ -196,8 +209,7 @@ def run_ours(args, rank, local, ws):
     st64 = R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
     torch.cuda.synchronize()
     rr64 = rel_residual(A, x64, b)
-    xl = torch.linalg.lstsq(A, b.unsqueeze(1), driver="gels").solution.squeeze(1)
-    rrl = rel_residual(A, xl, b)
+    rrl = lapack_rel_residual(A, b)
 
     for _ in range(args.warmup):
         R.blendenpik_dev(A, b, x, tol, l, sf, o)

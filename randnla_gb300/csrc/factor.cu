@@ -54,9 +54,270 @@ __global__ void __launch_bounds__(256) hh_step_kernel(double* __restrict__ X, in
     }
 }
 
+// The same factorization as one cooperative launch: CTA c owns columns
+// c, c + G, ... (at most QR_OWN); step t applies reflector t-1 to the owned
+// columns j >= t, the owner of column t then builds reflector t, and a
+// bounded grid barrier publishes it.  n + 1 barriers instead of n + 1 launches.
+constexpr int QR_OWN = 4;
+
+__global__ void __launch_bounds__(256) hh_qr_coop_kernel(double* __restrict__ X, int64_t m, int64_t n,
+                                                         int64_t nc, int64_t ld, double* __restrict__ tau,
+                                                         GridBarrier bar) {
+    __shared__ double red[8];
+    const int64_t G = gridDim.x;
+    for (int64_t t = 0; t <= n; ++t) {
+        if (t > 0) {
+            const int64_t p = t - 1;
+            const double tp = tau[p];
+            if (tp != 0.0) {
+                const double* v = X + p * ld;
+                double dot[QR_OWN];
+#pragma unroll
+                for (int q = 0; q < QR_OWN; ++q) dot[q] = 0.0;
+                for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) {
+                    const double vi = v[i];
+#pragma unroll
+                    for (int q = 0; q < QR_OWN; ++q) {
+                        const int64_t j = blockIdx.x + q * G;
+                        if (j >= t && j < nc) dot[q] = fma(vi, X[i + j * ld], dot[q]);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < QR_OWN; ++q) {
+                    const int64_t j = blockIdx.x + q * G;
+                    if (j >= t && j < nc) {                       // uniform across the CTA
+                        double* col = X + j * ld;
+                        const double s = block_sum(dot[q], red) + col[p];
+                        const double f = tp * s;
+                        if (threadIdx.x == 0) col[p] -= f;
+                        for (int64_t i = p + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] = fma(-f, v[i], col[i]);
+                    }
+                }
+            }
+        }
+        if (t < n && (t % G) == (int64_t)blockIdx.x) {
+            __syncthreads();
+            double* col = X + t * ld;
+            double sacc = 0.0;
+            for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) sacc = fma(col[i], col[i], sacc);
+            const double xn2 = block_sum(sacc, red);
+            const double alpha = col[t];
+            if (xn2 == 0.0) {
+                if (threadIdx.x == 0) tau[t] = 0.0;
+            } else {
+                const double beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+                const double scale = 1.0 / (alpha - beta);
+                for (int64_t i = t + 1 + threadIdx.x; i < m; i += blockDim.x) col[i] *= scale;
+                if (threadIdx.x == 0) {
+                    tau[t] = (beta - alpha) / beta;
+                    col[t] = beta;
+                }
+            }
+        }
+        if (t < n && !grid_sync(bar)) return;
+    }
+}
+
+// Flag-pipelined variant: each CTA keeps its owned columns (c, c + G, ...)
+// in shared memory.  Step t: wait until reflector t-1 is published
+// (flags[t-1], bounded wait), apply it to the owned columns -- the owner of
+// column t first, which then builds reflector t, writes it to global memory
+// and raises flags[t] before updating its other columns.  No grid-wide
+// barrier sits on the critical path: a step costs one flag hand-off plus
+// one column update.
+__device__ __forceinline__ bool wait_flag(const unsigned int* f, unsigned int* status) {
+    __shared__ int ok_s;
+    if (threadIdx.x == 0) {
+        ok_s = 1;
+        const volatile unsigned int* vf = f;
+        if (*vf == 0u) {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int spins = 0;
+            while (*vf == 0u) {
+                if (*((volatile unsigned int*)status) != 0u) { ok_s = 0; break; }
+                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > 2000000000ull) {
+                    atomicCAS(status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+                    ok_s = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+template <int OWN>
+__global__ void __launch_bounds__(256) hh_qr_flag_kernel(double* __restrict__ X, int64_t m, int64_t n,
+                                                         int64_t nc, int64_t ld, double* __restrict__ tau,
+                                                         unsigned int* __restrict__ flags,
+                                                         unsigned int* status) {
+    extern __shared__ double cols[];                      // OWN x m
+    __shared__ double red[8 * (OWN + 1)];
+    const int64_t G = gridDim.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int64_t jq[OWN];
+#pragma unroll
+    for (int q = 0; q < OWN; ++q) {
+        jq[q] = blockIdx.x + q * G;
+        if (jq[q] < nc)
+            for (int64_t i = tid; i < m; i += blockDim.x) cols[q * m + i] = X[i + jq[q] * ld];
+    }
+    __syncthreads();
+    // block sums of up to OWN values at once (fixed order)
+    auto block_sums = [&](double (&v)[OWN], int cnt) {
+#pragma unroll
+        for (int q = 0; q < OWN; ++q) if (q < cnt) v[q] = warp_sum(v[q]);
+        if (lane == 0)
+#pragma unroll
+            for (int q = 0; q < OWN; ++q) if (q < cnt) red[warp * OWN + q] = v[q];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < OWN; ++q)
+            if (q < cnt) {
+                double s = 0.0;
+                for (int w = 0; w < 8; ++w) s += red[w * OWN + q];
+                v[q] = s;
+            }
+        __syncthreads();
+    };
+    // applies reflector p (v from global memory, tau) to owned column q if it is >= p + 1
+    auto reflector_norm_and_publish = [&](int q, int64_t t) {
+        double* col = cols + q * m;
+        double a[1];
+        a[0] = 0.0;
+        for (int64_t i = t + 1 + tid; i < m; i += blockDim.x) a[0] = fma(col[i], col[i], a[0]);
+        double tmp[OWN];
+#pragma unroll
+        for (int r = 0; r < OWN; ++r) tmp[r] = (r == 0) ? a[0] : 0.0;
+        block_sums(tmp, 1);
+        const double xn2 = tmp[0];
+        const double alpha = col[t];
+        double tt = 0.0, beta = alpha;
+        if (xn2 != 0.0) {
+            beta = -copysign(sqrt(fma(alpha, alpha, xn2)), alpha);
+            const double scale = 1.0 / (alpha - beta);
+            for (int64_t i = t + 1 + tid; i < m; i += blockDim.x) col[i] *= scale;
+            tt = (beta - alpha) / beta;
+        }
+        __syncthreads();
+        if (tid == 0) { col[t] = beta; tau[t] = tt; }
+        __syncthreads();
+        for (int64_t i = t + tid; i < m; i += blockDim.x) X[i + t * ld] = col[i];
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            atomicExch(&flags[t], 1u);
+        }
+    };
+    // owner of column 0 starts the chain
+    if (blockIdx.x == 0 && n > 0) reflector_norm_and_publish(0, 0);
+    for (int64_t p = 0; p < n; ++p) {
+        if (!wait_flag(&flags[p], status)) return;
+        const double tp = tau[p];
+        const int64_t t = p + 1;                           // the next reflector's column
+        if (tp != 0.0) {
+            const double* v = X + p * ld;
+            // the owner of column t updates it first (look-ahead)
+            int first = -1;
+#pragma unroll
+            for (int q = 0; q < OWN; ++q) if (jq[q] == t && t < n) first = q;
+            for (int pass = 0; pass < 2; ++pass) {
+                double dot[OWN];
+                int sel[OWN];
+                int cnt = 0;
+#pragma unroll
+                for (int q = 0; q < OWN; ++q) {
+                    const bool mine = jq[q] < nc && jq[q] > p;
+                    const bool in_pass = (pass == 0) ? (q == first) : (q != first);
+                    if (mine && in_pass) sel[cnt++] = q;
+                }
+                for (int c = cnt; c < OWN; ++c) sel[c] = -1;
+                if (cnt == 0) continue;
+#pragma unroll
+                for (int c = 0; c < OWN; ++c) dot[c] = 0.0;
+                for (int64_t i = p + 1 + tid; i < m; i += blockDim.x) {
+                    const double vi = v[i];
+#pragma unroll
+                    for (int c = 0; c < OWN; ++c)
+                        if (c < cnt) dot[c] = fma(vi, cols[sel[c] * m + i], dot[c]);
+                }
+                block_sums(dot, cnt);
+#pragma unroll
+                for (int c = 0; c < OWN; ++c) {
+                    if (c >= cnt) break;
+                    double* col = cols + sel[c] * m;
+                    const double f = tp * (dot[c] + col[p]);
+                    for (int64_t i = p + 1 + tid; i < m; i += blockDim.x) col[i] = fma(-f, v[i], col[i]);
+                    __syncthreads();
+                    if (tid == 0) col[p] -= f;
+                    __syncthreads();
+                }
+                if (pass == 0 && first >= 0) reflector_norm_and_publish(first, t);
+            }
+        } else if (t < n) {
+#pragma unroll
+            for (int q = 0; q < OWN; ++q)
+                if (jq[q] == t) reflector_norm_and_publish(q, t);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < OWN; ++q)
+        if (jq[q] < nc)
+            for (int64_t i = tid; i < m; i += blockDim.x) X[i + jq[q] * ld] = cols[q * m + i];
+}
+
 void householder_qr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld, double* tau) {
     if (n <= 0) return;
     if (m < n) fail(RNLA_ERR_INVALID_DIMENSIONS, "householder_qr needs m >= n");
+    {
+        // flag-pipelined kernel when the owned columns fit in shared memory
+        int64_t G = 2LL * ctx.sm_count;
+        if (G > nc) G = nc;
+        const int own = (int)((nc + G - 1) / G);
+        const size_t smem = (size_t)own * m * sizeof(double);
+        if (n >= 8 && own <= 4 && smem <= 200 * 1024) {
+            const void* k = own == 1 ? (const void*)hh_qr_flag_kernel<1>
+                          : own == 2 ? (const void*)hh_qr_flag_kernel<2>
+                          : own == 3 ? (const void*)hh_qr_flag_kernel<3>
+                                     : (const void*)hh_qr_flag_kernel<4>;
+            RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            int nb = 0;
+            RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, smem));
+            if ((int64_t)nb * ctx.sm_count >= G) {
+                DevBuf<unsigned int> flags(n, ctx.stream);
+                RNLA_CUDA(cudaMemsetAsync(flags.get(), 0, n * sizeof(unsigned int), ctx.stream));
+                RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+                unsigned int* fl = flags.get();
+                unsigned int* st = ctx.status;
+                void* args[] = {&X, &m, &n, &nc, &ld, &tau, &fl, &st};
+                RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3((unsigned)G), dim3(256), args, smem, ctx.stream));
+                count_launch();
+                ctx.check_status("householder_qr");
+                return;
+            }
+        }
+    }
+    {
+        int nb = 0;
+        RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, hh_qr_coop_kernel, 256, 0));
+        int64_t G = (int64_t)(nb < 2 ? nb : 2) * ctx.sm_count;
+        if (G > nc) G = nc;
+        if (nb >= 1 && n >= 32 && (nc + G - 1) / G <= QR_OWN) {
+            DevBuf<unsigned int> bw(2, ctx.stream);
+            RNLA_CUDA(cudaMemsetAsync(bw.get(), 0, 2 * sizeof(unsigned int), ctx.stream));
+            RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
+            GridBarrier bar{bw.get(), bw.get() + 1, ctx.status};
+            void* args[] = {&X, &m, &n, &nc, &ld, &tau, &bar};
+            RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)hh_qr_coop_kernel, dim3((unsigned)G), dim3(256),
+                                                  args, 0, ctx.stream));
+            count_launch();
+            ctx.check_status("householder_qr");
+            return;
+        }
+    }
     for (int64_t t = 0; t <= n; ++t) {
         const int64_t jfirst = (t < n) ? t : n;
         const int64_t cnt = nc - jfirst;

@@ -41,63 +41,55 @@ template <typename TA>
 __device__ __forceinline__ double ld_a(const TA* A, int64_t idx) { return (double)A[idx]; }
 
 // y_i = sum_{j>=i} M_ij x_j (row i of M = column i of Mt); identity when M is null.
-// Distributed over all warps of the grid.
+// One CTA per row (rows round-robin over the grid), fixed-order block sums.
 __device__ void trmv_rows(const IterArgs& a, const double* __restrict__ xin, double scale,
                           double* __restrict__ yout) {
+    __shared__ double red_r[32];
     const int64_t n = a.n;
-    const int lane = threadIdx.x & 31;
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwg = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t i = gw; i < n; i += nwg) {
-        double s;
-        if (a.Mt) {
-            const double* row = a.Mt + i * n;
-            s = 0.0;
-            for (int64_t j = i + lane; j < n; j += 32) s = fma(row[j], xin[j], s);
-            s = warp_sum(s);
-        } else {
-            s = xin[i];
-        }
-        if (lane == 0) yout[i] = s * scale;
+    if (!a.Mt) {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+             i += (int64_t)gridDim.x * blockDim.x)
+            yout[i] = xin[i] * scale;
+        return;
+    }
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const double* row = a.Mt + i * n;
+        double s = 0.0;
+        for (int64_t j = i + threadIdx.x; j < n; j += blockDim.x) s = fma(row[j], xin[j], s);
+        s = block_sum(s, red_r);
+        if (threadIdx.x == 0) yout[i] = s * scale;
     }
 }
 
-// z_j = sum_{i<=j} M_ij g_i (column j of M); identity when M is null.  Each
-// warp handles whole j's; returns through the callback-free path: writes
-// f(z_j, j) via the lambda-like functor below.
+// z_j = sum_{i<=j} M_ij g_i (column j of M); identity when M is null.  One
+// CTA per column; f(z_j, j, lane) is called by thread 0 of that CTA with lane 0.
 template <typename F>
 __device__ void trmv_cols(const IterArgs& a, const double* __restrict__ gin, F f) {
+    __shared__ double red_c[32];
     const int64_t n = a.n;
-    const int lane = threadIdx.x & 31;
-    const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwg = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t j = gw; j < n; j += nwg) {
-        double s;
-        if (a.M) {
-            const double* col = a.M + j * n;
-            s = 0.0;
-            for (int64_t i = lane; i <= j; i += 32) s = fma(col[i], gin[i], s);
-            s = warp_sum(s);
-        } else {
-            s = gin[j];
-        }
-        f(s, j, lane);
+    if (!a.M) {
+        for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+             j += (int64_t)gridDim.x * blockDim.x)
+            f(gin[j], j, 0);
+        return;
+    }
+    for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+        const double* col = a.M + j * n;
+        double s = 0.0;
+        for (int64_t i = threadIdx.x; i <= j; i += blockDim.x) s = fma(col[i], gin[i], s);
+        s = block_sum(s, red_c);
+        if (threadIdx.x == 0) f(s, j, 0);
     }
 }
 
-// Sum of per-CTA partial slot `slot` in a fixed order (identical in every CTA).
+// Sum of per-CTA partial slot `slot`: every CTA runs the same fixed-order
+// reduction (strided per thread, then block_sum), so all CTAs get identical
+// bits without serialising on one thread.
 __device__ __forceinline__ double sum_partials(const double* sp, int slot) {
-    __shared__ double v_s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        for (unsigned c = 0; c < gridDim.x; ++c) s += ((volatile double*)sp)[c * 4 + slot];
-        v_s = s;
-    }
-    __syncthreads();
-    const double r = v_s;
-    __syncthreads();
-    return r;
+    __shared__ double red_sp[32];
+    double s = 0.0;
+    for (unsigned c = threadIdx.x; c < gridDim.x; c += blockDim.x) s += sp[c * 4 + slot];
+    return block_sum(s, red_sp);
 }
 
 // Block sum of a per-thread value, written by thread 0 to sp[cta*4 + slot].
@@ -106,14 +98,16 @@ __device__ __forceinline__ void write_partial(double v, double* sp, int slot, do
     if (threadIdx.x == 0) sp[blockIdx.x * 4 + slot] = v;
 }
 
-// g_j = sum over CTAs of part[c][j]
+// g_j = sum over CTAs of part[c][j]: one CTA per column, threads over the
+// CTAs' partials, fixed-order block sum.
 __device__ void reduce_columns(const IterArgs& a) {
+    __shared__ double red_g[32];
     const int64_t n = a.n;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
-         j += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
         double s = 0.0;
-        for (unsigned c = 0; c < gridDim.x; ++c) s += a.part[(int64_t)c * n + j];
-        a.g[j] = s;
+        for (unsigned c = threadIdx.x; c < gridDim.x; c += blockDim.x) s += a.part[(int64_t)c * n + j];
+        s = block_sum(s, red_g);
+        if (threadIdx.x == 0) a.g[j] = s;
     }
 }
 
@@ -366,7 +360,16 @@ __device__ void row_pass_stream(const IterArgs& a, double* __restrict__ smem_d, 
                     const float2 y = ysf[j];
                     ff_madd(ah, al, y.x, y.y, sh, sl);
                 }
-                part = (double)sh + (double)sl;
+                // combine the lanes of the same row in float-float (FP32 pipe)
+#pragma unroll
+                for (int o = R; o < 32; o <<= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+                    const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+                    float t;
+                    two_sum(sh, oh, sh, t);
+                    sl = sl + ol + t;
+                }
+                if (co == 0) ((float2*)rowred)[warp * 16 + rr_me] = make_float2(sh, sl);
             } else {
                 for (int64_t j = co + (int64_t)CPI * warp; j < n; j += (int64_t)CPI * 8) {
                     float ah, al;
@@ -375,15 +378,24 @@ __device__ void row_pass_stream(const IterArgs& a, double* __restrict__ smem_d, 
                     part = fma(dd, ysd[j], part);
                 }
             }
+            if (!FF) {
 #pragma unroll
-            for (int o = R; o < 32; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            if (co == 0) rowred[warp * 16 + rr_me] = part;
+                for (int o = R; o < 32; o <<= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if (co == 0) rowred[warp * 16 + rr_me] = part;
+            }
         }
         __syncthreads();
         if (tid < R) {
             double tsum = 0.0;
-            if (c1 != 0.0)
-                for (int w = 0; w < 8; ++w) tsum += rowred[w * 16 + tid];
+            if (c1 != 0.0) {
+                if (FF)
+                    for (int w = 0; w < 8; ++w) {
+                        const float2 v = ((const float2*)rowred)[w * 16 + tid];
+                        tsum += (double)v.x + (double)v.y;
+                    }
+                else
+                    for (int w = 0; w < 8; ++w) tsum += rowred[w * 16 + tid];
+            }
             double nv = 0.0;
             if (tid < rows) {
                 const int64_t i = i0 + tid;
@@ -434,6 +446,161 @@ __device__ void row_pass_stream(const IterArgs& a, double* __restrict__ smem_d, 
     if (want_b2) write_partial(b2, a.sp, 3, red);
 }
 
+// Float-float pass specialised for (hi, lo) FP32 storage (8-byte elements,
+// R = 8 rows per tile).  Same data flow as row_pass_stream, tuned for issue
+// rate: in the A y phase a thread's swizzle position is the same for all of
+// its columns ((j >> 1) & 3 is fixed by lane and warp), so addressing is a
+// pointer increment, and four independent TwoSum chains hide latency; in the
+// A^T u phase each 16-byte load brings two rows, u sits in registers, and
+// each column keeps two chains.
+__device__ __forceinline__ void ff_add(float& h, float& l, float oh, float ol) {
+    float t;
+    two_sum(h, oh, h, t);
+    l = l + ol + t;
+}
+
+template <int NACC>
+__device__ void row_pass_ff2(const IterArgs& a, double* __restrict__ smem_d, double c1, double c2, double c3,
+                             double* __restrict__ vec, bool want_b2, bool accumulate_at) {
+    using ST = float2;
+    constexpr int R = 8;
+    const int64_t m = a.m, n = a.n;
+    uint8_t* tiles = (uint8_t*)smem_d;
+    double* ysd = smem_d + (size_t)STG * n * (SEG / 8);
+    float2* ysf = (float2*)ysd;
+    double* usd = ysd + n;
+    float2* usf = (float2*)usd;
+    double* rowred = usd + 16;
+    double* red = rowred + 8 * 16;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int64_t j = tid; j < n; j += blockDim.x) {
+        float h, l;
+        split_ff(a.y[j], h, l);
+        ysf[j] = make_float2(h, l);
+    }
+    const bool aligned16 = ((a.lda * 8) % 16 == 0) && (((uintptr_t)a.A & 15) == 0);
+    float ach[NACC][2], acl[NACC][2];
+#pragma unroll
+    for (int q = 0; q < NACC; ++q) { ach[q][0] = ach[q][1] = acl[q][0] = acl[q][1] = 0.f; }
+    double sq = 0.0, b2 = 0.0;
+    const int64_t ntiles = (m + R - 1) / R;
+    const int64_t G = gridDim.x;
+    const size_t tile_bytes = (size_t)n * SEG;
+    __syncthreads();
+#pragma unroll 1
+    for (int s = 0; s < STG - 1; ++s) {
+        const int64_t t = blockIdx.x + (int64_t)s * G;
+        if (t < ntiles) issue_tile<ST>(a, tiles + s * tile_bytes, t, aligned16);
+        cp_commit();
+    }
+    // A y mapping: row rr of the tile, columns j = co + 4 warp + 32 k
+    const int rr = lane & 7, co = lane >> 3;
+    const int j0 = co + 4 * warp;
+    const int off_y = ((((rr >> 1) ^ ((j0 >> 1) & 3))) << 4) + ((rr & 1) << 3);
+#pragma unroll 1
+    for (int64_t k = 0;; ++k) {
+        const int64_t t = blockIdx.x + k * G;
+        if (t >= ntiles) break;
+        {
+            const int64_t t2 = blockIdx.x + (k + STG - 1) * G;
+            if (t2 < ntiles) issue_tile<ST>(a, tiles + ((k + STG - 1) % STG) * tile_bytes, t2, aligned16);
+            cp_commit();
+        }
+        cp_wait<STG - 1>();
+        __syncthreads();
+        const uint8_t* tb = tiles + (k % STG) * tile_bytes;
+        const int64_t i0 = t * R;
+        const int rows = (int)min((int64_t)R, m - i0);
+        if (c1 != 0.0) {
+            float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
+            const uint8_t* pa = tb + (size_t)j0 * SEG + off_y;
+            int64_t j = j0;
+            for (; j + 96 < n; j += 128, pa += 128 * SEG) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float2 av = *(const float2*)(pa + u * 32 * SEG);
+                    const float2 yv = ysf[j + 32 * u];
+                    ff_madd(av.x, av.y, yv.x, yv.y, h[u], l[u]);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {       // at most three columns remain
+                if (j + 32 * u < n) {
+                    const float2 av = *(const float2*)(pa + u * 32 * SEG);
+                    const float2 yv = ysf[j + 32 * u];
+                    ff_madd(av.x, av.y, yv.x, yv.y, h[u], l[u]);
+                }
+            }
+            ff_add(h[0], l[0], h[1], l[1]);
+            ff_add(h[2], l[2], h[3], l[3]);
+            ff_add(h[0], l[0], h[2], l[2]);
+#pragma unroll
+            for (int o = 8; o < 32; o <<= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, h[0], o);
+                const float ol = __shfl_xor_sync(0xffffffffu, l[0], o);
+                ff_add(h[0], l[0], oh, ol);
+            }
+            if (co == 0) ((float2*)rowred)[warp * 16 + rr] = make_float2(h[0], l[0]);
+        }
+        __syncthreads();
+        if (tid < R) {
+            double tsum = 0.0;
+            if (c1 != 0.0)
+                for (int w = 0; w < 8; ++w) {
+                    const float2 v = ((const float2*)rowred)[w * 16 + tid];
+                    tsum += (double)v.x + (double)v.y;
+                }
+            double nv = 0.0;
+            if (tid < rows) {
+                const int64_t i = i0 + tid;
+                const double bi = (c3 != 0.0 || want_b2) ? a.b[i] : 0.0;
+                const double old = (c2 != 0.0) ? vec[i] : 0.0;
+                nv = c1 * tsum + c2 * old + c3 * bi;
+                vec[i] = nv;
+                sq = fma(nv, nv, sq);
+                if (want_b2) b2 = fma(bi, bi, b2);
+            }
+            float hh, ll;
+            split_ff(nv, hh, ll);
+            usf[tid] = make_float2(hh, ll);
+        }
+        __syncthreads();
+        if (accumulate_at) {
+            float uh[R], ul[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) { const float2 uv = usf[r]; uh[r] = uv.x; ul[r] = uv.y; }
+#pragma unroll
+            for (int q = 0; q < NACC; ++q) {
+                const int64_t j = tid + (int64_t)q * blockDim.x;
+                if (j < n) {
+                    const uint8_t* seg = tb + j * SEG;
+                    const int sw = (int)((j >> 1) & 3);
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float4 v = *(const float4*)(seg + ((c ^ sw) << 4));   // rows 2c, 2c+1
+                        ff_madd(v.x, v.y, uh[2 * c], ul[2 * c], ach[q][0], acl[q][0]);
+                        ff_madd(v.z, v.w, uh[2 * c + 1], ul[2 * c + 1], ach[q][1], acl[q][1]);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    cp_wait<0>();
+    if (accumulate_at) {
+#pragma unroll
+        for (int q = 0; q < NACC; ++q) {
+            const int64_t j = tid + (int64_t)q * blockDim.x;
+            if (j < n) {
+                ff_add(ach[q][0], acl[q][0], ach[q][1], acl[q][1]);
+                a.part[(int64_t)blockIdx.x * n + j] = (double)ach[q][0] + (double)acl[q][0];
+            }
+        }
+    }
+    write_partial(sq, a.sp, 0, red);
+    if (want_b2) write_partial(b2, a.sp, 3, red);
+}
+
 // MODE 0: general staging pass (any n <= 4096), FP64
 // MODE 1: streaming pass, FP64 arithmetic, storage TA
 // MODE 2: streaming pass, float-float arithmetic, storage float2 (TA = double, split copy) or float
@@ -443,7 +610,7 @@ __device__ __forceinline__ void do_pass(const IterArgs& a, double* smem, double 
     if constexpr (MODE == 0) do_pass<TA, NACC, MODE>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
     else if constexpr (MODE == 1) row_pass_stream<TA, false, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
     else if constexpr (std::is_same<TA, double>::value)
-        row_pass_stream<float2, true, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+        row_pass_ff2<NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
     else row_pass_stream<float, true, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
 }
 
@@ -697,21 +864,17 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
         norm_s = norm_s_new;
         // p = s + beta p ; y = M s + beta y   (cg.rs:52-54)
         for (int64_t j = gt; j < n; j += gthreads) a.w[j] = fma(beta, a.w[j], a.vun[j]);
-        {
-            const int lane = threadIdx.x & 31;
-            const int64_t gw = gt >> 5, nwg = gthreads >> 5;
-            for (int64_t r = gw; r < n; r += nwg) {
-                double s;
-                if (a.Mt) {
-                    const double* row = a.Mt + r * n;
-                    s = 0.0;
-                    for (int64_t j = r + lane; j < n; j += 32) s = fma(row[j], a.vun[j], s);
-                    s = warp_sum(s);
-                } else {
-                    s = a.vun[r];
-                }
-                if (lane == 0) a.y[r] = fma(beta, a.y[r], s);
+        if (a.Mt) {
+            __shared__ double red_y[32];
+            for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+                const double* row = a.Mt + r * n;
+                double s = 0.0;
+                for (int64_t j = r + threadIdx.x; j < n; j += blockDim.x) s = fma(row[j], a.vun[j], s);
+                s = block_sum(s, red_y);
+                if (threadIdx.x == 0) a.y[r] = fma(beta, a.y[r], s);
             }
+        } else {
+            for (int64_t r = gt; r < n; r += gthreads) a.y[r] = fma(beta, a.y[r], a.vun[r]);
         }
         if (!grid_sync(a.bar)) return;
     }

@@ -11,22 +11,24 @@
 // carrying the sign of y.  A digit times a sketch entry is an integer of
 // magnitude <= 63*128 < 2^13, so the FP32 tensor-core accumulation of 2048
 // consecutive K (one "window") is an integer below 2^24: exact.  After each
-// window the epilogue warps read the P accumulators from TMEM and fold
-// D_1 2^(7(P-1)) + ... + D_P into int64 registers; at the end of the CTA's
-// K range the sum is scaled by 2^(E_j - 7P - 3) into FP64.  The only
-// rounding is the digit truncation (|error| <= 2^(E_j - 7P - 1) per entry of
-// Y) and the final FP64 conversion; S is applied exactly.
+// window the worker warps read the P accumulators from TMEM, fold
+// D_1 2^(7(P-1)) + ... + D_P exactly in int64, scale by 2^(E_j - 7P - 3)
+// and add the result into the CTA's FP64 partial tile.  The roundings are
+// the digit truncation (|error| <= 2^(E_j - 7P - 1) per entry of Y), one
+// FP64 conversion per window, and the FP64 sums of windows and K chunks;
+// S is applied exactly.
 //
-// Kernel structure (one CTA per SM, 448 threads):
+// Kernel structure (one CTA per SM, 576 threads):
 //   warp 0      loads the digit tiles of Y with cp.async.bulk into a
 //               2-stage ring (mbarrier complete_tx);
 //   warp 1      allocates TMEM (512 columns) and issues tcgen05.mma
 //               (M = 128, N = 96, K = 16, bf16 x bf16 -> f32) from one lane;
-//   warps 2-5   generate the 128 x 64 sketch tile of each stage straight
-//               into shared memory in the SWIZZLE_128B K-major layout: S
-//               never exists in global memory;
-//   warps 6-13  drain TMEM after each window into int64 accumulators and
-//               write the FP64 partial tile of the CTA's K range.
+//   warps 2-17  ("workers") generate the 128 x 64 sketch tile of each stage
+//               straight into shared memory in the SWIZZLE_128B K-major
+//               layout -- S never exists in global memory -- and, after each
+//               window, drain TMEM into int64 accumulators (24 columns per
+//               warp); at the end they write the FP64 partial tile of the
+//               CTA's K range.
 // Split-K partials are summed in a fixed order by a second kernel.
 //
 // Every mbarrier wait is bounded (2 s of globaltimer); on timeout the CTA
@@ -34,6 +36,7 @@
 #include "rnla_internal.h"
 #include <cuda_bf16.h>
 #include <vector>
+#include <cstring>
 
 namespace rnla {
 
@@ -44,7 +47,8 @@ constexpr int BN = 96;            // data columns per CTA tile
 constexpr int BK = 64;            // K per pipeline stage (one 128-byte bf16 row)
 constexpr int WIN = 32;           // stages per exact window (2048 K values)
 constexpr int STAGES = 2;
-constexpr int THREADS = 448;
+constexpr int WORKERS = 16;                          // generator + epilogue warps
+constexpr int THREADS = 64 + 32 * WORKERS;           // + loader warp + MMA warp
 constexpr int S_BYTES = BM * BK * 2;                 // 16 KB sketch tile
 constexpr int ROW_BYTES = BK * 2;                    // 128
 constexpr int YD_BYTES = BN * ROW_BYTES;             // one digit tile, 12 KB
@@ -146,6 +150,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
           "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr));
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 struct Params {
@@ -172,40 +182,84 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return (__float_as_uint(lo) >> 16) | (__float_as_uint(hi) & 0xFFFF0000u);
 }
 
-template <int P>
+// DSMEM helpers: the shared::cluster address of `p` in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa_u32(uint32_t saddr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// local shared -> peer shared bulk copy, completing on the peer's mbarrier
+__device__ __forceinline__ void bulk_s2peer(uint32_t dst_cluster, uint32_t src_cta, uint32_t bytes,
+                                            uint32_t bar_cluster) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            dst_cluster),
+        "r"(src_cta), "r"(bytes), "r"(bar_cluster)
+        : "memory");
+}
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(bar)),
+        "h"(mask)
+        : "memory");
+}
+
+// C = CTAs per cluster along the column tiles of Y.  They apply the same
+// sketch tile, so each generates 1/C of its rows and copies that piece into
+// every peer's stage buffer (cp.async.bulk shared::cta -> shared::cluster);
+// MMA completion is multicast to every peer's `empty` barrier, so no CTA
+// overwrites a stage a peer is still reading.
+template <int P, int C>
 __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sS = smem;                                           // STAGES x 16 KB
     uint8_t* sY = smem + STAGES * S_BYTES;                        // STAGES x P x 12 KB
     uint64_t* bars = (uint64_t*)(sY + STAGES * P * YD_BYTES);
-    uint64_t* fullY = bars;
-    uint64_t* fullS = bars + STAGES;
-    uint64_t* empty = bars + 2 * STAGES;
-    uint64_t* accFull = bars + 3 * STAGES;
+    uint64_t* fullY = bars;                                       // digit tile landed (tx)
+    uint64_t* fullS = bars + STAGES;                              // whole sketch tile present (arrive + tx)
+    uint64_t* empty = bars + 2 * STAGES;                          // every cluster MMA done with the stage
+    uint64_t* genDone = bars + 3 * STAGES;                        // local worker warps wrote their rows
+    uint64_t* accFull = bars + 4 * STAGES;
     uint64_t* accEmpty = accFull + 1;
     uint64_t* drain = accEmpty + 1;
     uint32_t* tmem_slot = (uint32_t*)(drain + 1);
     volatile int* err = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // work unit of this CTA: blockIdx.x = it + tiles_m * (kc + kc_count * jt)
-    const int it = blockIdx.x % prm.tiles_m;
-    const int rest = blockIdx.x / prm.tiles_m;
+    // blockIdx.x = jr + C * (it + tiles_m * (kc + kc_count * jg)), jt = jg * C + jr
+    const uint32_t jr = (C > 1) ? cluster_rank() : 0u;
+    const int rest0 = blockIdx.x / C;
+    const int it = rest0 % prm.tiles_m;
+    const int rest = rest0 / prm.tiles_m;
     const int kc = rest % prm.kc_count;
-    const int jt = rest / prm.kc_count;
+    const int jg = rest / prm.kc_count;
+    const int jt = jg * C + (int)jr;
     const int s_begin = kc * prm.stages_per_kc;
     const int s_end = min(prm.Ks, s_begin + prm.stages_per_kc);
     const int nst = s_end - s_begin;
+    // this CTA's share of the 32 four-row groups of the sketch tile
+    const int g_lo = (32 * (int)jr) / C, g_hi = (32 * ((int)jr + 1)) / C;
+    const uint32_t own_bytes = (uint32_t)(g_hi - g_lo) * 4u * ROW_BYTES;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&fullY[s], 1);
-            mbar_init(&fullS[s], 4);
-            mbar_init(&empty[s], 1);
+            mbar_init(&fullS[s], 1);
+            mbar_init(&empty[s], C);
+            mbar_init(&genDone[s], WORKERS);
         }
         mbar_init(accFull, 1);
-        mbar_init(accEmpty, 8);
+        mbar_init(accEmpty, WORKERS);
         mbar_init(drain, 1);
         *err = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -218,6 +272,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm)
     }
     tc_before();
     __syncthreads();
+    if (C > 1) cluster_sync_all();          // peers' barriers exist before any remote operation
     tc_after();
     const uint32_t tmem = *tmem_slot;
 
@@ -236,7 +291,6 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm)
                     bulk_g2s(sY + (slot * P + p) * YD_BYTES, src + p * YD_BYTES, YD_BYTES, &fullY[slot]);
                 ++issued;
             }
-            // copies still in flight must land before the CTA may exit
             for (int i = (issued > STAGES ? issued - STAGES : 0); i < issued; ++i) {
                 const int slot = i % STAGES;
                 if (!mbar_try(&fullY[slot], (i / STAGES) & 1)) {
@@ -270,110 +324,121 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm)
                         mma_bf16(tmem + p * BN, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
                                  (in_win > 0 || kk > 0) ? 1u : 0u);
                 }
-                mma_commit(&empty[slot]);
+                if (C > 1) mma_commit_mc(&empty[slot], (uint16_t)((1u << C) - 1u));
+                else mma_commit(&empty[slot]);
                 if (in_win == WIN - 1 || i == nst - 1) {
                     mma_commit(accFull);
                     ++win_count;
                 }
             }
-            // every MMA issued by this thread completes before TMEM is released
             mma_commit(drain);
             const unsigned long long t0 = globaltimer_ns();
             while (!mbar_try(drain, 0))
                 if (globaltimer_ns() - t0 > WAIT_NS) { *err = 1; break; }
         }
-    } else if (warp < 6) {
-        // ---------------- sketch generators (128 threads) ----------------
-        const int gt = threadIdx.x - 64;
+    } else {
+        // ---------------- workers: this CTA's rows of each sketch tile, TMEM drain per window ----
+        const int wk = warp - 2;
+        const int wt = threadIdx.x - 64;
         const int64_t i_base = (int64_t)it * BM;
         const uint64_t gstride = (uint64_t)(prm.M4 >> 2);
-        for (int i = 0; i < nst; ++i) {
+        const int q = warp & 3;
+        const int h = wk >> 2;
+        constexpr int CW = BN / 4;
+        const int row = 32 * q + lane;
+        const int tile = it + prm.tiles_m * jt;
+        double* out = prm.partial + ((size_t)kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BN);
+        const int units = (g_hi - g_lo) * 32;          // (4 rows, 2 consecutive k) per unit
+        int win = 0;
+        bool ok = true;
+        for (int i = 0; i < nst && ok; ++i) {
             const int slot = i % STAGES;
             if (i >= STAGES) {
-                bool ok = true;
-                if (lane == 0) ok = mbar_wait(&empty[slot], ((i / STAGES) - 1) & 1, err);
-                ok = __shfl_sync(0xffffffffu, ok, 0);
-                if (!ok) break;
+                bool w_ok = true;
+                if (lane == 0) w_ok = mbar_wait(&empty[slot], ((i / STAGES) - 1) & 1, err);
+                w_ok = __shfl_sync(0xffffffffu, w_ok, 0);
+                if (!w_ok) { ok = false; break; }
             }
             const int64_t k0 = (int64_t)(s_begin + i) * BK;
             uint8_t* dst = sS + slot * S_BYTES;
 #pragma unroll 1
-            for (int r = 0; r < 2; ++r) {
-                const int u = gt + 128 * r;        // unit: 4 rows x 8 consecutive k
-                const int ig = u & 31, kcol = u >> 5;
+            for (int u = wt; u < units; u += 32 * WORKERS) {
+                const int kp = u & 31, ig = g_lo + (u >> 5);
                 const int64_t row0 = i_base + 4 * ig;
-                uint32_t w[4][4];                   // [row][k pair]
-#pragma unroll
-                for (int kk = 0; kk < 8; kk += 2) {
-                    float v0[4], v1[4];
-                    const int64_t k = k0 + kcol * 8 + kk;
-                    if (row0 < prm.M && k < prm.K) sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, v0);
-                    else v0[0] = v0[1] = v0[2] = v0[3] = 0.f;
-                    if (row0 < prm.M && k + 1 < prm.K)
-                        sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, v1);
-                    else v1[0] = v1[1] = v1[2] = v1[3] = 0.f;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        const bool rv = row0 + t < prm.M;
-                        w[t][kk >> 1] = pack_bf16(rv ? v0[t] : 0.f, rv ? v1[t] : 0.f);
-                    }
-                }
+                const int64_t k = k0 + 2 * kp;
+                float v0[4], v1[4];
+                if (row0 < prm.M && k < prm.K) sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, v0);
+                else v0[0] = v0[1] = v0[2] = v0[3] = 0.f;
+                if (row0 < prm.M && k + 1 < prm.K)
+                    sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, v1);
+                else v1[0] = v1[1] = v1[2] = v1[3] = 0.f;
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
-                    const int row = 4 * ig + t;
-                    uint4* q = (uint4*)(dst + row * ROW_BYTES + ((kcol ^ (row & 7)) << 4));
-                    *q = make_uint4(w[t][0], w[t][1], w[t][2], w[t][3]);
+                    const int r = 4 * ig + t;
+                    const bool rv = row0 + t < prm.M;
+                    const int kl = 2 * kp;                      // 0..62 within the stage
+                    uint32_t* qd = (uint32_t*)(dst + r * ROW_BYTES + ((((kl >> 3) ^ (r & 7))) << 4) + ((kl & 7) << 1));
+                    *qd = pack_bf16(rv ? v0[t] : 0.f, rv ? v1[t] : 0.f);
                 }
             }
             fence_proxy_async();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&fullS[slot]);
-        }
-    } else {
-        // ---------------- epilogue (256 threads) ----------------
-        const int q = warp & 3;                       // TMEM lane quadrant of this warp
-        const int h = (warp - 6) >> 2;                // column half: [48h, 48h + 48)
-        const int row = 32 * q + lane;
-        long long acc[BN / 2];
-#pragma unroll
-        for (int c = 0; c < BN / 2; ++c) acc[c] = 0;
-        const int nwin = (nst + WIN - 1) / WIN;
-        bool ok = true;
-        for (int wi = 0; wi < nwin && ok; ++wi) {
-            ok = mbar_wait(accFull, wi & 1, err);
-            if (!ok) break;
-            tc_after();
-#pragma unroll
-            for (int c16 = 0; c16 < BN / 2; c16 += 16) {
-#pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    uint32_t r[16];
-                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(p * BN + h * (BN / 2) + c16), r);
-                    tmem_ld_wait();
-#pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        const long long d = (long long)__float2int_rn(__uint_as_float(r[c]));
-                        acc[c16 + c] += d * (1LL << (7 * (P - 1 - p)));
+            if (lane == 0) mbar_arrive(&genDone[slot]);
+            if (wk == 0 && lane == 0) {
+                // all local rows written: push them to the peers, then announce them locally
+                if (!mbar_wait(&genDone[slot], (i / STAGES) & 1, err)) { ok = false; }
+                else {
+                    if (C > 1) {
+                        const uint32_t src = smem_u32(dst) + (uint32_t)(4 * g_lo * ROW_BYTES);
+                        for (uint32_t pr = 0; pr < (uint32_t)C; ++pr) {
+                            if (pr == jr) continue;
+                            bulk_s2peer(mapa_u32(src, pr), src, own_bytes, mapa_u32(smem_u32(&fullS[slot]), pr));
+                        }
+                        mbar_expect_tx(&fullS[slot], (uint32_t)S_BYTES - own_bytes);
+                    } else {
+                        mbar_arrive(&fullS[slot]);
                     }
                 }
             }
-            tc_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(accEmpty);
-        }
-        if (ok && !*err) {
-            const int tile = it + prm.tiles_m * jt;
-            double* out = prm.partial + ((size_t)kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BN);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            if ((i % WIN) == WIN - 1 || i == nst - 1) {
+                if (!mbar_wait(accFull, win & 1, err)) { ok = false; break; }
+                tc_after();
+#pragma unroll 1
+                for (int c8 = 0; c8 < CW; c8 += 8) {
+                    long long v[8];
 #pragma unroll
-            for (int c = 0; c < BN / 2; ++c) {
-                const int col = h * (BN / 2) + c;
-                const int e = prm.colexp[jt * BN + col];
-                out[(size_t)col * BM + row] = ldexp((double)acc[c], e - 7 * P - 3);
+                    for (int c = 0; c < 8; ++c) v[c] = 0;
+#pragma unroll
+                    for (int p = 0; p < P; ++p) {
+                        uint32_t r[8];
+                        tmem_ld8(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(p * BN + h * CW + c8), r);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            const long long d = (long long)__float2int_rn(__uint_as_float(r[c]));
+                            v[c] += d * (1LL << (7 * (P - 1 - p)));
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        const int col = h * CW + c8 + c;
+                        const double val = ldexp((double)v[c], prm.colexp[jt * BN + col] - 7 * P - 3);
+                        double* o = out + (size_t)col * BM + row;
+                        *o = (win == 0) ? val : *o + val;
+                    }
+                }
+                tc_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(accEmpty);
+                ++win;
             }
         }
     }
     tc_before();
     __syncthreads();
+    if (C > 1) cluster_sync_all();          // no peer still copies into or arrives on this CTA
     tc_after();
     if (warp == 1) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
@@ -516,14 +581,88 @@ __global__ void splitk_sum_kernel(const double* __restrict__ part, int kc_count,
 
 template <int P>
 static size_t smem_bytes() {
-    return 1024 + (size_t)STAGES * S_BYTES + (size_t)STAGES * P * YD_BYTES + 256;
+    return 1024 + (size_t)STAGES * S_BYTES + (size_t)STAGES * P * YD_BYTES + 512;
+}
+
+// cluster sizes that are instantiated; a column-tile count between them is
+// padded with all-zero tiles
+static int pick_cluster(int tiles_n) {
+    static const int sizes[] = {1, 2, 4, 6, 8};
+    if (tiles_n <= 8) {
+        for (int c : sizes) if (c >= tiles_n) return c;
+    }
+    const int groups = (tiles_n + 7) / 8;
+    const int want = (tiles_n + groups - 1) / groups;
+    for (int c : sizes) if (c >= want) return c;
+    return 8;
+}
+
+template <int P, int C>
+static void launch_sketch(Ctx& ctx, const Params& prm, int64_t grid, size_t smem) {
+    auto kfn = sketch_tc_kernel<P, C>;
+    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RNLA_CUDA(cudaLaunchKernelEx(&cfg, kfn, prm));
+    RNLA_LAUNCH_CHECK();
+}
+
+template <int P, int C>
+static bool cluster_fits(size_t smem) {
+    auto kfn = sketch_tc_kernel<P, C>;
+    if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (C == 1) return true;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof cfg);
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kfn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return nclusters > 0;
 }
 
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t K, int64_t N0, int64_t ldy,
                 const double* extra, int64_t M, double* C, int64_t ldc) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
-    const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
+    const int tiles_m = div_up(M, BM), tiles_n_real = div_up(N, BN);
+    const size_t smem = smem_bytes<P>();
+    int CL = (P >= 4) ? pick_cluster(tiles_n_real) : 1;
+    bool fits = true;
+    switch (CL) {
+        case 2: fits = cluster_fits<P, 2>(smem); break;
+        case 4: fits = cluster_fits<P, 4>(smem); break;
+        case 6: fits = cluster_fits<P, 6>(smem); break;
+        case 8: fits = cluster_fits<P, 8>(smem); break;
+        default: break;
+    }
+    if (!fits) CL = 1;
+    const int tiles_n = ((tiles_n_real + CL - 1) / CL) * CL;
     const int Ks = div_up(K, BK);
     const int wins = div_up(Ks, WIN);
     // choose the K split: minimise waves x windows-per-CTA plus partial traffic
@@ -539,7 +678,7 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
         const double cost = (double)waves * wpk + 0.02 * (double)kc_eff * tiles / sm;
         if (cost < best_cost - 1e-9) { best_cost = cost; best_kc = kc_eff; }
     }
-    const int spk = div_up(Ks, best_kc);             // stages per K chunk (multiple of nothing in particular)
+    const int spk = div_up(Ks, best_kc);
     const int kc_count = div_up(Ks, spk);
 
     DevBuf<int> E((size_t)tiles_n * BN, ctx.stream);
@@ -565,12 +704,15 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.kc_count = kc_count; prm.stages_per_kc = spk;
     prm.ydig = dig; prm.colexp = E; prm.partial = part; prm.status = ctx.status;
-    const size_t smem = smem_bytes<P>();
-    RNLA_CUDA(cudaFuncSetAttribute(sketch_tc_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
     const int64_t grid = tiles * kc_count;
-    sketch_tc_kernel<P><<<(unsigned)grid, THREADS, smem, ctx.stream>>>(prm);
-    RNLA_LAUNCH_CHECK();
+    switch (CL) {
+        case 2: launch_sketch<P, 2>(ctx, prm, grid, smem); break;
+        case 4: launch_sketch<P, 4>(ctx, prm, grid, smem); break;
+        case 6: launch_sketch<P, 6>(ctx, prm, grid, smem); break;
+        case 8: launch_sketch<P, 8>(ctx, prm, grid, smem); break;
+        default: launch_sketch<P, 1>(ctx, prm, grid, smem); break;
+    }
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
     splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, C, ldc);
