@@ -12,6 +12,7 @@
 // the same scalars and the run is reproducible.  Grid barriers are bounded
 // (rnla_common.cuh) and end the kernel with a status code on timeout.
 #include "rnla_internal.h"
+#include "rnla_ff.cuh"
 #include <cooperative_groups.h>
 #include <type_traits>
 
@@ -82,14 +83,22 @@ __device__ void trmv_cols(const IterArgs& a, const double* __restrict__ gin, F f
     }
 }
 
-// Sum of per-CTA partial slot `slot`: every CTA runs the same fixed-order
-// reduction (strided per thread, then block_sum), so all CTAs get identical
-// bits without serialising on one thread.
+// Sum of per-CTA partial slot `slot`: warp 0 of every CTA runs the same
+// fixed-order reduction (lanes strided over CTAs, then a butterfly), so all
+// CTAs get identical bits; one warp keeps GB300's slow FP64 pipe lightly used.
 __device__ __forceinline__ double sum_partials(const double* sp, int slot) {
-    __shared__ double red_sp[32];
-    double s = 0.0;
-    for (unsigned c = threadIdx.x; c < gridDim.x; c += blockDim.x) s += sp[c * 4 + slot];
-    return block_sum(s, red_sp);
+    __shared__ double v_sp;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (unsigned c = threadIdx.x; c < gridDim.x; c += 32) s += sp[c * 4 + slot];
+        s = warp_sum(s);
+        if (threadIdx.x == 0) v_sp = s;
+    }
+    __syncthreads();
+    const double r = v_sp;
+    __syncthreads();
+    return r;
 }
 
 // Block sum of a per-thread value, written by thread 0 to sp[cta*4 + slot].
@@ -225,21 +234,6 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, int src
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float bp = s - a;
-    e = (a - (s - bp)) + (b - bp);
-}
-// (sh, sl) += (ah + al) * (yh + yl), dropping al*yl
-__device__ __forceinline__ void ff_madd(float ah, float al, float yh, float yl, float& sh, float& sl) {
-    const float p = __fmul_rn(ah, yh);
-    const float e = __fmaf_rn(ah, yh, -p);
-    const float c = __fmaf_rn(ah, yl, __fmaf_rn(al, yh, e));
-    float t;
-    two_sum(sh, p, sh, t);
-    sl += t + c;
-}
 
 __device__ __forceinline__ void split_ff(double v, float& h, float& l) {
     h = __double2float_rn(v);
@@ -453,12 +447,6 @@ __device__ void row_pass_stream(const IterArgs& a, double* __restrict__ smem_d, 
 // pointer increment, and four independent TwoSum chains hide latency; in the
 // A^T u phase each 16-byte load brings two rows, u sits in registers, and
 // each column keeps two chains.
-__device__ __forceinline__ void ff_add(float& h, float& l, float oh, float ol) {
-    float t;
-    two_sum(h, oh, h, t);
-    l = l + ol + t;
-}
-
 template <int NACC>
 __device__ void row_pass_ff2(const IterArgs& a, double* __restrict__ smem_d, double c1, double c2, double c3,
                              double* __restrict__ vec, bool want_b2, bool accumulate_at) {
@@ -531,14 +519,14 @@ __device__ void row_pass_ff2(const IterArgs& a, double* __restrict__ smem_d, dou
                     ff_madd(av.x, av.y, yv.x, yv.y, h[u], l[u]);
                 }
             }
-            ff_add(h[0], l[0], h[1], l[1]);
-            ff_add(h[2], l[2], h[3], l[3]);
-            ff_add(h[0], l[0], h[2], l[2]);
+            ff_acc(h[0], l[0], h[1], l[1]);
+            ff_acc(h[2], l[2], h[3], l[3]);
+            ff_acc(h[0], l[0], h[2], l[2]);
 #pragma unroll
             for (int o = 8; o < 32; o <<= 1) {
                 const float oh = __shfl_xor_sync(0xffffffffu, h[0], o);
                 const float ol = __shfl_xor_sync(0xffffffffu, l[0], o);
-                ff_add(h[0], l[0], oh, ol);
+                ff_acc(h[0], l[0], oh, ol);
             }
             if (co == 0) ((float2*)rowred)[warp * 16 + rr] = make_float2(h[0], l[0]);
         }
@@ -592,7 +580,7 @@ __device__ void row_pass_ff2(const IterArgs& a, double* __restrict__ smem_d, dou
         for (int q = 0; q < NACC; ++q) {
             const int64_t j = tid + (int64_t)q * blockDim.x;
             if (j < n) {
-                ff_add(ach[q][0], acl[q][0], ach[q][1], acl[q][1]);
+                ff_acc(ach[q][0], acl[q][0], ach[q][1], acl[q][1]);
                 a.part[(int64_t)blockIdx.x * n + j] = (double)ach[q][0] + (double)acl[q][0];
             }
         }
@@ -889,37 +877,13 @@ __global__ void __launch_bounds__(IT_THREADS) cgls_kernel(IterArgs a) {
 // hi + lo carries 48 bits of v.  Values outside the FP32 exponent window
 // fall back to conversions.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float2 split_bits(double v) {
-    const uint64_t b = (uint64_t)__double_as_longlong(v);
-    const int e = (int)((b >> 52) & 0x7ff);
-    if (e < 1023 - 100 || e > 1023 + 100) {
-        if (e == 0 && (b << 1) == 0) return make_float2(__uint_as_float((uint32_t)(b >> 32) & 0x80000000u), 0.f);
-        const float h = __double2float_rn(v);
-        return make_float2(h, __double2float_rn(v - (double)h));
-    }
-    const uint32_t sign = (uint32_t)(b >> 63);
-    const uint64_t M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    uint64_t Mh = (M + (1ull << 28)) >> 29;             // 24-bit significand, rounded half up
-    int eh = e;
-    if (Mh >> 24) { Mh >>= 1; ++eh; }
-    const uint32_t hb = (sign << 31) | ((uint32_t)(eh - 896) << 23) | ((uint32_t)Mh & 0x7FFFFFu);
-    const long long rem = (long long)M - (long long)(Mh << (29 + (eh - e)));   // |rem| <= 2^28
-    float lo = 0.f;
-    if (rem != 0) {
-        const float rf = (float)(sign ? -rem : rem);                          // 24-bit rounding
-        const int be = (int)((__float_as_uint(rf) >> 23) & 0xff) + (e - 1075);  // rescale by 2^(e-1075)
-        if (be > 0) lo = __uint_as_float((__float_as_uint(rf) & 0x807FFFFFu) | ((uint32_t)be << 23));
-    }
-    return make_float2(__uint_as_float(hb), lo);
-}
-
 __global__ void split_ff_kernel(const double* __restrict__ A, int64_t m, int64_t n, int64_t lda,
                                 float2* __restrict__ out, int64_t ldo) {
     const int64_t total = m * n;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = e % m, j = e / m;
-        out[i + j * ldo] = split_bits(A[i + j * lda]);
+        out[i + j * ldo] = ff_split(A[i + j * lda]);
     }
 }
 
@@ -1042,6 +1006,8 @@ LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, 
                       const LsqrParams& prm, double* x, double* var, double* arnorms_dev, bool ffp) {
     if (n > (int64_t)IT_THREADS * IT_MAXACC)
         fail(RNLA_ERR_UNSUPPORTED, "lsqr: n > 4096 is not supported by the fused kernel");
+    if (ffp && a64 && lsqr_ff_supported(n))
+        return lsqr_ff_solve(ctx, a64, m, n, lda, M, b, x0, prm, x, var, arnorms_dev);
     IterArgs a;
     IterBufs B;
     int G;

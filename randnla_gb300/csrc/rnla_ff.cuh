@@ -1,0 +1,116 @@
+// Float-float ("double-float") arithmetic on the FP32 pipe.
+//
+// A value is the unevaluated sum hi + lo of two floats, about 48 significant
+// bits.  The building blocks are the classical error-free transformations:
+// TwoSum (Knuth: s + e = a + b exactly, any magnitudes), FastTwoSum (Dekker:
+// the same when |a| >= |b|) and TwoProduct through one FMA (p + e = a b
+// exactly).  Products drop the lo*lo term.
+//
+// GB300 executes FP64 at 1/64 of the FP32 rate and a dependent FP64
+// operation costs ~64 cycles (a divide or square root several hundred), so
+// vector arithmetic that needs more than FP32 runs in this form instead.
+#pragma once
+#include <cstdint>
+
+namespace rnla {
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    e = b - (s - a);
+}
+
+// (sh, sl) += (ah + al)(bh + bl): exact product of the high parts (FMA error
+// term), TwoSum into the running high part, every low-order term into sl.
+// The accumulator is left unnormalised; ff_norm() renormalises it.
+__device__ __forceinline__ void ff_madd(float ah, float al, float bh, float bl, float& sh, float& sl) {
+    const float p = __fmul_rn(ah, bh);
+    const float e = __fmaf_rn(ah, bh, -p);
+    const float c = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+    float t;
+    two_sum(sh, p, sh, t);
+    sl += t + c;
+}
+
+// (h, l) += (oh, ol) for unnormalised accumulators
+__device__ __forceinline__ void ff_acc(float& h, float& l, float oh, float ol) {
+    float t;
+    two_sum(h, oh, h, t);
+    l = l + ol + t;
+}
+
+__device__ __forceinline__ float2 ff_norm(float h, float l) {
+    float s, e;
+    fast_two_sum(h, l, s, e);
+    return make_float2(s, e);
+}
+
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    float s, e;
+    two_sum(a.x, b.x, s, e);
+    e += a.y + b.y;
+    return ff_norm(s, e);
+}
+
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    float e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e));
+    return ff_norm(p, e);
+}
+
+// a b + c
+__device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return ff_add(ff_mul(a, b), c); }
+
+__device__ __forceinline__ double ff_to_double(float2 a) { return (double)a.x + (double)a.y; }
+
+// FP64 -> (hi, lo) with integer operations only (no FP64 pipe): hi = v
+// rounded to 24 bits (half up in magnitude), lo = the remainder rounded to
+// 24 bits, so hi + lo carries 48 bits of v.  Values outside 2^+-100 take the
+// conversion route.
+__device__ __forceinline__ float2 ff_split(double v) {
+    const uint64_t b = (uint64_t)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e < 1023 - 100 || e > 1023 + 100) {
+        if (e == 0 && (b << 1) == 0) return make_float2(__uint_as_float((uint32_t)(b >> 32) & 0x80000000u), 0.f);
+        const float h = __double2float_rn(v);
+        return make_float2(h, __double2float_rn(v - (double)h));
+    }
+    const uint32_t sign = (uint32_t)(b >> 63);
+    const uint64_t M = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    uint64_t Mh = (M + (1ull << 28)) >> 29;
+    int eh = e;
+    if (Mh >> 24) { Mh >>= 1; ++eh; }
+    const uint32_t hb = (sign << 31) | ((uint32_t)(eh - 896) << 23) | ((uint32_t)Mh & 0x7FFFFFu);
+    const long long rem = (long long)M - (long long)(Mh << (29 + (eh - e)));   // |rem| <= 2^28
+    float lo = 0.f;
+    if (rem != 0) {
+        const float rf = (float)(sign ? -rem : rem);
+        const int be = (int)((__float_as_uint(rf) >> 23) & 0xff) + (e - 1075);
+        if (be > 0) lo = __uint_as_float((__float_as_uint(rf) & 0x807FFFFFu) | ((uint32_t)be << 23));
+    }
+    return make_float2(__uint_as_float(hb), lo);
+}
+
+// Butterfly sum over the warp of an unnormalised accumulator; every lane
+// receives lane 0's result, so all lanes hold identical bits.
+__device__ __forceinline__ float2 ff_warp_sum(float h, float l) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, l, o);
+        ff_acc(h, l, oh, ol);
+    }
+    h = __shfl_sync(0xffffffffu, h, 0);
+    l = __shfl_sync(0xffffffffu, l, 0);
+    return ff_norm(h, l);
+}
+
+}  // namespace rnla

@@ -83,6 +83,12 @@ LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, 
 int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                    int64_t lda, const double* M, const double* b, const double* x0,
                    double tolerance, int64_t num_iterations, double* x, bool* converged);
+// Float-float LSQR (lsqr_ff.cu) on FP64 data, 1 <= n <= 1024; same contract
+// as lsqr_solve.
+bool lsqr_ff_supported(int64_t n);
+LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
+                         const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
+                         double* arnorms_dev);
 // Workspace-based LSQR used by the allocation-free entry point (noalloc.cu).
 size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem,
                             const void** kernel);

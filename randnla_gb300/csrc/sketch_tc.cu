@@ -34,6 +34,7 @@
 // Every mbarrier wait is bounded (2 s of globaltimer); on timeout the CTA
 // records an error, drains its own bulk copies, frees TMEM and exits.
 #include "rnla_internal.h"
+#include "rnla_async.cuh"
 #include <cuda_bf16.h>
 #include <vector>
 #include <cstring>
@@ -54,58 +55,6 @@ constexpr int ROW_BYTES = BK * 2;                    // 128
 constexpr int YD_BYTES = BN * ROW_BYTES;             // one digit tile, 12 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t tx) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(tx)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for the phase with the given parity; false on timeout or
-// when another role already failed.
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* err) {
-    if (mbar_try(b, parity)) return true;
-    const unsigned long long t0 = globaltimer_ns();
-    uint32_t spins = 0;
-    while (!mbar_try(b, parity)) {
-        if (*err) return false;
-        if ((++spins & 63u) == 0u && globaltimer_ns() - t0 > WAIT_NS) {
-            *err = 1;
-            return false;
-        }
-    }
-    return true;
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            smem_u32(dst)),
-        "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void fence_proxy_async() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
