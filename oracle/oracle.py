@@ -58,6 +58,8 @@ def lib():
         L.oracle_sketch_fill.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                          ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_void_p, ctypes.c_int64]
+        L.oracle_qgauss_t.argtypes = [ctypes.c_uint32]
+        L.oracle_qgauss_t.restype = ctypes.c_int
         L.oracle_sketch_fill_quantized.argtypes = [ctypes.c_int, ctypes.c_uint64,
                                                    ctypes.c_uint64, ctypes.c_int64,
                                                    ctypes.c_int64, ctypes.c_void_p,

@@ -26,11 +26,18 @@
  *     +,-,*,/,sqrt and fma, with series for log and sin/cos written from
  *     their Taylor expansions), so the GPU generator and this oracle agree
  *     bit for bit.
+ *   - Quantised Gaussian of the tensor-core sketch: this project's own
+ *     definition, an alias-table sample of round(8 g) clamped to [-63, 63]
+ *     per 32-bit word; the table (rnla_qgauss_table.h, shared data) is
+ *     checked against the exact discretised-Gaussian probabilities by
+ *     tests/test_oracle_rng.py, and the lookup below is written separately
+ *     from the CUDA one.
  *
  * Build: gcc -O2 -ffp-contract=off -fPIC -shared (see oracle/build_oracle.sh).
  * -ffp-contract=off matters: every fused multiply-add below is an explicit
  * fmaf() call, and no other a*b+c may be contracted.
  */
+#include "../randnla_gb300/csrc/rnla_qgauss_table.h"
 #include <stdint.h>
 #include <string.h>
 #include <math.h>
@@ -278,19 +285,28 @@ void oracle_sketch_fill(int dist, int gen, uint64_t key0, uint64_t key1,
             out[i + j * ld] = oracle_sketch_entry(dist, gen, key0, key1, rows, i, j);
 }
 
-/* Quantised Gaussian used by the tensor-core sketch: nearest multiple of
-   1/8, clamped to [-63/8, 63/8]; exactly representable in bf16. */
-float oracle_quantize_eighth(float g) {
-    float t = rintf(g * 8.0f);
-    if (t > 63.0f) t = 63.0f;
-    if (t < -63.0f) t = -63.0f;
-    return t * 0.125f;
+/* Quantised Gaussian used by the tensor-core sketch: t = round(8 g) clamped
+   to [-63, 63], g ~ N(0, 1), drawn from one 32-bit word with the Walker
+   alias table of rnla_qgauss_table.h (generated by make_qgauss_table.py:
+   P(t) = W_t / 2^25).  Entry (i, j) uses word L = i + j*rows4, like every
+   other distribution.  Returns t / 8. */
+static const uint32_t QGAUSS[128] = RNLA_QGAUSS_INIT;
+
+int oracle_qgauss_t(uint32_t u) {
+    uint32_t e = QGAUSS[u >> 25];
+    uint32_t x = (u >> 7) & 0x3FFFFu;
+    uint32_t o = (x < (e & 0x3FFFFu)) ? ((e >> 18) & 0x7Fu) : (e >> 25);
+    return (int)o - 63;
 }
 
 void oracle_sketch_fill_quantized(int gen, uint64_t key0, uint64_t key1,
                                   int64_t rows, int64_t cols, float *out, int64_t ld) {
+    int64_t rows4 = (rows + 3) & ~(int64_t)3;
     for (int64_t j = 0; j < cols; ++j)
-        for (int64_t i = 0; i < rows; ++i)
-            out[i + j * ld] = oracle_quantize_eighth(
-                oracle_sketch_entry(DIST_GAUSSIAN, gen, key0, key1, rows, i, j));
+        for (int64_t i = 0; i < rows; ++i) {
+            uint64_t L = (uint64_t)(i + j * rows4);
+            uint32_t w[4];
+            block_words(gen, key0, key1, L >> 2, w);
+            out[i + j * ld] = (float)oracle_qgauss_t(w[L & 3]) * 0.125f;
+        }
 }

@@ -348,9 +348,16 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     tm.mark();
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
     DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
-    householder_qr(ctx, SK, d, n, nc, d, tau);
-    if (!upper_inverse(ctx, SK, n, d, Mi, n))                       // line 55
-        fail(RNLA_ERR_SINGULAR_MATRIX, "the R factor of the sketch is singular");
+    bool inv_ok;
+    if (o.precision != RNLA_PREC_FP64 && qr_ff_supported(ctx, d, n, nc)) {
+        // float-float factorization on the FP32 pipe (qr_ff.cu)
+        householder_qr_ff(ctx, SK, d, n, nc, d);
+        inv_ok = upper_inverse_ff(ctx, SK, n, d, Mi, n);
+    } else {
+        householder_qr(ctx, SK, d, n, nc, d, tau);
+        inv_ok = upper_inverse(ctx, SK, n, d, Mi, n);               // line 55
+    }
+    if (!inv_ok) fail(RNLA_ERR_SINGULAR_MATRIX, "the R factor of the sketch is singular");
     tm.mark();
     const double* z0 = SK.get() + n * d;
     DevBuf<double> z(n, ctx.stream);

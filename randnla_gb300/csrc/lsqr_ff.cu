@@ -3,19 +3,20 @@
 // (sketch_and_precondition.rs:56), in one persistent cooperative launch.
 //
 // Layout.  The data matrix is re-laid out once per solve as a ROW-MAJOR
-// float-float copy AF: row i holds n (hi, lo) pairs, the row stride ldf is n
-// rounded up to even, padding zero.  A tile of R rows is then one contiguous
-// block that a single cp.async.bulk moves into shared memory, completing on
-// an mbarrier.  Each CTA streams its tiles (tile t = cta + k G) through a
-// 3-stage ring that runs continuously across passes -- A never changes -- so
-// the first tiles of the next pass are in flight while the grid is between
-// passes.
+// float-float copy AF: the row stride ldf is n rounded up to even, and each
+// 16-byte chunk holds a column pair as (hi_2p, hi_2p+1, lo_2p, lo_2p+1), so
+// one load yields two packed f32x2 operands.  A tile of R rows is one
+// contiguous block that a single cp.async.bulk moves into shared memory,
+// completing on an mbarrier.  Each CTA streams its tiles (tile t = cta + k G)
+// through a 3-stage ring that runs continuously across passes -- A never
+// changes -- so the first tiles of the next pass are in flight while the
+// grid is between passes.
 //
-// One pass over a tile (256 threads = 8 warps):
-//   phase 1  warp w forms t_r = (A y)_r for rows r = w, w + 8, ...: each lane
-//            reads 16-byte chunks (two columns) of the row, y sits in
-//            registers, products are exact (FMA error term) and summed with
-//            TwoSum, then a warp butterfly; lane 0 forms
+// One pass over a tile (256 threads = 8 warps, R = 8 RW rows):
+//   phase 1  warp w forms t_r = (A y)_r for rows r = w + 8 s (s < RW): each
+//            lane reads 16-byte chunks of the row, y sits in registers,
+//            products are exact (FMA error term) and summed with TwoSum on
+//            packed pairs, then a warp butterfly; lane s forms
 //            u_r = c1 t_r + c2 u_r + c3 b_r and accumulates ||u||^2;
 //   phase 2  thread t owns the column pairs t + 256 q and accumulates A^T u
 //            over the tile's rows.
@@ -114,24 +115,30 @@ __device__ __forceinline__ void set_status(const Args& a, unsigned int code) {
 //   dst_i = c1 (A y)_i + c2 old_i + c3 bvec_i     (A y skipped when !dot)
 // accumulating sum dst_i^2 (spF slot 0), sum bvec_i^2 (slot 3, want_b2) and,
 // when acc_at, the CTA's partial of A^T dst into partF.
-template <int KP>
-__device__ bool ff_pass(const Args& a, Ring& rg, float2* usm, float2 c1, float2 c2, float2 c3, bool dot,
+// Tile rows: warp w handles rows w + 8 s (s < RW); a 16-byte chunk of a row
+// is one column pair stored (hi_2p, hi_2p+1, lo_2p, lo_2p+1), i.e. two packed
+// f32x2 operands, so every float-float multiply-add below serves two columns.
+template <int KP, int RW>
+__device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, float2 c2, float2 c3, bool dot,
                         const float2* oldv, const float2* bvec, float2* dst, bool want_b2, bool acc_at,
                         volatile int* err) {
-    __shared__ float4 wred[W];
+    constexpr int R = W * RW;
+    __shared__ float2 wred[W][2];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int hp = (int)a.hp;
-    float4 yv[KP];
+    f32x2 yh[KP], nyh[KP], yl[KP];
 #pragma unroll
     for (int k = 0; k < KP; ++k) {
         const int p = lane + 32 * k;
-        yv[k] = (dot && p < hp) ? reinterpret_cast<const float4*>(a.yF)[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
+        if (dot && p < hp) { y0 = a.yF[2 * p]; y1 = a.yF[2 * p + 1]; }
+        yh[k] = pk2(y0.x, y1.x);
+        nyh[k] = pk2(-y0.x, -y1.x);
+        yl[k] = pk2(y0.y, y1.y);
     }
-    float ah[2][2][2], al[2][2][2];      // [pair q][column of pair][row-parity chain]
+    f32x2 ah[2][2], al[2][2];            // phase 2: [pair q][row-parity chain]
 #pragma unroll
-    for (int q = 0; q < 2; ++q)
-#pragma unroll
-        for (int c = 0; c < 2; ++c) { ah[q][c][0] = ah[q][c][1] = al[q][c][0] = al[q][c][1] = 0.f; }
+    for (int q = 0; q < 2; ++q) { ah[q][0] = ah[q][1] = al[q][0] = al[q][1] = 0ull; }
     float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
 
 #pragma unroll 1
@@ -140,40 +147,67 @@ __device__ bool ff_pass(const Args& a, Ring& rg, float2* usm, float2 c1, float2 
         const int st = (int)(s % ST);
         const bool ok = mbar_wait(&rg.full[st], (uint32_t)((s / ST) & 1), err);
         const int64_t t = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
-        const int64_t r0 = t * a.R;
-        const int rows = (int)min((int64_t)a.R, a.m - r0);
-        const float4* tile = rg.tiles + (size_t)st * a.R * hp;
+        const int64_t r0 = t * R;
+        const int rows = (int)min((int64_t)R, a.m - r0);
+        const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
         if (ok) {
-            for (int r = warp; r < rows; r += W) {
-                const int64_t i = r0 + r;
-                float2 uo = make_float2(0.f, 0.f), bb = make_float2(0.f, 0.f);
-                if (lane == 0) {
-                    if (oldv) uo = oldv[i];
-                    if (bvec) bb = bvec[i];
-                }
-                float2 tv = make_float2(0.f, 0.f);
-                if (dot) {
-                    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
-                    const float4* rp = tile + (size_t)r * hp;
+            // lane w prefetches the old value and b of row warp + 8 w
+            float2 uo = make_float2(0.f, 0.f), bb = make_float2(0.f, 0.f);
+            if (lane < RW && warp + W * lane < rows) {
+                const int64_t i = r0 + warp + W * lane;
+                if (oldv) uo = oldv[i];
+                if (bvec) bb = bvec[i];
+            }
+            float tvh[RW], tvl[RW];
 #pragma unroll
-                    for (int kk = 0; kk < KP; ++kk) {
-                        const int p = lane + 32 * kk;
-                        if (p < hp) {
-                            const float4 v = rp[p];
-                            ff_madd(v.x, v.y, yv[kk].x, yv[kk].y, h0, l0);
-                            ff_madd(v.z, v.w, yv[kk].z, yv[kk].w, h1, l1);
+            for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
+            if (dot) {
+                f32x2 sh[RW][2], sl[RW][2];
+#pragma unroll
+                for (int w = 0; w < RW; ++w) { sh[w][0] = sh[w][1] = sl[w][0] = sl[w][1] = 0ull; }
+#pragma unroll
+                for (int kk = 0; kk < KP; ++kk) {
+                    const int p = lane + 32 * kk;
+                    if (p < hp) {
+#pragma unroll
+                        for (int w = 0; w < RW; ++w) {
+                            const ulonglong2 v = tile[(size_t)(warp + W * w) * hp + p];
+                            ff2_madd(v.x, v.y, yh[kk], nyh[kk], yl[kk], sh[w][kk & 1], sl[w][kk & 1]);
                         }
                     }
-                    ff_acc(h0, l0, h1, l1);
-                    tv = ff_warp_sum(h0, l0);
                 }
-                if (lane == 0) {
-                    float2 nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
-                    dst[i] = nv;
-                    usm[r] = nv;
-                    ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
-                    if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
+#pragma unroll
+                for (int w = 0; w < RW; ++w) {
+                    ff2_acc(sh[w][0], sl[w][0], sh[w][1], sl[w][1]);
+                    const float2 H = upk2(sh[w][0]), L = upk2(sl[w][0]);
+                    float h = H.x, l = L.x;
+                    ff_acc(h, l, H.y, L.y);
+                    tvh[w] = h;
+                    tvl[w] = l;
                 }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int w = 0; w < RW; ++w) {
+                        const float oh = __shfl_xor_sync(0xffffffffu, tvh[w], o);
+                        const float ol = __shfl_xor_sync(0xffffffffu, tvl[w], o);
+                        ff_acc(tvh[w], tvl[w], oh, ol);
+                    }
+            }
+            // lane w forms row warp + 8 w (its own butterfly result: all lanes hold the sum)
+            if (lane < RW && warp + W * lane < rows) {
+                float th = tvh[0], tl = tvl[0];
+#pragma unroll
+                for (int w = 1; w < RW; ++w)
+                    if (lane == w) { th = tvh[w]; tl = tvl[w]; }
+                const int r = warp + W * lane;
+                const int64_t i = r0 + r;
+                const float2 tv = ff_norm(th, tl);
+                const float2 nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
+                dst[i] = nv;
+                usm[r] = make_ulonglong2(pk2(nv.x, nv.x), pk2(nv.y, nv.y));
+                ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
+                if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
             }
         }
         __syncthreads();
@@ -181,29 +215,28 @@ __device__ bool ff_pass(const Args& a, Ring& rg, float2* usm, float2 c1, float2 
         if (acc_at) {
             int r = 0;
             for (; r + 1 < rows; r += 2) {
-                const float2 u0 = usm[r], u1 = usm[r + 1];
+                const ulonglong2 u0 = usm[r], u1 = usm[r + 1];
+                const f32x2 nu0 = neg2(u0.x), nu1 = neg2(u1.x);
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const int p = tid + q * T;
                     if (p < hp) {
-                        const float4 v0 = tile[(size_t)r * hp + p];
-                        const float4 v1 = tile[(size_t)(r + 1) * hp + p];
-                        ff_madd(v0.x, v0.y, u0.x, u0.y, ah[q][0][0], al[q][0][0]);
-                        ff_madd(v0.z, v0.w, u0.x, u0.y, ah[q][1][0], al[q][1][0]);
-                        ff_madd(v1.x, v1.y, u1.x, u1.y, ah[q][0][1], al[q][0][1]);
-                        ff_madd(v1.z, v1.w, u1.x, u1.y, ah[q][1][1], al[q][1][1]);
+                        const ulonglong2 v0 = tile[(size_t)r * hp + p];
+                        const ulonglong2 v1 = tile[(size_t)(r + 1) * hp + p];
+                        ff2_madd(v0.x, v0.y, u0.x, nu0, u0.y, ah[q][0], al[q][0]);
+                        ff2_madd(v1.x, v1.y, u1.x, nu1, u1.y, ah[q][1], al[q][1]);
                     }
                 }
             }
             if (r < rows) {
-                const float2 u0 = usm[r];
+                const ulonglong2 u0 = usm[r];
+                const f32x2 nu0 = neg2(u0.x);
 #pragma unroll
                 for (int q = 0; q < 2; ++q) {
                     const int p = tid + q * T;
                     if (p < hp) {
-                        const float4 v0 = tile[(size_t)r * hp + p];
-                        ff_madd(v0.x, v0.y, u0.x, u0.y, ah[q][0][0], al[q][0][0]);
-                        ff_madd(v0.z, v0.w, u0.x, u0.y, ah[q][1][0], al[q][1][0]);
+                        const ulonglong2 v0 = tile[(size_t)r * hp + p];
+                        ff2_madd(v0.x, v0.y, u0.x, nu0, u0.y, ah[q][0], al[q][0]);
                     }
                 }
             }
@@ -218,21 +251,24 @@ __device__ bool ff_pass(const Args& a, Ring& rg, float2* usm, float2 c1, float2 
         for (int q = 0; q < 2; ++q) {
             const int p = tid + q * T;
             if (p < hp) {
-                ff_acc(ah[q][0][0], al[q][0][0], ah[q][0][1], al[q][0][1]);
-                ff_acc(ah[q][1][0], al[q][1][0], ah[q][1][1], al[q][1][1]);
-                const float2 c0 = ff_norm(ah[q][0][0], al[q][0][0]);
-                const float2 c1v = ff_norm(ah[q][1][0], al[q][1][0]);
+                ff2_acc(ah[q][0], al[q][0], ah[q][1], al[q][1]);
+                const float2 H = upk2(ah[q][0]), L = upk2(al[q][0]);
+                const float2 c0 = ff_norm(H.x, L.x), c1v = ff_norm(H.y, L.y);
                 P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
             }
         }
     }
-    if (lane == 0) wred[warp] = make_float4(sqh, sql, b2h, b2l);
+    {
+        const float2 sq = ff_warp_sum(sqh, sql);
+        const float2 b2 = ff_warp_sum(b2h, b2l);
+        if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
+    }
     __syncthreads();
     if (tid == 0) {
         float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
         for (int w = 0; w < W; ++w) {
-            ff_acc(h, l, wred[w].x, wred[w].y);
-            ff_acc(h2, l2, wred[w].z, wred[w].w);
+            ff_acc(h, l, wred[w][0].x, wred[w][0].y);
+            ff_acc(h2, l2, wred[w][1].x, wred[w][1].y);
         }
         a.spF[blockIdx.x * 4 + 0] = ff_norm(h, l);
         a.spF[blockIdx.x * 4 + 3] = ff_norm(h2, l2);
@@ -344,8 +380,8 @@ __device__ __forceinline__ double lane_rsqrt(double arg) { return arg > 0.0 ? rs
 
 __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-template <int KP>
-__global__ void __launch_bounds__(T, (KP <= 8 ? 2 : 1)) lsqr_ff_kernel(Args a) {
+template <int KP, int RW>
+__global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t full[ST];
     __shared__ Bcast bc;
@@ -362,7 +398,7 @@ __global__ void __launch_bounds__(T, (KP <= 8 ? 2 : 1)) lsqr_ff_kernel(Args a) {
     rg.cnt = 0;
     rg.issued = 0;
     rg.ntl = (blockIdx.x < a.ntiles) ? (a.ntiles - blockIdx.x + G - 1) / G : 0;
-    float2* usm = reinterpret_cast<float2*>(dsm + (size_t)ST * a.R * a.ldf * 8);
+    ulonglong2* usm = reinterpret_cast<ulonglong2*>(dsm + (size_t)ST * a.R * a.ldf * 8);
     volatile int* err = &err_s;
     if (tid == 0) {
         err_s = 0;
@@ -381,7 +417,7 @@ __global__ void __launch_bounds__(T, (KP <= 8 ? 2 : 1)) lsqr_ff_kernel(Args a) {
     } while (0)
 #define LSFF_PASS(...)                                             \
     do {                                                           \
-        if (!ff_pass<KP>(a, rg, usm, __VA_ARGS__, err)) {          \
+        if (!ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err)) {      \
             set_status(a, KSTATUS_BARRIER_TIMEOUT);                \
             ring_drain(rg);                                        \
             return;                                                \
@@ -651,10 +687,11 @@ __global__ void __launch_bounds__(T, (KP <= 8 ? 2 : 1)) lsqr_ff_kernel(Args a) {
 #undef LSFF_PASS
 }
 
-// Row-major float-float copy: AF[i * ldf + j] = split(A[i + j lda]), zero
-// for j in [n, ldf).  32 x 32 tiles through shared memory.
+// Row-major float-float copy in column-pair order: row i is hp = ldf / 2
+// chunks of 16 bytes, chunk p = (hi_2p, hi_2p+1, lo_2p, lo_2p+1); zero for
+// columns in [n, ldf).  32 x 32 tiles through shared memory.
 __global__ void rowmajor_split_kernel(const double* __restrict__ A, int64_t m, int64_t n, int64_t lda,
-                                      float2* __restrict__ AF, int64_t ldf) {
+                                      float* __restrict__ AF, int64_t ldf) {
     __shared__ float2 tile[32][33];
     const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
     for (int k = threadIdx.y; k < 32; k += 8) {
@@ -666,7 +703,12 @@ __global__ void rowmajor_split_kernel(const double* __restrict__ A, int64_t m, i
     __syncthreads();
     for (int k = threadIdx.y; k < 32; k += 8) {
         const int64_t i = i0 + k, j = j0 + threadIdx.x;
-        if (i < m && j < ldf) AF[i * ldf + j] = tile[threadIdx.x][k];
+        if (i < m && j < ldf) {
+            const float2 v = tile[threadIdx.x][k];
+            float* row = AF + i * 2 * ldf + 4 * (j >> 1) + (j & 1);
+            row[0] = v.x;
+            row[2] = v.y;
+        }
     }
 }
 
@@ -687,15 +729,18 @@ __global__ void msplit_kernel(const double* __restrict__ M, int64_t n, int64_t l
     }
 }
 
-template <int KP>
-static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP>; }
+template <int KP, int RW>
+static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW>; }
 
-static const void* pick_kernel(int64_t hp) {
-    if (hp <= 32) return kernel_kp<1>();
-    if (hp <= 64) return kernel_kp<2>();
-    if (hp <= 128) return kernel_kp<4>();
-    if (hp <= 256) return kernel_kp<8>();
-    return kernel_kp<16>();
+// (kernel, rows per warp) for hp column pairs: the y registers cover hp, and
+// a tile of 8 RW rows stays within 64 KB.
+static const void* pick_kernel(int64_t hp, int& RW) {
+    if (hp <= 32) { RW = 4; return kernel_kp<1, 4>(); }
+    if (hp <= 64) { RW = 4; return kernel_kp<2, 4>(); }
+    if (hp <= 128) { RW = 2; return kernel_kp<4, 2>(); }
+    if (hp <= 256) { RW = 2; return kernel_kp<8, 2>(); }
+    RW = 1;
+    return kernel_kp<16, 1>();
 }
 
 }  // namespace lsff
@@ -710,11 +755,10 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     cudaStream_t st = ctx.stream;
     const int64_t ldf = (n + 1) & ~1LL;
     const int64_t hp = ldf / 2;
-    int mult = (int)(32768 / (64 * ldf));
-    mult = mult < 1 ? 1 : (mult > 8 ? 8 : mult);
-    const int R = 8 * mult;
-    const size_t smem = (size_t)ST * R * ldf * 8 + (size_t)R * 8;
-    const void* k = pick_kernel(hp);
+    int RW = 1;
+    const void* k = pick_kernel(hp, RW);
+    const int R = W * RW;
+    const size_t smem = (size_t)ST * R * ldf * 8 + (size_t)R * 16;
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
@@ -743,7 +787,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), st));
     {
         dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
-        rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, AF, ldf);
+        rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, reinterpret_cast<float*>(AF.get()), ldf);
         RNLA_LAUNCH_CHECK();
         int g = (int)div_up(m, 256);
         if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;

@@ -71,6 +71,31 @@ __device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return 
 
 __device__ __forceinline__ double ff_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
+// a / b: two-term long division (Dekker): q1 = a.hi / b.hi, q2 from the
+// float-float remainder a - q1 b; relative error ~2^-46.
+__device__ __forceinline__ float2 ff_div(float2 a, float2 b) {
+    const float q1 = __fdiv_rn(a.x, b.x);
+    const float2 r = ff_add(a, ff_neg(ff_mul(make_float2(q1, 0.f), b)));
+    const float q2 = __fdiv_rn(r.x, b.x);
+    return ff_norm(q1, q2);
+}
+
+// sqrt(a), a >= 0 (Karp and Markstein): y = a.hi rsqrt(a.hi), then two
+// Newton corrections y + (a - y^2) / (2 y), the residual a - y^2 formed in
+// float-float each time.
+__device__ __forceinline__ float2 ff_sqrt(float2 a) {
+    if (!(a.x > 0.f)) return make_float2(0.f, 0.f);
+    const float x = rsqrtf(a.x);
+    const float hx = __fmul_rn(x, 0.5f);
+    const float y = __fmul_rn(a.x, x);
+    const float p = __fmul_rn(y, y);
+    const float e = __fmaf_rn(y, y, -p);
+    const float2 r = ff_add(a, make_float2(-p, -e));
+    const float2 y2 = ff_norm(y, __fmul_rn(r.x, hx));
+    const float2 r2 = ff_add(a, ff_neg(ff_mul(y2, y2)));
+    return ff_add(y2, make_float2(__fmul_rn(r2.x, hx), 0.f));
+}
+
 // FP64 -> (hi, lo) with integer operations only (no FP64 pipe): hi = v
 // rounded to 24 bits (half up in magnitude), lo = the remainder rounded to
 // 24 bits, so hi + lo carries 48 bits of v.  Values outside 2^+-100 take the
@@ -111,6 +136,74 @@ __device__ __forceinline__ float2 ff_warp_sum(float h, float l) {
     h = __shfl_sync(0xffffffffu, h, 0);
     l = __shfl_sync(0xffffffffu, l, 0);
     return ff_norm(h, l);
+}
+
+}  // namespace rnla
+
+// ---------------------------------------------------------------------------
+// Packed pairs: two independent FP32 values in one 64-bit register pair,
+// operated on by the sm_100+ .f32x2 instructions (one instruction, two
+// IEEE round-to-nearest results).  ff2_* apply the float-float operations
+// above to two independent lanes at once.
+// ---------------------------------------------------------------------------
+namespace rnla {
+
+typedef unsigned long long f32x2;
+
+__device__ __forceinline__ f32x2 pk2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 r) {
+    float a, b;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+    return make_float2(a, b);
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 neg2(f32x2 a) { return a ^ 0x8000000080000000ull; }
+
+// (sh, sl) += (ah + al)(bh + bl) on both lanes (see ff_madd); nbh = -bh is
+// passed in (b is reused across many a, so the negation is hoisted) and the
+// TwoSum is written around -p: 12 instructions for two multiply-adds.
+__device__ __forceinline__ void ff2_madd(f32x2 ah, f32x2 al, f32x2 bh, f32x2 nbh, f32x2 bl, f32x2& sh,
+                                         f32x2& sl) {
+    const f32x2 np = mul2(ah, nbh);                        // -p, p = ah bh
+    const f32x2 e = fma2(ah, bh, np);                      // ah bh - p, exact
+    const f32x2 c = fma2(ah, bl, fma2(al, bh, e));
+    const f32x2 s = sub2(sh, np);                          // sh + p
+    const f32x2 bp = sub2(s, sh);
+    const f32x2 t = sub2(sub2(sh, sub2(s, bp)), add2(np, bp));
+    sh = s;
+    sl = add2(sl, add2(t, c));
+}
+
+// (h, l) += (oh, ol) on both lanes (see ff_acc)
+__device__ __forceinline__ void ff2_acc(f32x2& h, f32x2& l, f32x2 oh, f32x2 ol) {
+    const f32x2 s = add2(h, oh);
+    const f32x2 bp = sub2(s, h);
+    const f32x2 t = add2(sub2(h, sub2(s, bp)), sub2(oh, bp));
+    h = s;
+    l = add2(add2(l, ol), t);
 }
 
 }  // namespace rnla

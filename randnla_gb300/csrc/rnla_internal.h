@@ -39,6 +39,14 @@ void householder_qr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64
 // Thin Q (m x n) from the reflectors stored in V (m x n, ld) and tau.
 void householder_form_q(Ctx& ctx, const double* V, int64_t m, int64_t n, int64_t ldv,
                         const double* tau, double* Q, int64_t ldq);
+// Float-float Householder QR (qr_ff.cu): R in the upper triangle of X and
+// Q^T applied to columns n..nc-1 (reflectors are not kept); the same
+// contract as householder_qr without tau.  Supported when the column blocks
+// fit in shared memory.
+bool qr_ff_supported(const Ctx& ctx, int64_t m, int64_t n, int64_t nc);
+void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld);
+// Float-float R^-1 (qr_ff.cu); false on an exactly zero pivot (synchronises).
+bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi);
 // Rinv (n x n, upper) = R^-1; returns false on an exactly zero pivot (synchronises).
 bool upper_inverse(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi);
 // back substitution with the reference's zero-pivot rule (solvers.rs:22-41)

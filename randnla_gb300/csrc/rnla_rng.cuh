@@ -12,6 +12,7 @@
 // reproduce every value exactly.
 #pragma once
 #include <cstdint>
+#include "rnla_qgauss_table.h"
 
 namespace rnla {
 
@@ -130,12 +131,17 @@ __device__ __forceinline__ float uniform_pm1(uint32_t a) {
     return __fadd_rn(__fmul_rn((float)((int32_t)(a >> 8) - 0x800000), 0x1p-23f), 0x1p-24f);
 }
 
-// Nearest multiple of 1/8, clamped to +-63/8: exact in bf16, and the digit
-// products of the tensor-core sketch stay below 2^13.
-__device__ __forceinline__ float quantize_eighth(float g) {
-    float t = rintf(__fmul_rn(g, 8.0f));
-    t = fminf(fmaxf(t, -63.0f), 63.0f);
-    return __fmul_rn(t, 0.125f);
+// Quantised Gaussian of the tensor-core sketch: t = round(8 g) clamped to
+// [-63, 63] for g ~ N(0, 1), drawn from one 32-bit word through the alias
+// table of rnla_qgauss_table.h (P(t) = W_t / 2^25).  t / 8 is exact in bf16
+// and the digit products of the tensor-core sketch stay below 2^13.
+static __device__ const uint32_t k_qgauss_table[128] = RNLA_QGAUSS_INIT;
+
+__device__ __forceinline__ int qgauss_t(uint32_t u, const uint32_t* tab) {
+    const uint32_t e = tab[u >> 25];
+    const uint32_t x = (u >> 7) & 0x3FFFFu;
+    const uint32_t o = (x < (e & 0x3FFFFu)) ? ((e >> 18) & 0x7Fu) : (e >> 25);
+    return (int)o - 63;
 }
 
 // The four entries generated by block g for distribution `dist`.

@@ -121,15 +121,18 @@ __global__ void sketch_fill_kernel(RngKey key, int dist, int64_t rows, int64_t c
         const int64_t j = (int64_t)(g / (uint64_t)bpc);
         const int64_t i0 = 4 * (int64_t)(g % (uint64_t)bpc);
         float v[4];
-        block_entries(key, dist, g, v);
+        if (QUANT) {
+            uint32_t w[4];
+            block_words(key, g, w);
+#pragma unroll
+            for (int t = 0; t < 4; ++t) v[t] = __fmul_rn((float)qgauss_t(w[t], k_qgauss_table), 0.125f);
+        } else {
+            block_entries(key, dist, g, v);
+        }
         T* col = out + j * ld;
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            if (i0 + t < rows) {
-                const float e = QUANT ? quantize_eighth(v[t]) : v[t];
-                col[i0 + t] = (T)e;
-            }
-        }
+        for (int t = 0; t < 4; ++t)
+            if (i0 + t < rows) col[i0 + t] = (T)v[t];
     }
 }
 

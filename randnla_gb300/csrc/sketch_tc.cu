@@ -120,10 +120,12 @@ struct Params {
 
 // 8x the 4 quantised sketch entries of block g (rows 4q..4q+3 of stream
 // column k): the integers t in [-63, 63]; the 1/8 goes into the final scale.
-__device__ __forceinline__ void sketch_block(const RngKey& key, uint64_t g, float v[4]) {
-    block_entries(key, DIST_GAUSSIAN, g, v);
+// The four quantised entries t (integers, |t| <= 63) of block g.
+__device__ __forceinline__ void sketch_block(const RngKey& key, uint64_t g, const uint32_t* tab, float v[4]) {
+    uint32_t w[4];
+    block_words(key, g, w);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) v[t] = __fmul_rn(quantize_eighth(v[t]), 8.0f);
+    for (int t = 0; t < 4; ++t) v[t] = (float)qgauss_t(w[t], tab);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -170,6 +172,7 @@ __device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
 template <int P, int C>
 __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
+    __shared__ uint32_t qtab[128];                                // quantised-Gaussian alias table
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sS = smem;                                           // STAGES x 16 KB
     uint8_t* sY = smem + STAGES * S_BYTES;                        // STAGES x P x 12 KB
@@ -200,6 +203,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm)
     const int g_lo = (32 * (int)jr) / C, g_hi = (32 * ((int)jr + 1)) / C;
     const uint32_t own_bytes = (uint32_t)(g_hi - g_lo) * 4u * ROW_BYTES;
 
+    if (threadIdx.x < 128) qtab[threadIdx.x] = k_qgauss_table[threadIdx.x];
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&fullY[s], 1);
@@ -316,10 +320,10 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_tc_kernel(const Params prm)
                 const int64_t row0 = i_base + 4 * ig;
                 const int64_t k = k0 + 2 * kp;
                 float v0[4], v1[4];
-                if (row0 < prm.M && k < prm.K) sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, v0);
+                if (row0 < prm.M && k < prm.K) sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, qtab, v0);
                 else v0[0] = v0[1] = v0[2] = v0[3] = 0.f;
                 if (row0 < prm.M && k + 1 < prm.K)
-                    sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, v1);
+                    sketch_block(prm.key, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, qtab, v1);
                 else v1[0] = v1[1] = v1[2] = v1[3] = 0.f;
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
