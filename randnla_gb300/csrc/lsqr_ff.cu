@@ -8,34 +8,39 @@
 // one load yields two packed f32x2 operands.  A tile of R rows is one
 // contiguous block that a single cp.async.bulk moves into shared memory,
 // completing on an mbarrier.  Each CTA streams its tiles (tile t = cta + k G)
-// through a 3-stage ring that runs continuously across passes -- A never
-// changes -- so the first tiles of the next pass are in flight while the
-// grid is between passes.
+// through a ring of ST stages (up to 192 KB) that runs continuously across
+// passes -- A never changes -- so the first tiles of the next pass are in
+// flight while the grid is between passes.
 //
-// One pass over a tile (256 threads = 8 warps, R = 8 RW rows):
-//   phase 1  warp w forms t_r = (A y)_r for rows r = w + 8 s (s < RW): each
-//            lane reads 16-byte chunks of the row, y sits in registers,
-//            products are exact (FMA error term) and summed with TwoSum on
-//            packed pairs, then a warp butterfly; lane s forms
-//            u_r = c1 t_r + c2 u_r + c3 b_r and accumulates ||u||^2;
-//   phase 2  thread t owns the column pairs t + 256 q and accumulates A^T u
-//            over the tile's rows.
-// Both phases read 512 contiguous bytes per warp instruction (no bank
+// One pass (512 threads, two warp roles working on consecutive tiles):
+//   row warps 0-7     tile k: warp w forms t_r = (A y)_r for rows
+//                     r = w + 8 s (s < RW): 16-byte chunks of the row, y in
+//                     registers, exact FMA products summed with TwoSum on
+//                     packed pairs, a warp butterfly; lane s then forms
+//                     u_r = c1 t_r + c2 u_r + c3 b_r, accumulates ||u||^2 and
+//                     hands u to the column warps (double-buffered, named
+//                     barriers: bar.arrive "u ready", bar.sync "u consumed");
+//   column warps 8-15 tile k - 1: thread t owns the column pairs t + 256 q
+//                     and accumulates A^T u over the tile's rows, then frees
+//                     the ring stage and issues the next bulk copy.
+// Both roles read 512 contiguous bytes per warp instruction (no bank
 // conflicts).  Per-CTA partials are summed in a fixed order, so the run is
 // reproducible.
 //
 // Arithmetic.  Every vector operation is float-float on the FP32 pipe.  FP64
-// is used only by warp 0 of each CTA for the scalar recurrences: on GB300 a
-// dependent FP64 operation takes ~64 cycles and a divide or square root
-// several hundred, so the recurrences are arranged as a few lane-parallel
-// rsqrt steps (different lanes of one warp instruction evaluate independent
-// reciprocal square roots) plus multiplies; divisions become products with
-// those reciprocals.  Results agree with the FP64 LSQR to float-float
-// accuracy, and the iteration count can differ by one at a tolerance
-// boundary.
+// is used only by warp 0 of each CTA for the scalar recurrences (state kept
+// in shared memory): on GB300 a dependent FP64 operation takes ~64 cycles and
+// a divide or square root several hundred, so the recurrences are arranged as
+// a few lane-parallel rsqrt steps (different lanes of one warp instruction
+// evaluate independent reciprocal square roots) plus multiplies; divisions
+// become products with those reciprocals.  Results agree with the FP64 LSQR
+// to float-float accuracy, and the iteration count can differ by one at a
+// tolerance boundary.
 //
 // Waits are bounded: the grid barrier and the tile mbarriers give up after
-// 2 s, record a status, let the CTA's own bulk copies land and return.
+// 2 s and record a status; the named-barrier hand-offs still run to the end
+// of the pass (no role leaves early), then the CTA lets its own bulk copies
+// land and returns.
 #include "rnla_internal.h"
 #include "rnla_ff.cuh"
 #include "rnla_async.cuh"
@@ -43,15 +48,22 @@
 namespace rnla {
 namespace lsff {
 
-constexpr int T = 256;          // threads per CTA
+constexpr int T = 512;          // threads per CTA
 constexpr int W = T / 32;       // warps per CTA
-constexpr int ST = 3;           // tile ring depth
+constexpr int WA = 8;           // row warps (0..7); warps 8..15 are column warps
+constexpr int TB = T - 32 * WA; // column threads
+constexpr int MAX_ST = 6;       // ring stages
+constexpr size_t RING_BYTES = 192 * 1024;
 constexpr int64_t MAX_N = 1024;
+// named barriers (0 is __syncthreads)
+constexpr int NB_URDY = 1;      // + (k & 1): u of tile k written
+constexpr int NB_UFREE = 3;     // + (k & 1): u of tile k consumed
 
 struct Args {
     const float2* AF;           // row-major float-float copy of A, m x ldf
     int64_t m, n, ldf, hp;      // hp = ldf / 2 column pairs
     int R;                      // rows per tile (multiple of 8)
+    int ST;                     // ring stages
     int64_t ntiles;
     const float2* MF;           // M, column-major n x n (null: identity)
     const float2* MtF;          // M^T, column-major (row i of M contiguous)
@@ -76,35 +88,65 @@ struct Bcast {
     int istop;
 };
 
+// Scalar state of the recurrences (warp 0).
+struct Scal {
+    double alfa, beta, bnorm, ibn, us;
+    double rhobar, phibar, rnorm, r1norm, r2norm, anorm, acond, ddnorm, res2, xnorm, xxnorm, z, cs2, sn2, arnorm;
+    double rho, irho, c, s, phi, tau, psi;
+    int istop;
+};
+
+// Tile ring.  Every thread tracks the stage and mbarrier phase of the next
+// tile to consume; the issuing thread also tracks the next stage to fill, the
+// next tile (index into this CTA's tile list) and the copies in flight.  All
+// counters advance by increment and wrap: no integer division in the loop.
 struct Ring {
     uint64_t* full;             // ST mbarriers
     float4* tiles;              // ST stages of R x hp float4
-    int64_t cnt;                // sequence number of the next tile to consume
-    int64_t issued;             // sequence number of the next tile to issue (thread 0)
     int64_t ntl;                // tiles of this CTA per pass
+    int cst;                    // stage of the next tile to consume
+    uint32_t cph;               // its phase parity
+    int ist;                    // issuer: next stage to fill
+    int64_t ik;                 // issuer: next tile index (0..ntl-1)
+    int inflight;               // issuer: issued and not yet consumed
 };
+
+constexpr int ISSUER = 32 * WA;  // first column thread issues the bulk copies
+
+__device__ __forceinline__ void nb_sync(int id) { asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(T) : "memory"); }
+__device__ __forceinline__ void nb_arrive(int id) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "n"(T) : "memory"); }
 
 __device__ __forceinline__ void ring_issue(const Args& a, Ring& rg) {
     if (rg.ntl == 0) return;
-    while (rg.issued < rg.cnt + ST) {
-        const int64_t t = (int64_t)blockIdx.x + (rg.issued % rg.ntl) * (int64_t)gridDim.x;
+    while (rg.inflight < a.ST) {
+        const int64_t t = (int64_t)blockIdx.x + rg.ik * (int64_t)gridDim.x;
         const int64_t r0 = t * a.R;
         const int64_t rows = min((int64_t)a.R, a.m - r0);
         const uint32_t bytes = (uint32_t)(rows * a.ldf * 8);
-        const int st = (int)(rg.issued % ST);
-        mbar_expect_tx(&rg.full[st], bytes);
-        bulk_g2s(rg.tiles + (size_t)st * a.R * a.hp, a.AF + r0 * a.ldf, bytes, &rg.full[st]);
-        ++rg.issued;
+        mbar_expect_tx(&rg.full[rg.ist], bytes);
+        bulk_g2s(rg.tiles + (size_t)rg.ist * a.R * a.hp, a.AF + r0 * a.ldf, bytes, &rg.full[rg.ist]);
+        rg.ist = (rg.ist + 1 == a.ST) ? 0 : rg.ist + 1;
+        rg.ik = (rg.ik + 1 == rg.ntl) ? 0 : rg.ik + 1;
+        ++rg.inflight;
     }
 }
 
-// Thread 0: wait (bounded) until every copy still in flight has landed, so
-// the CTA can exit with no bulk copy writing into its shared memory.
-__device__ void ring_drain(Ring& rg) {
-    if (threadIdx.x != 0) return;
+__device__ __forceinline__ void ring_advance(const Args& a, Ring& rg) {
+    if (++rg.cst == a.ST) { rg.cst = 0; rg.cph ^= 1u; }
+}
+
+// Issuing thread: wait (bounded) until every copy still in flight has
+// landed, so the CTA can exit with no bulk copy writing into its shared
+// memory.
+__device__ void ring_drain(const Args& a, Ring& rg) {
+    if (threadIdx.x != ISSUER) return;
     volatile int quiet = 0;
-    for (int64_t s = rg.cnt; s < rg.issued; ++s)
-        mbar_wait(&rg.full[s % ST], (uint32_t)((s / ST) & 1), &quiet);
+    int st = rg.cst;
+    uint32_t ph = rg.cph;
+    for (int c = 0; c < rg.inflight; ++c) {
+        mbar_wait(&rg.full[st], ph, &quiet);
+        if (++st == a.ST) { st = 0; ph ^= 1u; }
+    }
 }
 
 __device__ __forceinline__ void set_status(const Args& a, unsigned int code) {
@@ -114,54 +156,65 @@ __device__ __forceinline__ void set_status(const Args& a, unsigned int code) {
 // One pass over the CTA's tiles:
 //   dst_i = c1 (A y)_i + c2 old_i + c3 bvec_i     (A y skipped when !dot)
 // accumulating sum dst_i^2 (spF slot 0), sum bvec_i^2 (slot 3, want_b2) and,
-// when acc_at, the CTA's partial of A^T dst into partF.
-// Tile rows: warp w handles rows w + 8 s (s < RW); a 16-byte chunk of a row
-// is one column pair stored (hi_2p, hi_2p+1, lo_2p, lo_2p+1), i.e. two packed
-// f32x2 operands, so every float-float multiply-add below serves two columns.
+// when acc_at, the CTA's partial of A^T dst into partF.  Returns false if a
+// tile wait failed (after completing the hand-off protocol).
 template <int KP, int RW>
 __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, float2 c2, float2 c3, bool dot,
                         const float2* oldv, const float2* bvec, float2* dst, bool want_b2, bool acc_at,
                         volatile int* err) {
-    constexpr int R = W * RW;
-    __shared__ float2 wred[W][2];
+    constexpr int R = WA * RW;
+    __shared__ float2 wred[WA][2];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int hp = (int)a.hp;
-    f32x2 yh[KP], nyh[KP], yl[KP];
+    const int64_t ntl = rg.ntl;
+    if (warp < WA) {
+        // ---------------- row warps ----------------
+        f32x2 yh[KP], nyh[KP], yl[KP];
 #pragma unroll
-    for (int k = 0; k < KP; ++k) {
-        const int p = lane + 32 * k;
-        float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
-        if (dot && p < hp) { y0 = a.yF[2 * p]; y1 = a.yF[2 * p + 1]; }
-        yh[k] = pk2(y0.x, y1.x);
-        nyh[k] = pk2(-y0.x, -y1.x);
-        yl[k] = pk2(y0.y, y1.y);
-    }
-    f32x2 ah[2][2], al[2][2];            // phase 2: [pair q][row-parity chain]
-#pragma unroll
-    for (int q = 0; q < 2; ++q) { ah[q][0] = ah[q][1] = al[q][0] = al[q][1] = 0ull; }
-    float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
-
-#pragma unroll 1
-    for (int64_t k = 0; k < rg.ntl; ++k) {
-        const int64_t s = rg.cnt;
-        const int st = (int)(s % ST);
-        const bool ok = mbar_wait(&rg.full[st], (uint32_t)((s / ST) & 1), err);
-        const int64_t t = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
-        const int64_t r0 = t * R;
-        const int rows = (int)min((int64_t)R, a.m - r0);
-        const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
-        if (ok) {
-            // lane w prefetches the old value and b of row warp + 8 w
-            float2 uo = make_float2(0.f, 0.f), bb = make_float2(0.f, 0.f);
-            if (lane < RW && warp + W * lane < rows) {
-                const int64_t i = r0 + warp + W * lane;
-                if (oldv) uo = oldv[i];
-                if (bvec) bb = bvec[i];
+        for (int k = 0; k < KP; ++k) {
+            const int p = lane + 32 * k;
+            float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
+            if (dot && p < hp) { y0 = a.yF[2 * p]; y1 = a.yF[2 * p + 1]; }
+            yh[k] = pk2(y0.x, y1.x);
+            nyh[k] = pk2(-y0.x, -y1.x);
+            yl[k] = pk2(y0.y, y1.y);
+        }
+        float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
+        // lane s < RW owns row warp + 8 s of every tile; its old value and b
+        // are loaded two tiles ahead (the loads sit behind the streaming)
+        auto row_of = [&](int64_t kk) { return ((int64_t)blockIdx.x + kk * (int64_t)gridDim.x) * R + warp + WA * lane; };
+        auto fetch = [&](int64_t kk, float2& u, float2& bv) {
+            u = make_float2(0.f, 0.f);
+            bv = make_float2(0.f, 0.f);
+            if (lane < RW && kk < ntl) {
+                const int64_t i = row_of(kk);
+                if (i < a.m) {
+                    if (oldv) u = oldv[i];
+                    if (bvec) bv = bvec[i];
+                }
             }
+        };
+        float2 qu0, qb0, qu1, qb1;
+        fetch(0, qu0, qb0);
+        fetch(1, qu1, qb1);
+#pragma unroll 1
+        for (int64_t k = 0; k < ntl; ++k) {
+            const float2 uo = qu0, bb = qb0;
+            qu0 = qu1;
+            qb0 = qb1;
+            fetch(k + 2, qu1, qb1);
+            const int st = rg.cst;
+            const bool ok = mbar_wait(&rg.full[st], rg.cph, err);
+            ring_advance(a, rg);
+            const int64_t t = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
+            const int64_t r0 = t * R;
+            const int rows = (int)min((int64_t)R, a.m - r0);
+            const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
+            const bool mine = lane < RW && warp + WA * lane < rows;
             float tvh[RW], tvl[RW];
 #pragma unroll
             for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
-            if (dot) {
+            if (dot && ok) {
                 f32x2 sh[RW][2], sl[RW][2];
 #pragma unroll
                 for (int w = 0; w < RW; ++w) { sh[w][0] = sh[w][1] = sl[w][0] = sl[w][1] = 0ull; }
@@ -171,7 +224,7 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
                     if (p < hp) {
 #pragma unroll
                         for (int w = 0; w < RW; ++w) {
-                            const ulonglong2 v = tile[(size_t)(warp + W * w) * hp + p];
+                            const ulonglong2 v = tile[(size_t)(warp + WA * w) * hp + p];
                             ff2_madd(v.x, v.y, yh[kk], nyh[kk], yl[kk], sh[w][kk & 1], sl[w][kk & 1]);
                         }
                     }
@@ -194,86 +247,112 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
                         ff_acc(tvh[w], tvl[w], oh, ol);
                     }
             }
-            // lane w forms row warp + 8 w (its own butterfly result: all lanes hold the sum)
-            if (lane < RW && warp + W * lane < rows) {
+            float2 nv = make_float2(0.f, 0.f);
+            int r = 0;
+            if (mine) {
                 float th = tvh[0], tl = tvl[0];
 #pragma unroll
                 for (int w = 1; w < RW; ++w)
                     if (lane == w) { th = tvh[w]; tl = tvl[w]; }
-                const int r = warp + W * lane;
-                const int64_t i = r0 + r;
+                r = warp + WA * lane;
                 const float2 tv = ff_norm(th, tl);
-                const float2 nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
-                dst[i] = nv;
-                usm[r] = make_ulonglong2(pk2(nv.x, nv.x), pk2(nv.y, nv.y));
+                nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
+            }
+            if (k >= 2) nb_sync(NB_UFREE + (int)(k & 1));        // column warps are done with this u buffer
+            if (mine && ok) {
+                dst[r0 + r] = nv;
+                usm[(k & 1) * R + r] = make_ulonglong2(pk2(nv.x, nv.x), pk2(nv.y, nv.y));
                 ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
                 if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
             }
+            nb_arrive(NB_URDY + (int)(k & 1));
         }
-        __syncthreads();
-        if (*err) return false;
-        if (acc_at) {
-            int r = 0;
-            for (; r + 1 < rows; r += 2) {
-                const ulonglong2 u0 = usm[r], u1 = usm[r + 1];
-                const f32x2 nu0 = neg2(u0.x), nu1 = neg2(u1.x);
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const int p = tid + q * T;
-                    if (p < hp) {
-                        const ulonglong2 v0 = tile[(size_t)r * hp + p];
-                        const ulonglong2 v1 = tile[(size_t)(r + 1) * hp + p];
-                        ff2_madd(v0.x, v0.y, u0.x, nu0, u0.y, ah[q][0], al[q][0]);
-                        ff2_madd(v1.x, v1.y, u1.x, nu1, u1.y, ah[q][1], al[q][1]);
-                    }
-                }
-            }
-            if (r < rows) {
-                const ulonglong2 u0 = usm[r];
-                const f32x2 nu0 = neg2(u0.x);
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const int p = tid + q * T;
-                    if (p < hp) {
-                        const ulonglong2 v0 = tile[(size_t)r * hp + p];
-                        ff2_madd(v0.x, v0.y, u0.x, nu0, u0.y, ah[q][0], al[q][0]);
-                    }
-                }
-            }
-        }
-        __syncthreads();
-        ++rg.cnt;
-        if (tid == 0) ring_issue(a, rg);
-    }
-    if (acc_at) {
-        float4* P4 = reinterpret_cast<float4*>(a.partF) + (size_t)blockIdx.x * hp;
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int p = tid + q * T;
-            if (p < hp) {
-                ff2_acc(ah[q][0], al[q][0], ah[q][1], al[q][1]);
-                const float2 H = upk2(ah[q][0]), L = upk2(al[q][0]);
-                const float2 c0 = ff_norm(H.x, L.x), c1v = ff_norm(H.y, L.y);
-                P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
-            }
-        }
-    }
-    {
+        for (int64_t k = (ntl >= 2 ? ntl - 2 : 0); k < ntl; ++k) nb_sync(NB_UFREE + (int)(k & 1));
         const float2 sq = ff_warp_sum(sqh, sql);
         const float2 b2 = ff_warp_sum(b2h, b2l);
         if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
+    } else {
+        // ---------------- column warps ----------------
+        const int tb = tid - 32 * WA;
+        constexpr int CH = (KP >= 16) ? 2 : 4;   // independent accumulation chains (rows mod CH)
+        constexpr int QP = (KP >= 16) ? 2 : 1;   // column pairs per thread
+        f32x2 ah[QP][CH], al[QP][CH];
+#pragma unroll
+        for (int q = 0; q < QP; ++q)
+#pragma unroll
+            for (int c = 0; c < CH; ++c) { ah[q][c] = 0ull; al[q][c] = 0ull; }
+#pragma unroll 1
+        for (int64_t k = 0; k < ntl; ++k) {
+            const int st = rg.cst;
+            const bool ok = mbar_wait(&rg.full[st], rg.cph, err);
+            ring_advance(a, rg);
+            const int64_t t = (int64_t)blockIdx.x + k * (int64_t)gridDim.x;
+            const int rows = (int)min((int64_t)R, a.m - t * R);
+            const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
+            const ulonglong2* ub = usm + (k & 1) * R;
+            nb_sync(NB_URDY + (int)(k & 1));
+            if (acc_at && ok) {
+                int r = 0;
+                for (; r + CH <= rows; r += CH) {
+#pragma unroll
+                    for (int c = 0; c < CH; ++c) {
+                        const ulonglong2 u = ub[r + c];
+                        const f32x2 nu = neg2(u.x);
+#pragma unroll
+                        for (int q = 0; q < QP; ++q) {
+                            const int p = tb + q * TB;
+                            if (p < hp) {
+                                const ulonglong2 v = tile[(size_t)(r + c) * hp + p];
+                                ff2_madd(v.x, v.y, u.x, nu, u.y, ah[q][c], al[q][c]);
+                            }
+                        }
+                    }
+                }
+                for (; r < rows; ++r) {
+                    const ulonglong2 u = ub[r];
+                    const f32x2 nu = neg2(u.x);
+#pragma unroll
+                    for (int q = 0; q < QP; ++q) {
+                        const int p = tb + q * TB;
+                        if (p < hp) {
+                            const ulonglong2 v = tile[(size_t)r * hp + p];
+                            ff2_madd(v.x, v.y, u.x, nu, u.y, ah[q][0], al[q][0]);
+                        }
+                    }
+                }
+            }
+            nb_arrive(NB_UFREE + (int)(k & 1));
+            if (tid == ISSUER) {
+                --rg.inflight;
+                ring_issue(a, rg);
+            }
+        }
+        if (acc_at) {
+            float4* P4 = reinterpret_cast<float4*>(a.partF) + (size_t)blockIdx.x * hp;
+#pragma unroll
+            for (int q = 0; q < QP; ++q) {
+                const int p = tb + q * TB;
+                if (p < hp) {
+#pragma unroll
+                    for (int c = 1; c < CH; ++c) ff2_acc(ah[q][0], al[q][0], ah[q][c], al[q][c]);
+                    const float2 H = upk2(ah[q][0]), L = upk2(al[q][0]);
+                    const float2 c0 = ff_norm(H.x, L.x), c1v = ff_norm(H.y, L.y);
+                    P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
+                }
+            }
+        }
     }
     __syncthreads();
     if (tid == 0) {
         float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
-        for (int w = 0; w < W; ++w) {
+        for (int w = 0; w < WA; ++w) {
             ff_acc(h, l, wred[w][0].x, wred[w][0].y);
             ff_acc(h2, l2, wred[w][1].x, wred[w][1].y);
         }
         a.spF[blockIdx.x * 4 + 0] = ff_norm(h, l);
         a.spF[blockIdx.x * 4 + 3] = ff_norm(h2, l2);
     }
-    return true;
+    return *err == 0;
 }
 
 // Sum over CTAs of scalar slot `slot` (warp-level, identical in every CTA).
@@ -383,35 +462,40 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 template <int KP, int RW>
 __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     extern __shared__ __align__(128) unsigned char dsm[];
-    __shared__ __align__(8) uint64_t full[ST];
+    __shared__ __align__(8) uint64_t full[MAX_ST];
     __shared__ Bcast bc;
+    __shared__ Scal sc;
     __shared__ int err_s;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t n = a.n;
     const int64_t G = gridDim.x;
     const double eps = 2.220446049250313e-16;
     const double dampsq = a.damp * a.damp;
+    const int XW = T - 32;                 // threads of warps 1..W-1 (elementwise work)
 
     Ring rg;
     rg.full = full;
     rg.tiles = reinterpret_cast<float4*>(dsm);
-    rg.cnt = 0;
-    rg.issued = 0;
     rg.ntl = (blockIdx.x < a.ntiles) ? (a.ntiles - blockIdx.x + G - 1) / G : 0;
-    ulonglong2* usm = reinterpret_cast<ulonglong2*>(dsm + (size_t)ST * a.R * a.ldf * 8);
+    rg.cst = 0;
+    rg.cph = 0;
+    rg.ist = 0;
+    rg.ik = 0;
+    rg.inflight = 0;
+    ulonglong2* usm = reinterpret_cast<ulonglong2*>(dsm + (size_t)a.ST * a.R * a.ldf * 8);
     volatile int* err = &err_s;
     if (tid == 0) {
         err_s = 0;
-        for (int s = 0; s < ST; ++s) mbar_init(&full[s], 1);
+        for (int s = 0; s < a.ST; ++s) mbar_init(&full[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        ring_issue(a, rg);
     }
     __syncthreads();
+    if (tid == ISSUER) ring_issue(a, rg);
 
 #define LSFF_SYNC()                    \
     do {                               \
         if (!grid_sync(a.bar)) {       \
-            ring_drain(rg);            \
+            ring_drain(a, rg);         \
             return;                    \
         }                              \
     } while (0)
@@ -419,7 +503,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     do {                                                           \
         if (!ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err)) {      \
             set_status(a, KSTATUS_BARRIER_TIMEOUT);                \
-            ring_drain(rg);                                        \
+            ring_drain(a, rg);                                     \
             return;                                                \
         }                                                          \
     } while (0)
@@ -442,22 +526,20 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     // u = b - A M x0 (or b); beta^2, ||b||^2, A^T u partials
     LSFF_PASS(a.x0F ? mone2 : zero2, zero2, one2, a.x0F != nullptr, nullptr, a.bF, a.uF, true, true);
     LSFF_SYNC();
-
-    // warp 0 keeps the scalar state (all lanes identical)
-    double alfa = 0, beta = 0, bnorm = 0, ibn = 0, us = 0;
     if (warp == 0) {
         const float2 S = sum_slot(a, 0, lane);
         const float2 B2 = sum_slot(a, 3, lane);
         const double Sd = ff_to_double(S), B2d = ff_to_double(B2);
         const double r = lane_rsqrt(lane == 0 ? Sd : B2d);
         const double ib = shfl_d(r, 0);
-        ibn = shfl_d(r, 1);
-        beta = Sd * ib;
-        bnorm = B2d * ibn;
-        us = ib;
+        const double ibn = shfl_d(r, 1);
         if (lane == 0) {
+            sc.beta = Sd * ib;
+            sc.bnorm = B2d * ibn;
+            sc.ibn = ibn;
+            sc.us = ib;
             bc.ib = ff_split(ib);
-            bc.beta = ff_split(beta);
+            bc.beta = ff_split(sc.beta);
         }
     } else {
         reduce_columns(a, warp, lane);
@@ -470,27 +552,34 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
         sum_colsq(a, lane, A2, W2);
         const double A2d = ff_to_double(A2);
         const double ia = lane_rsqrt(A2d);
-        alfa = A2d * ia;
-        if (lane == 0) bc.ia = ff_split(ia);
+        if (lane == 0) {
+            sc.alfa = A2d * ia;
+            bc.ia = ff_split(ia);
+        }
     } else {
         trmv_rows_raw(a, a.vunF, a.yF, warp, lane);
     }
     __syncthreads();
     if (warp > 0) {
         scale_rows(a, a.yF, bc.ia, warp, lane);
-        for (int64_t j = (int64_t)blockIdx.x * (T - 32) + (tid - 32); j < n; j += G * (T - 32)) {
+        for (int64_t j = (int64_t)blockIdx.x * XW + (tid - 32); j < n; j += G * XW) {
             const float2 vv = ff_mul(a.vunF[j], bc.ia);
             a.vF[j] = vv;
             a.wF[j] = vv;
         }
+    } else if (lane == 0) {
+        bc.istop = (sc.alfa * sc.beta == 0.0) ? -1 : 0;
+        sc.rhobar = sc.alfa; sc.phibar = sc.beta; sc.rnorm = sc.beta; sc.r1norm = sc.beta; sc.r2norm = sc.beta;
+        sc.anorm = 0; sc.acond = 0; sc.ddnorm = 0; sc.res2 = 0; sc.xnorm = 0; sc.xxnorm = 0; sc.z = 0;
+        sc.cs2 = -1.0; sc.sn2 = 0.0;
+        sc.arnorm = sc.alfa * sc.beta;
+        sc.istop = 0;
+        bc.c2 = ff_split(-sc.alfa * sc.us);
     }
-    // all lanes of warp 0 hold the scalars; publish what the exit test needs
-    if (warp == 0 && lane == 0) bc.istop = (alfa * beta == 0.0) ? -1 : 0;
     LSFF_SYNC();
     if (bc.istop == -1) {
         if (gt == 0) {
-            const double bb = (double)bc.beta.x + (double)bc.beta.y;
-            a.out[0] = 0; a.out[1] = 0; a.out[2] = bb; a.out[3] = bb;
+            a.out[0] = 0; a.out[1] = 0; a.out[2] = sc.beta; a.out[3] = sc.beta;
             a.out[4] = 0; a.out[5] = 0; a.out[6] = 0; a.out[7] = 0;
             if (a.arn) a.arn[0] = 0.0;
         }
@@ -498,24 +587,14 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             a.x[j] = ff_to_double(a.xF[j]);
             if (a.calc_var && a.var) a.var[j] = 0.0;
         }
-        ring_drain(rg);
+        ring_drain(a, rg);
         return;
     }
-
-    double rhobar = alfa, phibar = beta, rnorm = beta, r1norm = beta, r2norm = beta;
-    double anorm = 0.0, acond = 0.0, ddnorm = 0.0, res2 = 0.0, xnorm = 0.0, xxnorm = 0.0, z = 0.0;
-    double cs2 = -1.0, sn2 = 0.0;
-    double arnorm = alfa * beta;
-    double rho = 0, irho = 0, c = 0, s = 0, phi = 0, tau = 0, psi = 0;
-    int beta_pos = 1;
     const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
     int64_t itn = 0;
-    int istop = 0;
-    if (warp == 0 && lane == 0) bc.c2 = ff_split(-alfa * us);
-    __syncthreads();
 
     while (itn < a.iter_lim) {
-        if (gt == 0 && a.arn) a.arn[itn] = arnorm;
+        if (gt == 0 && a.arn) a.arn[itn] = sc.arnorm;
         ++itn;
         // u = A M v - alfa u (u stored unnormalised); A^T u partials (solvers.rs:194-195)
         {
@@ -527,20 +606,17 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             // beta, the first plane rotation and phi, tau, t1 need only beta (solvers.rs:196-216)
             const float2 S = sum_slot(a, 0, lane);
             const double Sd = ff_to_double(S);
-            beta_pos = Sd > 0.0;
+            const int beta_pos = Sd > 0.0;
+            const double rhobar = sc.rhobar, alfa = sc.alfa, anorm0 = sc.anorm;
             const double rb2 = rhobar * rhobar + dampsq;
-            const double an2 = anorm * anorm + alfa * alfa + Sd + dampsq;
+            const double an2 = anorm0 * anorm0 + alfa * alfa + Sd + dampsq;
             const double arg = lane == 0 ? Sd : lane == 1 ? rb2 + Sd : lane == 2 ? rb2 : an2;
             const double r = lane_rsqrt(arg);
             const double ib = shfl_d(r, 0);
-            irho = shfl_d(r, 1);
+            const double irho = shfl_d(r, 1);
             const double irb1 = shfl_d(r, 2);
             const double ian = shfl_d(r, 3);
-            beta = Sd * ib;
-            if (beta_pos) {
-                us = ib;
-                anorm = an2 * ian;
-            }
+            const double beta = Sd * ib;
             double rhobar1, cs1, sn1;
             if (dampsq == 0.0) {
                 rhobar1 = fabs(rhobar);
@@ -551,15 +627,22 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
                 cs1 = rhobar * irb1;
                 sn1 = a.damp * irb1;
             }
-            psi = sn1 * phibar;
-            phibar *= cs1;
-            rho = (rb2 + Sd) * irho;
-            c = rhobar1 * irho;
-            s = beta * irho;
-            phi = c * phibar;
+            const double psi = sn1 * sc.phibar;
+            double phibar = sc.phibar * cs1;
+            const double rho = (rb2 + Sd) * irho;
+            const double c = rhobar1 * irho;
+            const double s = beta * irho;
+            const double phi = c * phibar;
             phibar = s * phibar;
-            tau = s * phi;
+            const double tau = s * phi;
             if (lane == 0) {
+                sc.beta = beta;
+                if (beta_pos) {
+                    sc.us = ib;
+                    sc.anorm = an2 * ian;
+                }
+                sc.psi = psi; sc.phibar = phibar; sc.rho = rho; sc.irho = irho; sc.c = c; sc.s = s;
+                sc.phi = phi; sc.tau = tau;
                 bc.ib = ff_split(ib);
                 bc.beta = ff_split(beta);
                 bc.beta_pos = beta_pos;
@@ -589,17 +672,19 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             float2 A2, W2;
             sum_colsq(a, lane, A2, W2);
             wsq = ff_to_double(W2);
+            double alfa = sc.alfa;
             if (bp) {
                 const double A2d = ff_to_double(A2);
                 const double ia = lane_rsqrt(A2d);
                 alfa = A2d * ia;
                 if (lane == 0) bc.ia = ff_split(ia);
             }
-            const double theta = s * alfa;
-            rhobar = -c * alfa;
+            const double theta = sc.s * alfa;
             if (lane == 0) {
-                bc.t2 = ff_split(-theta * irho);
-                bc.c2 = ff_split(-alfa * us);
+                sc.alfa = alfa;
+                sc.rhobar = -sc.c * alfa;
+                bc.t2 = ff_split(-theta * sc.irho);
+                bc.c2 = ff_split(-alfa * sc.us);
             }
         } else if (bp) {
             trmv_rows_raw(a, a.vunF, a.yF, warp, lane);
@@ -609,7 +694,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             // x += t1 w ; w = v + t2 w ; var += (w / rho)^2 ; y = M v  (solvers.rs:222-232)
             if (bp) scale_rows(a, a.yF, bc.ia, warp, lane);
             const float2 t1 = bc.t1, t2 = bc.t2, ia = bc.ia, ir = bc.irho;
-            for (int64_t j = (int64_t)blockIdx.x * (T - 32) + (tid - 32); j < n; j += G * (T - 32)) {
+            for (int64_t j = (int64_t)blockIdx.x * XW + (tid - 32); j < n; j += G * XW) {
                 const float2 vv = bp ? ff_mul(a.vunF[j], ia) : a.vF[j];
                 const float2 wj = a.wF[j];
                 a.vF[j] = vv;
@@ -622,12 +707,14 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             }
         } else {
             // norm estimates and stopping tests (solvers.rs:235-272)
-            const double theta = s * alfa;
-            ddnorm += wsq * irho * irho;
-            const double delta = sn2 * rho;
-            const double gambar = -cs2 * rho;
-            const double rhs = phi - delta * z;
-            res2 += psi * psi;
+            const double alfa = sc.alfa, rho = sc.rho, irho = sc.irho, phi = sc.phi, psi = sc.psi;
+            const double phibar = sc.phibar, anorm = sc.anorm, bnorm_inv = sc.ibn;
+            const double theta = sc.s * alfa;
+            const double ddnorm = sc.ddnorm + wsq * irho * irho;
+            const double delta = sc.sn2 * rho;
+            const double gambar = -sc.cs2 * rho;
+            const double rhs = phi - delta * sc.z;
+            const double res2 = sc.res2 + psi * psi;
             const double rn2 = phibar * phibar + res2;
             const double g2 = gambar * gambar + theta * theta;
             const double arg1 = lane == 0 ? g2 : lane == 1 ? gambar * gambar : lane == 2 ? ddnorm : rn2;
@@ -637,22 +724,21 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             const double idd = shfl_d(r1, 2);
             const double irn = shfl_d(r1, 3);
             const double zbar = rhs * igb * sgn(gambar);
-            cs2 = gambar * igamma;
-            sn2 = theta * igamma;
-            z = rhs * igamma;
-            const double xn2 = xxnorm + zbar * zbar;
-            xxnorm += z * z;
-            acond = anorm * (ddnorm * idd);
-            rnorm = rn2 * irn;
-            arnorm = alfa * fabs(tau);
+            const double cs2 = gambar * igamma;
+            const double sn2 = theta * igamma;
+            const double z = rhs * igamma;
+            const double xn2 = sc.xxnorm + zbar * zbar;
+            const double xxnorm = sc.xxnorm + z * z;
+            const double acond = anorm * (ddnorm * idd);
+            const double rnorm = rn2 * irn;
+            const double arnorm = alfa * fabs(sc.tau);
             const double r1sq = rnorm * rnorm - dampsq * xxnorm;
             const double arg2 = lane == 0 ? xn2 : fabs(r1sq);
             const double r2 = lane_rsqrt(arg2);
-            xnorm = xn2 * shfl_d(r2, 0);
-            r1norm = fabs(r1sq) * shfl_d(r2, 1);
-            r2norm = rnorm;
-            const double test1 = rnorm * ibn;
-            const double axb = anorm * xnorm * ibn;
+            const double xnorm = xn2 * shfl_d(r2, 0);
+            const double r1norm = fabs(r1sq) * shfl_d(r2, 1);
+            const double test1 = rnorm * bnorm_inv;
+            const double axb = anorm * xnorm * bnorm_inv;
             const double arg3 = lane == 0 ? anorm * rnorm + eps : lane == 1 ? acond + eps : 1.0 + axb;
             const double r3 = lane_rsqrt(arg3);
             const double q0 = shfl_d(r3, 0), q1 = shfl_d(r3, 1), q2 = shfl_d(r3, 2);
@@ -660,7 +746,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             const double test3 = q1 * q1;
             const double tt1 = test1 * (q2 * q2);
             const double rtol = a.atol + a.btol * axb;
-            istop = 0;
+            int istop = 0;
             if (itn >= a.iter_lim) istop = 7;
             if (1.0 + test3 <= 1.0) istop = 6;
             if (1.0 + test2 <= 1.0) istop = 5;
@@ -669,7 +755,12 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             if (test2 <= a.atol) istop = 2;
             if (test1 <= rtol) istop = 1;
             if (a.abs_tol > 0.0 && arnorm < a.abs_tol && (istop == 0 || istop == 7)) istop = 2;
-            if (lane == 0) bc.istop = istop;
+            if (lane == 0) {
+                sc.ddnorm = ddnorm; sc.res2 = res2; sc.cs2 = cs2; sc.sn2 = sn2; sc.z = z; sc.xxnorm = xxnorm;
+                sc.acond = acond; sc.rnorm = rnorm; sc.arnorm = arnorm; sc.xnorm = xnorm; sc.r1norm = r1norm;
+                sc.r2norm = rnorm; sc.istop = istop;
+                bc.istop = istop;
+            }
         }
         LSFF_SYNC();
         if (bc.istop != 0) break;
@@ -679,10 +770,10 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
         if (a.calc_var && a.var) a.var[j] = ff_to_double(a.varF[j]);
     }
     if (gt == 0) {
-        a.out[0] = istop; a.out[1] = (double)itn; a.out[2] = r1norm; a.out[3] = r2norm;
-        a.out[4] = anorm; a.out[5] = acond; a.out[6] = xnorm; a.out[7] = arnorm;
+        a.out[0] = sc.istop; a.out[1] = (double)itn; a.out[2] = sc.r1norm; a.out[3] = sc.r2norm;
+        a.out[4] = sc.anorm; a.out[5] = sc.acond; a.out[6] = sc.xnorm; a.out[7] = sc.arnorm;
     }
-    ring_drain(rg);
+    ring_drain(a, rg);
 #undef LSFF_SYNC
 #undef LSFF_PASS
 }
@@ -732,12 +823,12 @@ __global__ void msplit_kernel(const double* __restrict__ M, int64_t n, int64_t l
 template <int KP, int RW>
 static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW>; }
 
-// (kernel, rows per warp) for hp column pairs: the y registers cover hp, and
-// a tile of 8 RW rows stays within 64 KB.
+// (kernel, rows per row-warp) for hp column pairs: the y registers cover hp,
+// and a tile (8 RW rows) is at most 64 KB, so the ring holds 3 or more tiles.
 static const void* pick_kernel(int64_t hp, int& RW) {
     if (hp <= 32) { RW = 4; return kernel_kp<1, 4>(); }
     if (hp <= 64) { RW = 4; return kernel_kp<2, 4>(); }
-    if (hp <= 128) { RW = 2; return kernel_kp<4, 2>(); }
+    if (hp <= 128) { RW = 4; return kernel_kp<4, 4>(); }
     if (hp <= 256) { RW = 2; return kernel_kp<8, 2>(); }
     RW = 1;
     return kernel_kp<16, 1>();
@@ -757,15 +848,17 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     const int64_t hp = ldf / 2;
     int RW = 1;
     const void* k = pick_kernel(hp, RW);
-    const int R = W * RW;
-    const size_t smem = (size_t)ST * R * ldf * 8 + (size_t)R * 16;
-    if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int R = WA * RW;
+    const size_t stage = (size_t)R * ldf * 8;
+    int STn = (int)(RING_BYTES / stage);
+    STn = STn > MAX_ST ? MAX_ST : STn;
+    if (STn < 3) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): tile ring does not fit");
+    const size_t smem = (size_t)STn * stage + (size_t)2 * R * 16;
+    RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, T, smem));
     if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): kernel does not fit on an SM");
-    if (nb > 2) nb = 2;
-    const int G = nb * ctx.sm_count;
+    const int G = ctx.sm_count;
 
     DevBuf<float2> AF, MF, MtF, bF, x0F, uF, yF, gF, vF, wF, xF, vunF, varF, partF, spF;
     DevBuf<float4> colsq;
@@ -811,7 +904,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
         RNLA_LAUNCH_CHECK();
         a.x0F = x0F.get();
     }
-    a.AF = AF.get(); a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.R = R; a.ntiles = div_up(m, R);
+    a.AF = AF.get(); a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.R = R; a.ST = STn; a.ntiles = div_up(m, R);
     a.bF = bF.get();
     a.uF = uF.get(); a.yF = yF.get(); a.gF = gF.get(); a.vF = vF.get(); a.wF = wF.get(); a.xF = xF.get();
     a.vunF = vunF.get(); a.varF = varF.get(); a.partF = partF.get(); a.spF = spF.get(); a.colsq = colsq.get();

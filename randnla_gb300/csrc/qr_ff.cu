@@ -3,127 +3,170 @@
 // sketch S A, R^-1).  Arithmetic is float-float on the FP32 pipe: on GB300 a
 // dependent FP64 operation takes ~64 cycles and a divide or square root
 // several hundred, and a QR of a d x n sketch is a chain of n dependent
-// column steps, so the FP64 chain length sets its time.
+// column steps, so the length of that chain sets its time.
 //
 // QR.  Columns are grouped in blocks of KB = 4; block b is owned by CTA
-// b mod G, which keeps its columns in shared memory.  Reflector block rb is
-// published to global memory (float-float v, tau) and announced by a flag.
-// On seeing flag rb, a CTA loads the block's reflectors into shared memory;
-// if it owns block rb + 1 it applies them there first, factors that block
-// (look-ahead) and publishes it, then applies them to its other blocks.  One
-// cross-CTA hand-off per KB columns sits on the critical path.
-// Reflectors follow LAPACK dlarfg: beta = -sign(alpha) ||(alpha, x)||,
-// v = x / (alpha - beta), tau = (beta - alpha) / beta, and tau = 0 when x is
-// exactly zero.  Flag waits are bounded (2 s) and end the kernel with a
-// status code.
+// b mod G, which keeps its columns in shared memory (512 threads, rows
+// strided over the threads).  The owner of a block factors it column by
+// column (LAPACK dlarfg reflectors: beta = -sign(alpha) ||(alpha, x)||,
+// v = x / (alpha - beta), tau = (beta - alpha) / beta, tau = 0 when x is
+// exactly zero), forms the block's triangular factor T (dlarft, forward,
+// columnwise) so that H_0 H_1 H_2 H_3 = I - V T V^T, publishes V, T and a
+// flag.  On seeing flag rb a CTA bulk-copies V and T of block rb into shared
+// memory and applies Q_rb^T = I - V T^T V^T to its later blocks -- the owner
+// of block rb + 1 first, which then factors that block (look-ahead).  One
+// cross-CTA hand-off and one batched reduction per block of 4 columns sit on
+// the critical path.  Flag and copy waits are bounded (2 s) and end the
+// kernel with a status code.
+//
+// Reductions are float-float: a reduce-scatter butterfly inside each warp
+// (NV values: each exchange level halves the values a lane keeps), then the
+// per-warp partials are summed by NV groups of 16 lanes.
 //
 // R^-1.  One CTA per column j: column-oriented back substitution
-// x_k = t_k / r_kk, t_{<k} -= r_{<k,k} x_k with t = e_j in shared memory and
-// the reciprocal pivots precomputed.
+// x_k = t_k / r_kk, t_{<k} -= r_{<k,k} x_k with t = e_j in shared memory,
+// the reciprocal pivots precomputed and the next column of R prefetched.
 #include "rnla_internal.h"
 #include "rnla_ff.cuh"
+#include "rnla_async.cuh"
 
 namespace rnla {
 namespace qrff {
 
-constexpr int T = 256;
+constexpr int T = 512;
 constexpr int W = T / 32;
 constexpr int KB = 4;
 constexpr int MAX_OWNB = 4;
-constexpr int MAXC = MAX_OWNB * KB;
 
 struct Args {
     double* X;              // m x nc, column-major, ld
     int64_t m, n, nc, ld;
-    float2* VF;             // m x n reflectors (column t: rows t+1..m-1)
-    float2* tauF;           // n
+    int64_t ldv;            // m rounded up to even: leading dimension of VF
+    float2* VF;             // ldv x n reflectors (column t: rows t+1..m-1)
+    float2* TF;             // per reflector block: 4 x 4 T (column-major) then 4 tau
     unsigned int* flags;    // one per reflector block
     unsigned int* status;
 };
 
-__device__ bool wait_flag(const unsigned int* f, unsigned int* status) {
-    __shared__ int ok_s;
-    if (threadIdx.x == 0) {
-        ok_s = 1;
-        const volatile unsigned int* vf = f;
-        if (*vf == 0u) {
-            const unsigned long long t0 = globaltimer_ns();
-            unsigned int spins = 0;
-            while (*vf == 0u) {
-                if (*((volatile unsigned int*)status) != 0u) { ok_s = 0; break; }
-                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > 2000000000ull) {
-                    atomicCAS(status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
-                    ok_s = 0;
-                    break;
-                }
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok_s != 0;
+__device__ __forceinline__ void fail_status(unsigned int* status) {
+    atomicCAS(status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
 }
 
-// Block sums of cnt unnormalised float-float accumulators; every thread
-// receives every total (fixed order: warps 0..W-1).
-template <int N>
-__device__ __forceinline__ void block_sums(float (&h)[N], float (&l)[N], int cnt, float2* red, float2* tot) {
+// Block-wide float-float sums of NV unnormalised accumulators (h, l); the
+// normalised totals land in tot[0..NV).  red: W * NV float2 of scratch.
+template <int NV>
+__device__ __forceinline__ void block_sums(float (&h)[NV], float (&l)[NV], float2* red, float2* tot) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int off = 16;
 #pragma unroll
-    for (int c = 0; c < N; ++c)
-        if (c < cnt) {
-            const float2 s = ff_warp_sum(h[c], l[c]);
-            if (lane == 0) red[warp * N + c] = s;
+    for (int half = NV / 2; half >= 1; half /= 2) {
+        const bool up = (lane & off) != 0;
+#pragma unroll
+        for (int k = 0; k < half; ++k) {
+            const float sh = up ? h[k] : h[k + half], sl = up ? l[k] : l[k + half];
+            float kh = up ? h[k + half] : h[k], kl = up ? l[k + half] : l[k];
+            const float rh = __shfl_xor_sync(0xffffffffu, sh, off);
+            const float rl = __shfl_xor_sync(0xffffffffu, sl, off);
+            ff_acc(kh, kl, rh, rl);
+            h[k] = kh;
+            l[k] = kl;
         }
+        off >>= 1;
+    }
+    float vh = h[0], vl = l[0];
+    for (; off >= 1; off >>= 1) {
+        const float rh = __shfl_xor_sync(0xffffffffu, vh, off);
+        const float rl = __shfl_xor_sync(0xffffffffu, vl, off);
+        ff_acc(vh, vl, rh, rl);
+    }
+    constexpr int SH = (NV == 1) ? 5 : (NV == 2) ? 4 : (NV == 4) ? 3 : (NV == 8) ? 2 : (NV == 16) ? 1 : 0;
+    if ((lane & ((1 << SH) - 1)) == 0) red[warp * NV + (lane >> SH)] = make_float2(vh, vl);
     __syncthreads();
-    if ((int)threadIdx.x < cnt) {
-        float th = 0.f, tl = 0.f;
-        for (int w = 0; w < W; ++w) ff_acc(th, tl, red[w * N + threadIdx.x].x, red[w * N + threadIdx.x].y);
-        tot[threadIdx.x] = ff_norm(th, tl);
+    // NV groups of 16 lanes: group v sums the W = 16 warp partials of value v
+    // (whole warps take part; lanes past NV * 16 carry zeros)
+    constexpr int PART = (NV * 16 + 31) & ~31;
+    if ((int)threadIdx.x < PART) {
+        const int v = threadIdx.x >> 4, w = threadIdx.x & 15;
+        float sh = 0.f, sl = 0.f;
+        if (v < NV) { sh = red[w * NV + v].x; sl = red[w * NV + v].y; }
+#pragma unroll
+        for (int o = 8; o >= 1; o >>= 1) {
+            const float rh = __shfl_xor_sync(0xffffffffu, sh, o);
+            const float rl = __shfl_xor_sync(0xffffffffu, sl, o);
+            ff_acc(sh, sl, rh, rl);
+        }
+        if (w == 0 && v < NV) tot[v] = ff_norm(sh, sl);
     }
     __syncthreads();
 }
 
-// Applies reflector t (v: row t implicit 1, rows > t in v[]) with tau to the
-// columns cols + slot[c] * m, c < cnt.
-__device__ void apply_reflector(const Args& a, const float2* v, float2 tau, int64_t t, float2* cols,
-                                const int* slot, int cnt, float2* red, float2* tot) {
-    const int64_t m = a.m;
-    float h[MAXC], l[MAXC];
+// v_r[i] of a reflector stored in a column with its head at row t: 0 above
+// t, 1 at t, the stored value below.
+__device__ __forceinline__ float2 vval(const float2* col, int64_t i, int64_t t) {
+    return (i > t) ? col[i] : make_float2(i == t ? 1.f : 0.f, 0.f);
+}
+
+// Applies Q_b^T = I - V T^T V^T of reflector block b (V: the KB columns at
+// vb with stride vs, heads at rows b*KB + r; Tm: 4 x 4 column-major) to the
+// KB columns at c (stride m).  nr = reflectors in the block.
+__device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int64_t b, int nr, float2* c,
+                            int64_t m, float2* red, float2* tot, float2* wsm) {
+    const int64_t t0 = b * KB;
+    float h[KB * KB], l[KB * KB];        // [column q][reflector r]
 #pragma unroll
-    for (int c = 0; c < MAXC; ++c) { h[c] = 0.f; l[c] = 0.f; }
-    for (int64_t i = t + threadIdx.x; i < m; i += T) {
-        const float2 vi = (i == t) ? make_float2(1.f, 0.f) : v[i];
+    for (int k = 0; k < KB * KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
+    for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
+        float2 v[KB], x[KB];
 #pragma unroll
-        for (int c = 0; c < MAXC; ++c)
-            if (c < cnt) {
-                const float2 x = cols[(size_t)slot[c] * m + i];
-                ff_madd(vi.x, vi.y, x.x, x.y, h[c], l[c]);
-            }
+        for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < KB; ++q) x[q] = c[(size_t)q * m + i];
+#pragma unroll
+        for (int q = 0; q < KB; ++q)
+#pragma unroll
+            for (int r = 0; r < KB; ++r) ff_madd(v[r].x, v[r].y, x[q].x, x[q].y, h[q * KB + r], l[q * KB + r]);
     }
-    block_sums<MAXC>(h, l, cnt, red, tot);
-    for (int64_t i = t + threadIdx.x; i < m; i += T) {
-        const float2 vi = (i == t) ? make_float2(1.f, 0.f) : v[i];
-        for (int c = 0; c < cnt; ++c) {
-            const float2 f = ff_mul(tau, tot[c]);
-            float2* x = cols + (size_t)slot[c] * m + i;
-            *x = ff_add(*x, ff_neg(ff_mul(f, vi)));
+    block_sums<KB * KB>(h, l, red, tot);
+    // w'[q][s] = sum_r T[r][s] w[q][r]  (T^T w), one thread per (q, s)
+    if ((int)threadIdx.x < KB * KB) {
+        const int q = threadIdx.x / KB, s = threadIdx.x % KB;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int r = 0; r <= s; ++r) acc = ff_add(acc, ff_mul(Tm[r + s * KB], tot[q * KB + r]));
+        wsm[q * KB + s] = acc;
+    }
+    __syncthreads();
+    float2 wv[KB * KB];
+#pragma unroll
+    for (int k = 0; k < KB * KB; ++k) wv[k] = ff_neg(wsm[k]);
+    for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
+        float2 v[KB];
+#pragma unroll
+        for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < KB; ++q) {
+            float2 x = c[(size_t)q * m + i];
+#pragma unroll
+            for (int r = 0; r < KB; ++r) x = ff_fma(v[r], wv[q * KB + r], x);
+            c[(size_t)q * m + i] = x;
         }
     }
     __syncthreads();
 }
 
-// Factors the KB columns in local slots q*KB.. (block b), publishes them.
-__device__ void factor_block(const Args& a, float2* cols, int q, int64_t b, float2* red, float2* tot,
-                             float2* taus_local) {
+// Factors the block b held at c (KB columns, stride m; columns >= nc are
+// absent), forms T and publishes V, T and the flag.
+__device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, float2* tot, float2* tsm) {
     const int64_t m = a.m, n = a.n, nc = a.nc;
-    for (int r = 0; r < KB; ++r) {
-        const int64_t t = b * KB + r;
-        if (t >= n) break;
-        float2* col = cols + (size_t)(q * KB + r) * m;
+    const int64_t t0 = b * KB;
+    const int nr = (int)min((int64_t)KB, n - t0);
+    const int ncol = (int)min((int64_t)KB, nc - t0);
+    float2* taus = tsm + KB * KB;
+    for (int r = 0; r < nr; ++r) {
+        const int64_t t = t0 + r;
+        float2* col = c + (size_t)r * m;
         float h[1] = {0.f}, l[1] = {0.f};
         for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) ff_madd(col[i].x, col[i].y, col[i].x, col[i].y, h[0], l[0]);
-        block_sums<1>(h, l, 1, red, tot);
+        block_sums<1>(h, l, red, tot);
         const float2 xn2 = tot[0];
         const float2 alpha = col[t];
         float2 tau = make_float2(0.f, 0.f), beta = alpha;
@@ -137,48 +180,78 @@ __device__ void factor_block(const Args& a, float2* cols, int q, int64_t b, floa
         __syncthreads();
         if (threadIdx.x == 0) {
             col[t] = beta;
-            taus_local[r] = tau;
+            taus[r] = tau;
         }
         __syncthreads();
-        // apply to the rest of the block (v = (1, col[t+1..]))
-        int slot[MAXC];
-        int cnt = 0;
-        for (int rr = r + 1; rr < KB && cnt < MAXC; ++rr)
-            if (b * KB + rr < nc) slot[cnt++] = q * KB + rr;
-        if (cnt > 0 && tau.x != 0.f) {
-            // the reflector's v: row t implicit 1 (col[t] now holds beta)
-            float hh[MAXC], ll[MAXC];
+        // H_t on the block's later columns
+        if (r + 1 < ncol && tau.x != 0.f) {
+            float hh[KB], ll[KB];
 #pragma unroll
-            for (int c = 0; c < MAXC; ++c) { hh[c] = 0.f; ll[c] = 0.f; }
+            for (int q = 0; q < KB; ++q) { hh[q] = 0.f; ll[q] = 0.f; }
             for (int64_t i = t + threadIdx.x; i < m; i += T) {
                 const float2 vi = (i == t) ? make_float2(1.f, 0.f) : col[i];
 #pragma unroll
-                for (int c = 0; c < MAXC; ++c)
-                    if (c < cnt) {
-                        const float2 x = cols[(size_t)slot[c] * m + i];
-                        ff_madd(vi.x, vi.y, x.x, x.y, hh[c], ll[c]);
+                for (int q = 0; q < KB; ++q)
+                    if (q > r && q < ncol) {
+                        const float2 x = c[(size_t)q * m + i];
+                        ff_madd(vi.x, vi.y, x.x, x.y, hh[q], ll[q]);
                     }
             }
-            block_sums<MAXC>(hh, ll, cnt, red, tot);
+            block_sums<KB>(hh, ll, red, tot);
+            float2 f[KB];
+#pragma unroll
+            for (int q = 0; q < KB; ++q) f[q] = ff_neg(ff_mul(tau, tot[q]));
             for (int64_t i = t + threadIdx.x; i < m; i += T) {
                 const float2 vi = (i == t) ? make_float2(1.f, 0.f) : col[i];
-                for (int c = 0; c < cnt; ++c) {
-                    const float2 f = ff_mul(tau, tot[c]);
-                    float2* x = cols + (size_t)slot[c] * m + i;
-                    *x = ff_add(*x, ff_neg(ff_mul(f, vi)));
-                }
+#pragma unroll
+                for (int q = 0; q < KB; ++q)
+                    if (q > r && q < ncol) c[(size_t)q * m + i] = ff_fma(f[q], vi, c[(size_t)q * m + i]);
             }
             __syncthreads();
         }
     }
-    // publish: reflectors and tau to global memory, then the flag
-    for (int r = 0; r < KB; ++r) {
-        const int64_t t = b * KB + r;
-        if (t >= n) break;
-        const float2* col = cols + (size_t)(q * KB + r) * m;
-        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) a.VF[i + t * m] = col[i];
-        if (threadIdx.x == 0) a.tauF[t] = taus_local[r];
+    // T (dlarft, forward, columnwise): T[s][s] = tau_s,
+    // T[0:s, s] = -tau_s T[0:s, 0:s] V[:, 0:s]^T v_s, with g_rs = v_r^T v_s.
+    {
+        float h[8], l[8];                  // pairs (r, s), r < s: (0,1) (0,2) (1,2) (0,3) (1,3) (2,3)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) { h[k] = 0.f; l[k] = 0.f; }
+        for (int64_t i = t0 + 1 + threadIdx.x; i < m; i += T) {
+            float2 v[KB];
+#pragma unroll
+            for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(c + (size_t)r * m, i, t0 + r) : make_float2(0.f, 0.f);
+            ff_madd(v[0].x, v[0].y, v[1].x, v[1].y, h[0], l[0]);
+            ff_madd(v[0].x, v[0].y, v[2].x, v[2].y, h[1], l[1]);
+            ff_madd(v[1].x, v[1].y, v[2].x, v[2].y, h[2], l[2]);
+            ff_madd(v[0].x, v[0].y, v[3].x, v[3].y, h[3], l[3]);
+            ff_madd(v[1].x, v[1].y, v[3].x, v[3].y, h[4], l[4]);
+            ff_madd(v[2].x, v[2].y, v[3].x, v[3].y, h[5], l[5]);
+        }
+        block_sums<8>(h, l, red, tot);
+        if (threadIdx.x == 0) {
+            float2 Tm[KB * KB];
+#pragma unroll
+            for (int k = 0; k < KB * KB; ++k) Tm[k] = make_float2(0.f, 0.f);
+            const int gi[KB][KB] = {{-1, 0, 1, 3}, {-1, -1, 2, 4}, {-1, -1, -1, 5}, {-1, -1, -1, -1}};
+            for (int s = 0; s < nr; ++s) {
+                Tm[s + s * KB] = taus[s];
+                for (int r = 0; r < s; ++r) {
+                    float2 acc = make_float2(0.f, 0.f);
+                    for (int k = r; k < s; ++k) acc = ff_add(acc, ff_mul(Tm[r + k * KB], tot[gi[k][s]]));
+                    Tm[r + s * KB] = ff_neg(ff_mul(taus[s], acc));
+                }
+            }
+            for (int k = 0; k < KB * KB; ++k) tsm[k] = Tm[k];
+        }
+        __syncthreads();
     }
+    // publish
+    for (int r = 0; r < nr; ++r) {
+        const int64_t t = t0 + r;
+        const float2* col = c + (size_t)r * m;
+        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) a.VF[i + t * a.ldv] = col[i];
+    }
+    if ((int)threadIdx.x < KB * KB + KB) a.TF[b * (KB * KB + KB) + threadIdx.x] = tsm[threadIdx.x];
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -187,15 +260,18 @@ __device__ void factor_block(const Args& a, float2* cols, int q, int64_t b, floa
 }
 
 template <int OWNB>
-__global__ void __launch_bounds__(T) qr_ff_kernel(Args a) {
+__global__ void __launch_bounds__(T, 1) qr_ff_kernel(Args a) {
     extern __shared__ __align__(16) float2 sm[];
-    __shared__ float2 red[W * MAXC];
-    __shared__ float2 tot[MAXC];
-    __shared__ float2 taus[KB];
-    __shared__ float2 taus_local[KB];
+    __shared__ float2 red[W * 16];
+    __shared__ float2 tot[16];
+    __shared__ float2 wsm[KB * KB];
+    __shared__ __align__(16) float2 tsm[KB * KB + KB];      // own T and taus while factoring
+    __shared__ __align__(16) float2 tin[KB * KB + KB];      // received T and taus
+    __shared__ __align__(8) uint64_t vbar;
+    __shared__ int ok_s;
     const int64_t m = a.m, n = a.n, nc = a.nc, G = gridDim.x;
-    float2* cols = sm;                                  // OWNB*KB columns of m
-    float2* vb = sm + (size_t)OWNB * KB * m;            // the current reflector block, KB x m
+    float2* cols = sm;                                  // OWNB * KB columns of m
+    float2* vb = sm + (size_t)OWNB * KB * m;            // received reflector block, KB x ldv
     const int64_t nblk = (nc + KB - 1) / KB, nref = (n + KB - 1) / KB;
     int64_t blk[OWNB];
     int64_t last = -1;
@@ -208,58 +284,63 @@ __global__ void __launch_bounds__(T) qr_ff_kernel(Args a) {
     for (int q = 0; q < OWNB; ++q)
         for (int r = 0; r < KB; ++r) {
             const int64_t j = blk[q] * KB + r;
-            if (blk[q] < nblk && j < nc)
+            if (blk[q] < nblk)
                 for (int64_t i = threadIdx.x; i < m; i += T)
-                    cols[(size_t)(q * KB + r) * m + i] = ff_split(a.X[i + j * a.ld]);
+                    cols[(size_t)(q * KB + r) * m + i] = (j < nc) ? ff_split(a.X[i + j * a.ld]) : make_float2(0.f, 0.f);
         }
+    if (threadIdx.x == 0) {
+        mbar_init(&vbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
-    if (blk[0] == 0 && nref > 0) factor_block(a, cols, 0, 0, red, tot, taus_local);
+    volatile int quiet = 0;
+    if (blk[0] == 0 && nref > 0) factor_block(a, cols, 0, red, tot, tsm);
     for (int64_t rb = 0; rb < nref && rb < last; ++rb) {
-        if (!wait_flag(&a.flags[rb], a.status)) return;
-        for (int r = 0; r < KB; ++r) {
-            const int64_t t = rb * KB + r;
-            if (t >= n) break;
-            for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) vb[(size_t)r * m + i] = __ldcg(a.VF + i + t * m);
-            if (threadIdx.x == 0) {
-                const float2 tv = __ldcg(a.tauF + t);
-                taus[r] = tv;
+        const int nr = (int)min((int64_t)KB, n - rb * KB);
+        // flag, then one bulk copy per reflector column (rows from the block head) and T
+        if (threadIdx.x == 0) {
+            ok_s = 1;
+            const volatile unsigned int* vf = a.flags + rb;
+            if (*vf == 0u) {
+                const unsigned long long t0 = globaltimer_ns();
+                unsigned int spins = 0;
+                while (*vf == 0u) {
+                    if (*((volatile unsigned int*)a.status) != 0u) { ok_s = 0; break; }
+                    if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > MBAR_WAIT_NS) {
+                        fail_status(a.status);
+                        ok_s = 0;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+            if (ok_s) {
+                const int64_t r0 = (rb * KB) & ~1LL;                 // even row: 16-byte aligned
+                const uint32_t bytes = (uint32_t)((a.ldv - r0) * sizeof(float2));
+                mbar_expect_tx(&vbar, (uint32_t)nr * bytes + (uint32_t)sizeof(tin));
+                for (int r = 0; r < nr; ++r)
+                    bulk_g2s(vb + (size_t)r * a.ldv + r0, a.VF + (rb * KB + r) * a.ldv + r0, bytes, &vbar);
+                bulk_g2s(tin, a.TF + rb * (KB * KB + KB), (uint32_t)sizeof(tin), &vbar);
+                if (!mbar_wait(&vbar, (uint32_t)(rb & 1), &quiet)) {
+                    fail_status(a.status);
+                    ok_s = 0;
+                }
             }
         }
         __syncthreads();
+        if (!ok_s) return;
         int la = -1;
 #pragma unroll
         for (int q = 0; q < OWNB; ++q)
             if (blk[q] == rb + 1) la = q;
-        // look-ahead: block rb + 1 first, factor and publish it
         if (la >= 0) {
-            int slot[MAXC];
-            int cnt = 0;
-            for (int r = 0; r < KB; ++r)
-                if ((rb + 1) * KB + r < nc) slot[cnt++] = la * KB + r;
-            for (int r = 0; r < KB; ++r) {
-                const int64_t t = rb * KB + r;
-                if (t >= n) break;
-                if (taus[r].x != 0.f) apply_reflector(a, vb + (size_t)r * m, taus[r], t, cols, slot, cnt, red, tot);
-            }
-            if (rb + 1 < nref) factor_block(a, cols, la, rb + 1, red, tot, taus_local);
+            apply_block(vb, a.ldv, tin, rb, nr, cols + (size_t)la * KB * m, m, red, tot, wsm);
+            if (rb + 1 < nref) factor_block(a, cols + (size_t)la * KB * m, rb + 1, red, tot, tsm);
         }
-        // the other owned blocks after rb
-        {
-            int slot[MAXC];
-            int cnt = 0;
 #pragma unroll
-            for (int q = 0; q < OWNB; ++q)
-                if (q != la && blk[q] > rb && blk[q] < nblk)
-                    for (int r = 0; r < KB; ++r)
-                        if (blk[q] * KB + r < nc) slot[cnt++] = q * KB + r;
-            if (cnt > 0)
-                for (int r = 0; r < KB; ++r) {
-                    const int64_t t = rb * KB + r;
-                    if (t >= n) break;
-                    if (taus[r].x != 0.f)
-                        apply_reflector(a, vb + (size_t)r * m, taus[r], t, cols, slot, cnt, red, tot);
-                }
-        }
+        for (int q = 0; q < OWNB; ++q)
+            if (q != la && blk[q] > rb && blk[q] < nblk)
+                apply_block(vb, a.ldv, tin, rb, nr, cols + (size_t)q * KB * m, m, red, tot, wsm);
         __syncthreads();
     }
 #pragma unroll
@@ -289,15 +370,32 @@ __global__ void __launch_bounds__(TI) rinv_ff_kernel(const double* __restrict__ 
         t[k] = make_float2(k == j ? 1.f : 0.f, 0.f);
     }
     __syncthreads();
+    // column k of R for this thread's rows, loaded one step ahead
+    constexpr int RPT = 8;       // rows per thread: n <= TI * RPT
+    double rk[RPT];
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+        const int64_t i = threadIdx.x + (int64_t)s * TI;
+        rk[s] = (i < j) ? R[i + j * ldr] : 0.0;
+    }
     for (int64_t k = j; k >= 0; --k) {
+        double rn[RPT];
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) {
+            const int64_t i = threadIdx.x + (int64_t)s * TI;
+            rn[s] = (k > 0 && i < k - 1) ? R[i + (k - 1) * ldr] : 0.0;
+        }
         const float2 xk = ff_mul(t[k], dinv[k]);
         __syncthreads();
         if (threadIdx.x == 0) t[k] = xk;
-        for (int64_t i = threadIdx.x; i < k; i += TI) {
-            const float2 r = ff_split(R[i + k * ldr]);
-            t[i] = ff_add(t[i], ff_neg(ff_mul(r, xk)));
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) {
+            const int64_t i = threadIdx.x + (int64_t)s * TI;
+            if (i < k) t[i] = ff_add(t[i], ff_neg(ff_mul(ff_split(rk[s]), xk)));
         }
         __syncthreads();
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) rk[s] = rn[s];
     }
     for (int64_t i = threadIdx.x; i < n; i += TI)
         Ri[i + j * ldi] = (i <= j) ? ff_to_double(t[i]) : 0.0;
@@ -308,20 +406,27 @@ static const void* qr_kernel() { return (const void*)qr_ff_kernel<OWNB>; }
 
 }  // namespace qrff
 
-// Whether the float-float QR fits: the owned column blocks and one
-// reflector block in shared memory, one CTA per SM.
+// Dynamic shared memory of the QR kernel: the owned blocks (stride m) and
+// one received reflector block (stride m rounded up to even).
+static size_t qr_ff_smem(int64_t ownb, int64_t m) {
+    return ((size_t)ownb * qrff::KB * m + (size_t)qrff::KB * ((m + 1) & ~1LL)) * sizeof(float2);
+}
+
+// Owned column blocks per CTA for the float-float QR (0: does not fit): the
+// owned blocks and one received reflector block in shared memory, one CTA
+// per SM.
 static int qr_ff_ownb(const Ctx& ctx, int64_t m, int64_t nc) {
     const int64_t nblk = (nc + qrff::KB - 1) / qrff::KB;
     const int64_t G = nblk < ctx.sm_count ? nblk : ctx.sm_count;
     const int64_t ownb = (nblk + G - 1) / G;
     if (ownb > qrff::MAX_OWNB) return 0;
-    const size_t smem = (size_t)(ownb + 1) * qrff::KB * m * sizeof(float2);
+    const size_t smem = qr_ff_smem(ownb, m);
     if (smem > 200 * 1024) return 0;
     return (int)ownb;
 }
 
 bool qr_ff_supported(const Ctx& ctx, int64_t m, int64_t n, int64_t nc) {
-    return m >= n && n >= 1 && nc >= n && qr_ff_ownb(ctx, m, nc) > 0;
+    return m >= n && n >= 1 && nc >= n && n <= qrff::TI * 8 && qr_ff_ownb(ctx, m, nc) > 0;
 }
 
 void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld) {
@@ -330,7 +435,7 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     if (ownb == 0 || m < n) fail(RNLA_ERR_UNSUPPORTED, "float-float QR: the sketch does not fit in shared memory");
     const int64_t nblk = (nc + KB - 1) / KB;
     const int64_t G = nblk < ctx.sm_count ? nblk : ctx.sm_count;
-    const size_t smem = (size_t)(ownb + 1) * KB * m * sizeof(float2);
+    const size_t smem = qr_ff_smem(ownb, m);
     const void* k = ownb == 1 ? qr_kernel<1>() : ownb == 2 ? qr_kernel<2>() : ownb == 3 ? qr_kernel<3>() : qr_kernel<4>();
     RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
@@ -338,11 +443,12 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     if ((int64_t)nb * ctx.sm_count < G) fail(RNLA_ERR_UNSUPPORTED, "float-float QR: grid not co-resident");
     cudaStream_t s = ctx.stream;
     const int64_t nref = (n + KB - 1) / KB;
-    DevBuf<float2> VF((size_t)m * n, s), tauF(n, s);
+    const int64_t ldv = (m + 1) & ~1LL;
+    DevBuf<float2> VF((size_t)ldv * n, s), TF((size_t)nref * (KB * KB + KB), s);
     DevBuf<unsigned int> flags(nref, s);
     RNLA_CUDA(cudaMemsetAsync(flags.get(), 0, nref * sizeof(unsigned int), s));
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), s));
-    Args a{X, m, n, nc, ld, VF.get(), tauF.get(), flags.get(), ctx.status};
+    Args a{X, m, n, nc, ld, ldv, VF.get(), TF.get(), flags.get(), ctx.status};
     void* args[] = {&a};
     RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3((unsigned)G), dim3(T), args, smem, s));
     count_launch();
@@ -352,8 +458,8 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
 bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi) {
     using namespace qrff;
     if (n <= 0) return true;
+    if (n > TI * 8) fail(RNLA_ERR_UNSUPPORTED, "float-float R^-1: n > 1024");
     const size_t smem = (size_t)2 * n * sizeof(float2);
-    if (smem > 200 * 1024) fail(RNLA_ERR_UNSUPPORTED, "float-float R^-1: n too large");
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(rinv_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     DevBuf<unsigned int> sing(1, ctx.stream);
