@@ -151,6 +151,7 @@ typedef struct {
     int32_t orth_fallbacks;   /* CholeskyQR2 -> Householder fallbacks taken */
     int32_t precision_used;
     double ms_sketch, ms_factor, ms_solve, ms_total;  /* device-timed stages */
+    double ms_kernel;         /* the inner solver's persistent kernel alone (device-timed; LSQR) */
 } rnla_stats;
 
 /* Defaults: FP64, reference mode, CGLS, power_iters 2, Philox4x32 key 0,

@@ -398,6 +398,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         st->ms_factor = tm.ms(1, 2);
         st->ms_solve = tm.ms(2, 3);
         st->ms_total = tm.ms(0, 3);
+        st->ms_kernel = lr.ms_kernel;
     }
 }
 

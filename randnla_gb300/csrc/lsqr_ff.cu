@@ -915,12 +915,22 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     a.calc_var = (prm.calc_var && var) ? 1 : 0;
     a.bar.count = bar.get(); a.bar.gen = bar.get() + 1; a.bar.status = ctx.status;
     void* params[] = {&a};
+    cudaEvent_t ev[2];
+    RNLA_CUDA(cudaEventCreate(&ev[0]));
+    RNLA_CUDA(cudaEventCreate(&ev[1]));
+    RNLA_CUDA(cudaEventRecord(ev[0], st));
     RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(T), params, smem, st));
     count_launch();
+    RNLA_CUDA(cudaEventRecord(ev[1], st));
     double h[8];
     RNLA_CUDA(cudaMemcpyAsync(h, out.get(), sizeof h, cudaMemcpyDeviceToHost, st));
     ctx.check_status("lsqr");
+    float kms = 0.f;
+    RNLA_CUDA(cudaEventElapsedTime(&kms, ev[0], ev[1]));
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
     LsqrResult r;
+    r.ms_kernel = kms;
     r.istop = (int64_t)h[0]; r.itn = (int64_t)h[1];
     r.r1norm = h[2]; r.r2norm = h[3]; r.anorm = h[4]; r.acond = h[5]; r.xnorm = h[6]; r.arnorm = h[7];
     return r;

@@ -78,6 +78,7 @@ struct LsqrParams {
 struct LsqrResult {
     int64_t istop = 0, itn = 0;
     double r1norm = 0, r2norm = 0, anorm = 0, acond = 0, xnorm = 0, arnorm = 0;
+    double ms_kernel = 0;   // device time of the persistent kernel
 };
 // LSQR on the operator A M (M upper-triangular n x n, or identity if
 // Minv_rowmajor == nullptr).  A is double (a64) or float (a32), m x n, lda.
