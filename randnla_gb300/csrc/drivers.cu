@@ -342,6 +342,9 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     } else {
         if (!tc_available(ctx))
             fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
+        // the whole BF16X solve is enqueued without intermediate host
+        // synchronisation; the device status is checked once at the end
+        ctx.deferred = true;
         // S [a b] in one pass: b rides along as column n of the digit planes
         tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d);
     }
@@ -383,6 +386,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     }
     trmv_upper(ctx, Mi, n, n, z, x);                                // line 58
     tm.mark();
+    if (ctx.deferred) ctx.finish("blendenpik (BF16X)");
     if (st) {
         st->iterations = iters;
         st->istop = istop;

@@ -877,7 +877,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaMemsetAsync(bar.get(), 0, 2 * sizeof(unsigned int), st));
     RNLA_CUDA(cudaMemsetAsync(out.get(), 0, 8 * sizeof(double), st));
     RNLA_CUDA(cudaMemsetAsync(yF.get(), 0, ldf * sizeof(float2), st));
-    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), st));
+    ctx.clear_status();
     {
         dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
         rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, reinterpret_cast<float*>(AF.get()), ldf);
@@ -924,6 +924,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaEventRecord(ev[1], st));
     double h[8];
     RNLA_CUDA(cudaMemcpyAsync(h, out.get(), sizeof h, cudaMemcpyDeviceToHost, st));
+    RNLA_CUDA(cudaStreamSynchronize(st));
     ctx.check_status("lsqr");
     float kms = 0.f;
     RNLA_CUDA(cudaEventElapsedTime(&kms, ev[0], ev[1]));

@@ -154,28 +154,59 @@ __device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int6
 }
 
 // Factors the block b held at c (KB columns, stride m; columns >= nc are
-// absent), forms T and publishes V, T and the flag.
+// absent), writing each reflector to global memory as soon as it is formed;
+// then forms T and publishes T, tau and the flag.  The Gram entries
+// g_qr = v_q^T v_r that T needs ride in column r's norm reduction:
+// sum_{i>t} v_q[i] c_r[i] is reduced with ||c_r[t+1:]||^2, and
+// g_qr = v_q[t] + scale_r * that sum once v_r = c_r scale_r is known.
 __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, float2* tot, float2* tsm) {
     const int64_t m = a.m, n = a.n, nc = a.nc;
     const int64_t t0 = b * KB;
     const int nr = (int)min((int64_t)KB, n - t0);
     const int ncol = (int)min((int64_t)KB, nc - t0);
     float2* taus = tsm + KB * KB;
-    for (int r = 0; r < nr; ++r) {
+    float2 g[KB][KB];                      // g[q][r], q < r (all threads hold the same values)
+#pragma unroll
+    for (int q = 0; q < KB; ++q)
+#pragma unroll
+        for (int r = 0; r < KB; ++r) g[q][r] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < KB; ++r) {
+        if (r >= nr) break;
         const int64_t t = t0 + r;
         float2* col = c + (size_t)r * m;
-        float h[1] = {0.f}, l[1] = {0.f};
-        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) ff_madd(col[i].x, col[i].y, col[i].x, col[i].y, h[0], l[0]);
-        block_sums<1>(h, l, red, tot);
+        // ||c_r[t+1:]||^2 (slot 0) and sum_{i>t} v_q[i] c_r[i] for q < r (slots 1 + q)
+        float h[KB], l[KB];
+#pragma unroll
+        for (int k = 0; k < KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
+        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
+            const float2 x = col[i];
+            ff_madd(x.x, x.y, x.x, x.y, h[0], l[0]);
+#pragma unroll
+            for (int q = 0; q < KB - 1; ++q)
+                if (q < r) {
+                    const float2 vq = c[(size_t)q * m + i];
+                    ff_madd(vq.x, vq.y, x.x, x.y, h[1 + q], l[1 + q]);
+                }
+        }
+        block_sums<KB>(h, l, red, tot);
         const float2 xn2 = tot[0];
         const float2 alpha = col[t];
-        float2 tau = make_float2(0.f, 0.f), beta = alpha;
+        float2 tau = make_float2(0.f, 0.f), beta = alpha, scale = make_float2(0.f, 0.f);
         if (xn2.x != 0.f) {
             const float2 nrm = ff_sqrt(ff_add(ff_mul(alpha, alpha), xn2));
             beta = (alpha.x >= 0.f) ? ff_neg(nrm) : nrm;
-            const float2 scale = ff_div(make_float2(1.f, 0.f), ff_add(alpha, ff_neg(beta)));
-            for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) col[i] = ff_mul(col[i], scale);
+            scale = ff_div(make_float2(1.f, 0.f), ff_add(alpha, ff_neg(beta)));
             tau = ff_div(ff_add(beta, ff_neg(alpha)), beta);
+        }
+#pragma unroll
+        for (int q = 0; q < KB - 1; ++q)
+            if (q < r) g[q][r] = ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[1 + q]));
+        // scale into the reflector and publish it (rows > t)
+        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
+            const float2 v = (xn2.x != 0.f) ? ff_mul(col[i], scale) : col[i];
+            col[i] = v;
+            a.VF[i + t * a.ldv] = v;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -211,47 +242,39 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
         }
     }
     // T (dlarft, forward, columnwise): T[s][s] = tau_s,
-    // T[0:s, s] = -tau_s T[0:s, 0:s] V[:, 0:s]^T v_s, with g_rs = v_r^T v_s.
-    {
-        float h[8], l[8];                  // pairs (r, s), r < s: (0,1) (0,2) (1,2) (0,3) (1,3) (2,3)
+    // T[0:s, s] = -tau_s T[0:s, 0:s] (g[0:s][s]); unrolled, in registers.
+    if (threadIdx.x == 0) {
+        float2 Tm[KB][KB];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) { h[k] = 0.f; l[k] = 0.f; }
-        for (int64_t i = t0 + 1 + threadIdx.x; i < m; i += T) {
-            float2 v[KB];
+        for (int r = 0; r < KB; ++r)
 #pragma unroll
-            for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(c + (size_t)r * m, i, t0 + r) : make_float2(0.f, 0.f);
-            ff_madd(v[0].x, v[0].y, v[1].x, v[1].y, h[0], l[0]);
-            ff_madd(v[0].x, v[0].y, v[2].x, v[2].y, h[1], l[1]);
-            ff_madd(v[1].x, v[1].y, v[2].x, v[2].y, h[2], l[2]);
-            ff_madd(v[0].x, v[0].y, v[3].x, v[3].y, h[3], l[3]);
-            ff_madd(v[1].x, v[1].y, v[3].x, v[3].y, h[4], l[4]);
-            ff_madd(v[2].x, v[2].y, v[3].x, v[3].y, h[5], l[5]);
-        }
-        block_sums<8>(h, l, red, tot);
-        if (threadIdx.x == 0) {
-            float2 Tm[KB * KB];
+            for (int s2 = 0; s2 < KB; ++s2) Tm[r][s2] = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < KB * KB; ++k) Tm[k] = make_float2(0.f, 0.f);
-            const int gi[KB][KB] = {{-1, 0, 1, 3}, {-1, -1, 2, 4}, {-1, -1, -1, 5}, {-1, -1, -1, -1}};
-            for (int s = 0; s < nr; ++s) {
-                Tm[s + s * KB] = taus[s];
-                for (int r = 0; r < s; ++r) {
-                    float2 acc = make_float2(0.f, 0.f);
-                    for (int k = r; k < s; ++k) acc = ff_add(acc, ff_mul(Tm[r + k * KB], tot[gi[k][s]]));
-                    Tm[r + s * KB] = ff_neg(ff_mul(taus[s], acc));
-                }
+        for (int s2 = 0; s2 < KB; ++s2) {
+            if (s2 < nr) {
+                const float2 ts = taus[s2];
+                Tm[s2][s2] = ts;
+#pragma unroll
+                for (int r = 0; r < KB; ++r)
+                    if (r < s2) {
+                        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int k = 0; k < KB; ++k)
+                            if (k >= r && k < s2) acc = ff_add(acc, ff_mul(Tm[r][k], g[k][s2]));
+                        Tm[r][s2] = ff_neg(ff_mul(ts, acc));
+                    }
             }
-            for (int k = 0; k < KB * KB; ++k) tsm[k] = Tm[k];
         }
-        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < KB; ++r)
+#pragma unroll
+            for (int s2 = 0; s2 < KB; ++s2) {
+                tsm[r + s2 * KB] = Tm[r][s2];
+                a.TF[b * (KB * KB + KB) + r + s2 * KB] = Tm[r][s2];
+            }
+#pragma unroll
+        for (int r = 0; r < KB; ++r) a.TF[b * (KB * KB + KB) + KB * KB + r] = taus[r];
     }
-    // publish
-    for (int r = 0; r < nr; ++r) {
-        const int64_t t = t0 + r;
-        const float2* col = c + (size_t)r * m;
-        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) a.VF[i + t * a.ldv] = col[i];
-    }
-    if ((int)threadIdx.x < KB * KB + KB) a.TF[b * (KB * KB + KB) + threadIdx.x] = tsm[threadIdx.x];
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -365,7 +388,7 @@ __global__ void __launch_bounds__(TI) rinv_ff_kernel(const double* __restrict__ 
     const int64_t j = blockIdx.x;
     for (int64_t k = threadIdx.x; k < n; k += TI) {
         const float2 d = ff_split(R[k + k * ldr]);
-        if (d.x == 0.f) atomicExch(singular, 1u);
+        if (d.x == 0.f) atomicCAS(singular, 0u, (unsigned int)KSTATUS_SINGULAR);
         dinv[k] = (d.x == 0.f) ? make_float2(0.f, 0.f) : ff_div(make_float2(1.f, 0.f), d);
         t[k] = make_float2(k == j ? 1.f : 0.f, 0.f);
     }
@@ -447,7 +470,7 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     DevBuf<float2> VF((size_t)ldv * n, s), TF((size_t)nref * (KB * KB + KB), s);
     DevBuf<unsigned int> flags(nref, s);
     RNLA_CUDA(cudaMemsetAsync(flags.get(), 0, nref * sizeof(unsigned int), s));
-    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), s));
+    ctx.clear_status();
     Args a{X, m, n, nc, ld, ldv, VF.get(), TF.get(), flags.get(), ctx.status};
     void* args[] = {&a};
     RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3((unsigned)G), dim3(T), args, smem, s));
@@ -462,12 +485,17 @@ bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double*
     const size_t smem = (size_t)2 * n * sizeof(float2);
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(rinv_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    DevBuf<unsigned int> sing(1, ctx.stream);
-    RNLA_CUDA(cudaMemsetAsync(sing.get(), 0, sizeof(unsigned int), ctx.stream));
-    rinv_ff_kernel<<<(unsigned)n, TI, smem, ctx.stream>>>(R, n, ldr, Rinv, ldi, sing.get());
+    // a zero pivot is reported through the status word (KSTATUS_SINGULAR):
+    // at once, or at the pending check in deferred mode
+    ctx.clear_status();
+    rinv_ff_kernel<<<(unsigned)n, TI, smem, ctx.stream>>>(R, n, ldr, Rinv, ldi, ctx.status);
     RNLA_LAUNCH_CHECK();
+    if (ctx.deferred) {
+        ctx.check_status("R^-1 of the sketch (float-float)");
+        return true;
+    }
     unsigned int h = 0;
-    RNLA_CUDA(cudaMemcpyAsync(&h, sing.get(), sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
     return h == 0;
 }

@@ -44,12 +44,23 @@ struct Ctx {
     int device = 0;
     int sm_count = 0;
     unsigned int* status = nullptr;   // device word: nonzero = kernel-side failure code
+    // Deferred mode: the status word is not cleared between kernels (the
+    // first failure code sticks, and later kernels that poll it stop early)
+    // and check_status does not synchronise; finish() does one check.
+    bool deferred = false;
+    const char* deferred_where = nullptr;
     explicit Ctx(cudaStream_t s);
     ~Ctx();
     Ctx(const Ctx&) = delete;
     Ctx& operator=(const Ctx&) = delete;
-    // Reads the device status word (synchronises the stream).
+    // Clears the status word before a kernel that reports through it (no-op
+    // in deferred mode).
+    void clear_status();
+    // Reads the device status word (synchronises the stream); in deferred
+    // mode only remembers `where`.
     void check_status(const char* where);
+    // Leaves deferred mode and performs the pending check (synchronises).
+    void finish(const char* where);
 };
 
 // Device buffer allocated from the library's stream-ordered pool and freed

@@ -71,12 +71,14 @@ __device__ __forceinline__ float2 ff_fma(float2 a, float2 b, float2 c) { return 
 
 __device__ __forceinline__ double ff_to_double(float2 a) { return (double)a.x + (double)a.y; }
 
-// a / b: two-term long division (Dekker): q1 = a.hi / b.hi, q2 from the
-// float-float remainder a - q1 b; relative error ~2^-46.
+// a / b: two-term long division (Dekker): q1 ~ a.hi / b.hi, q2 from the
+// float-float remainder a - q1 b (formed exactly), so q1 needs only FP32
+// accuracy and comes from the fast approximate divide; relative error
+// ~2^-44.  b must be a normal, nonzero number.
 __device__ __forceinline__ float2 ff_div(float2 a, float2 b) {
-    const float q1 = __fdiv_rn(a.x, b.x);
+    const float q1 = __fdividef(a.x, b.x);
     const float2 r = ff_add(a, ff_neg(ff_mul(make_float2(q1, 0.f), b)));
-    const float q2 = __fdiv_rn(r.x, b.x);
+    const float q2 = __fdividef(r.x, b.x);
     return ff_norm(q1, q2);
 }
 

@@ -75,7 +75,21 @@ Ctx::~Ctx() {
     if (status) pool_free(status, stream);
 }
 
+void Ctx::clear_status() {
+    if (!deferred) RNLA_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned int), stream));
+}
+
+void Ctx::finish(const char* where) {
+    deferred = false;
+    check_status(deferred_where ? deferred_where : where);
+    deferred_where = nullptr;
+}
+
 void Ctx::check_status(const char* where) {
+    if (deferred) {
+        if (!deferred_where) deferred_where = where;
+        return;
+    }
     unsigned int h = 0;
     RNLA_CUDA(cudaMemcpyAsync(&h, status, sizeof h, cudaMemcpyDeviceToHost, stream));
     RNLA_CUDA(cudaStreamSynchronize(stream));
