@@ -16,7 +16,8 @@
 //   row warps 0-7     tile k: warp w forms t_r = (A y)_r for rows
 //                     r = w + 8 s (s < RW): 16-byte chunks of the row, y in
 //                     registers, exact FMA products summed with TwoSum on
-//                     packed pairs, a warp butterfly; lane s then forms
+//                     packed pairs, a warp reduce-scatter over the RW rows;
+//                     one lane per row forms
 //                     u_r = c1 t_r + c2 u_r + c3 b_r, accumulates ||u||^2 and
 //                     hands u to the column warps (double-buffered, named
 //                     barriers: bar.arrive "u ready", bar.sync "u consumed");
@@ -180,13 +181,18 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
             yl[k] = pk2(y0.y, y1.y);
         }
         float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
-        // lane s < RW owns row warp + 8 s of every tile; its old value and b
-        // are loaded two tiles ahead (the loads sit behind the streaming)
-        auto row_of = [&](int64_t kk) { return ((int64_t)blockIdx.x + kk * (int64_t)gridDim.x) * R + warp + WA * lane; };
+        // After the reduce-scatter below, lane l holds the sum of row slot
+        // l >> SHL; the first lane of each group (owner) forms that row's u.
+        // Its old value and b are loaded two tiles ahead (the loads sit
+        // behind the streaming).
+        constexpr int SHL = (RW == 1) ? 5 : (RW == 2) ? 4 : (RW == 4) ? 3 : 2;
+        const bool owner = (lane & ((1 << SHL) - 1)) == 0;
+        const int rw = lane >> SHL;                      // row slot of an owner lane
+        auto row_of = [&](int64_t kk) { return ((int64_t)blockIdx.x + kk * (int64_t)gridDim.x) * R + warp + WA * rw; };
         auto fetch = [&](int64_t kk, float2& u, float2& bv) {
             u = make_float2(0.f, 0.f);
             bv = make_float2(0.f, 0.f);
-            if (lane < RW && kk < ntl) {
+            if (owner && kk < ntl) {
                 const int64_t i = row_of(kk);
                 if (i < a.m) {
                     if (oldv) u = oldv[i];
@@ -210,7 +216,7 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
             const int64_t r0 = t * R;
             const int rows = (int)min((int64_t)R, a.m - r0);
             const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
-            const bool mine = lane < RW && warp + WA * lane < rows;
+            const bool mine = owner && warp + WA * rw < rows;
             float tvh[RW], tvl[RW];
 #pragma unroll
             for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
@@ -238,23 +244,35 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
                     tvh[w] = h;
                     tvl[w] = l;
                 }
+                // reduce-scatter: each exchange level halves the rows a lane
+                // keeps (lanes with the level's bit set keep the upper half)
+                int off = 16;
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1)
+                for (int half = RW / 2; half >= 1; half /= 2) {
+                    const bool up = (lane & off) != 0;
 #pragma unroll
-                    for (int w = 0; w < RW; ++w) {
-                        const float oh = __shfl_xor_sync(0xffffffffu, tvh[w], o);
-                        const float ol = __shfl_xor_sync(0xffffffffu, tvl[w], o);
-                        ff_acc(tvh[w], tvl[w], oh, ol);
+                    for (int k2 = 0; k2 < half; ++k2) {
+                        const float sh_ = up ? tvh[k2] : tvh[k2 + half], sl_ = up ? tvl[k2] : tvl[k2 + half];
+                        float kh = up ? tvh[k2 + half] : tvh[k2], kl = up ? tvl[k2 + half] : tvl[k2];
+                        const float rh = __shfl_xor_sync(0xffffffffu, sh_, off);
+                        const float rl = __shfl_xor_sync(0xffffffffu, sl_, off);
+                        ff_acc(kh, kl, rh, rl);
+                        tvh[k2] = kh;
+                        tvl[k2] = kl;
                     }
+                    off >>= 1;
+                }
+                for (; off >= 1; off >>= 1) {
+                    const float oh = __shfl_xor_sync(0xffffffffu, tvh[0], off);
+                    const float ol = __shfl_xor_sync(0xffffffffu, tvl[0], off);
+                    ff_acc(tvh[0], tvl[0], oh, ol);
+                }
             }
             float2 nv = make_float2(0.f, 0.f);
             int r = 0;
             if (mine) {
-                float th = tvh[0], tl = tvl[0];
-#pragma unroll
-                for (int w = 1; w < RW; ++w)
-                    if (lane == w) { th = tvh[w]; tl = tvl[w]; }
-                r = warp + WA * lane;
+                const float th = tvh[0], tl = tvl[0];
+                r = warp + WA * rw;
                 const float2 tv = ff_norm(th, tl);
                 nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
             }

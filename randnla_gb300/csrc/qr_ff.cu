@@ -144,10 +144,11 @@ __device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int6
         for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < KB; ++q) {
-            float2 x = c[(size_t)q * m + i];
+            const float2 x = c[(size_t)q * m + i];
+            float xh = x.x, xl = x.y;                 // unnormalised accumulator, one renormalisation
 #pragma unroll
-            for (int r = 0; r < KB; ++r) x = ff_fma(v[r], wv[q * KB + r], x);
-            c[(size_t)q * m + i] = x;
+            for (int r = 0; r < KB; ++r) ff_madd(v[r].x, v[r].y, wv[q * KB + r].x, wv[q * KB + r].y, xh, xl);
+            c[(size_t)q * m + i] = ff_norm(xh, xl);
         }
     }
     __syncthreads();
@@ -236,7 +237,12 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
                 const float2 vi = (i == t) ? make_float2(1.f, 0.f) : col[i];
 #pragma unroll
                 for (int q = 0; q < KB; ++q)
-                    if (q > r && q < ncol) c[(size_t)q * m + i] = ff_fma(f[q], vi, c[(size_t)q * m + i]);
+                    if (q > r && q < ncol) {
+                        const float2 x = c[(size_t)q * m + i];
+                        float xh = x.x, xl = x.y;
+                        ff_madd(f[q].x, f[q].y, vi.x, vi.y, xh, xl);
+                        c[(size_t)q * m + i] = ff_norm(xh, xl);
+                    }
             }
             __syncthreads();
         }
@@ -379,46 +385,64 @@ __global__ void __launch_bounds__(T, 1) qr_ff_kernel(Args a) {
 // ---- R^-1 ----
 constexpr int TI = 128;
 
-__global__ void __launch_bounds__(TI) rinv_ff_kernel(const double* __restrict__ R, int64_t n, int64_t ldr,
+// RF = split(R) (upper triangle, column-major n x n)
+__global__ void rsplit_kernel(const double* __restrict__ R, int64_t n, int64_t ldr, float2* __restrict__ RF) {
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % n, j = idx / n;
+        RF[idx] = (i <= j) ? ff_split(R[i + j * ldr]) : make_float2(0.f, 0.f);
+    }
+}
+
+// One CTA per column j of R^-1: x_k = t_k / r_kk, t_{<k} -= r_{<k,k} x_k,
+// k = j .. 0, t = e_j in shared memory.  The thread's entries of the next
+// two columns of R are loaded ahead, so the L2 latency overlaps the steps.
+__global__ void __launch_bounds__(TI) rinv_ff_kernel(const float2* __restrict__ RF, int64_t n,
                                                      double* __restrict__ Ri, int64_t ldi,
-                                                     unsigned int* __restrict__ singular) {
+                                                     unsigned int* __restrict__ status) {
     extern __shared__ __align__(16) float2 smi[];
     float2* dinv = smi;          // n reciprocal pivots
     float2* t = smi + n;         // n: right-hand side / solution
     const int64_t j = blockIdx.x;
     for (int64_t k = threadIdx.x; k < n; k += TI) {
-        const float2 d = ff_split(R[k + k * ldr]);
-        if (d.x == 0.f) atomicCAS(singular, 0u, (unsigned int)KSTATUS_SINGULAR);
+        const float2 d = RF[k + k * n];
+        if (d.x == 0.f) atomicCAS(status, 0u, (unsigned int)KSTATUS_SINGULAR);
         dinv[k] = (d.x == 0.f) ? make_float2(0.f, 0.f) : ff_div(make_float2(1.f, 0.f), d);
         t[k] = make_float2(k == j ? 1.f : 0.f, 0.f);
     }
     __syncthreads();
-    // column k of R for this thread's rows, loaded one step ahead
     constexpr int RPT = 8;       // rows per thread: n <= TI * RPT
-    double rk[RPT];
+    float2 r0[RPT], r1[RPT];     // columns k and k - 1 (thread's rows)
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
         const int64_t i = threadIdx.x + (int64_t)s * TI;
-        rk[s] = (i < j) ? R[i + j * ldr] : 0.0;
+        r0[s] = (i < j) ? RF[i + j * n] : make_float2(0.f, 0.f);
+        r1[s] = (j > 0 && i < j - 1) ? RF[i + (j - 1) * n] : make_float2(0.f, 0.f);
     }
     for (int64_t k = j; k >= 0; --k) {
-        double rn[RPT];
+        float2 r2[RPT];          // column k - 2
 #pragma unroll
         for (int s = 0; s < RPT; ++s) {
             const int64_t i = threadIdx.x + (int64_t)s * TI;
-            rn[s] = (k > 0 && i < k - 1) ? R[i + (k - 1) * ldr] : 0.0;
+            r2[s] = (k > 1 && i < k - 2) ? RF[i + (k - 2) * n] : make_float2(0.f, 0.f);
         }
         const float2 xk = ff_mul(t[k], dinv[k]);
         __syncthreads();
         if (threadIdx.x == 0) t[k] = xk;
+        const float2 nx = ff_neg(xk);
 #pragma unroll
         for (int s = 0; s < RPT; ++s) {
             const int64_t i = threadIdx.x + (int64_t)s * TI;
-            if (i < k) t[i] = ff_add(t[i], ff_neg(ff_mul(ff_split(rk[s]), xk)));
+            if (i < k) {
+                const float2 ti = t[i];
+                float h = ti.x, l = ti.y;
+                ff_madd(r0[s].x, r0[s].y, nx.x, nx.y, h, l);
+                t[i] = ff_norm(h, l);
+            }
         }
         __syncthreads();
 #pragma unroll
-        for (int s = 0; s < RPT; ++s) rk[s] = rn[s];
+        for (int s = 0; s < RPT; ++s) { r0[s] = r1[s]; r1[s] = r2[s]; }
     }
     for (int64_t i = threadIdx.x; i < n; i += TI)
         Ri[i + j * ldi] = (i <= j) ? ff_to_double(t[i]) : 0.0;
@@ -488,7 +512,14 @@ bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double*
     // a zero pivot is reported through the status word (KSTATUS_SINGULAR):
     // at once, or at the pending check in deferred mode
     ctx.clear_status();
-    rinv_ff_kernel<<<(unsigned)n, TI, smem, ctx.stream>>>(R, n, ldr, Rinv, ldi, ctx.status);
+    DevBuf<float2> RF((size_t)n * n, ctx.stream);
+    {
+        int g = (int)div_up(n * n, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        rsplit_kernel<<<g, 256, 0, ctx.stream>>>(R, n, ldr, RF);
+        RNLA_LAUNCH_CHECK();
+    }
+    rinv_ff_kernel<<<(unsigned)n, TI, smem, ctx.stream>>>(RF, n, Rinv, ldi, ctx.status);
     RNLA_LAUNCH_CHECK();
     if (ctx.deferred) {
         ctx.check_status("R^-1 of the sketch (float-float)");
