@@ -349,6 +349,11 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d);
     }
     tm.mark();
+    // BF16X + LSQR: the float-float copies of A and b for the solver are built
+    // on the side stream while the QR runs
+    LsqrFFInput lsqr_in;
+    if (o.precision != RNLA_PREC_FP64 && o.inner_solver != RNLA_SOLVER_CGLS && !a_f32 && lsqr_ff_supported(n))
+        lsqr_ff_prepare(ctx, static_cast<const double*>(Av), m, n, lda, b, lsqr_in);
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
     DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
     bool inv_ok;
@@ -380,7 +385,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         p.iter_lim = l;
         if (o.atol == 0.0 && o.btol == 0.0) p.abs_arnorm_tol = epsilon;
         lr = lsqr_solve(ctx, a64, a32, m, n, lda, Mi, b, z0, p, z, nullptr, nullptr,
-                        o.precision != RNLA_PREC_FP64);
+                        o.precision != RNLA_PREC_FP64, lsqr_in.ready ? &lsqr_in : nullptr);
         iters = lr.itn;
         istop = lr.istop;
     }

@@ -856,11 +856,41 @@ static const void* pick_kernel(int64_t hp, int& RW) {
 
 bool lsqr_ff_supported(int64_t n) { return n >= 1 && n <= lsff::MAX_N; }
 
+// Float-float copies of A (row-major, column-pair order) and b, enqueued on
+// `st`.
+static void build_ff_input(Ctx& ctx, cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t lda,
+                           const double* b, int64_t ldf, float2* AF, float2* bF) {
+    using namespace lsff;
+    dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
+    rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, reinterpret_cast<float*>(AF), ldf);
+    RNLA_LAUNCH_CHECK();
+    int g = (int)div_up(m, 256);
+    if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+    vec_split_kernel<<<g, 256, 0, st>>>(b, m, bF);
+    RNLA_LAUNCH_CHECK();
+}
+
+void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* b,
+                     LsqrFFInput& in) {
+    if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
+    in.A = A; in.m = m; in.n = n;
+    in.ldf = (n + 1) & ~1LL;
+    in.AF.alloc((size_t)m * in.ldf, ctx.stream);
+    in.bF.alloc(m, ctx.stream);
+    const cudaStream_t side = side_stream(ctx.device);
+    stream_wait(side, ctx.stream);                 // buffers allocated, A and b written
+    build_ff_input(ctx, side, A, m, n, lda, b, in.ldf, in.AF, in.bF);
+    RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
+    in.owner = ctx.stream;
+    RNLA_CUDA(cudaEventRecord(in.ready, side));
+}
+
 LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
-                         double* arnorms_dev) {
+                         double* arnorms_dev, const LsqrFFInput* pre) {
     using namespace lsff;
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
+    if (pre && (pre->A != A || pre->m != m || pre->n != n)) pre = nullptr;
     cudaStream_t st = ctx.stream;
     const int64_t ldf = (n + 1) & ~1LL;
     const int64_t hp = ldf / 2;
@@ -878,12 +908,23 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): kernel does not fit on an SM");
     const int G = ctx.sm_count;
 
-    DevBuf<float2> AF, MF, MtF, bF, x0F, uF, yF, gF, vF, wF, xF, vunF, varF, partF, spF;
+    DevBuf<float2> AFo, MF, MtF, bFo, x0F, uF, yF, gF, vF, wF, xF, vunF, varF, partF, spF;
     DevBuf<float4> colsq;
     DevBuf<double> out;
     DevBuf<unsigned int> bar;
-    AF.alloc((size_t)m * ldf, st);
-    bF.alloc(m, st);
+    const float2* AF;
+    const float2* bF;
+    if (pre) {
+        RNLA_CUDA(cudaStreamWaitEvent(st, pre->ready, 0));
+        AF = pre->AF.get();
+        bF = pre->bF.get();
+    } else {
+        AFo.alloc((size_t)m * ldf, st);
+        bFo.alloc(m, st);
+        build_ff_input(ctx, st, A, m, n, lda, b, ldf, AFo, bFo);
+        AF = AFo.get();
+        bF = bFo.get();
+    }
     uF.alloc(m, st);
     yF.alloc(ldf, st);
     gF.alloc(n, st); vF.alloc(n, st); wF.alloc(n, st); xF.alloc(n, st); vunF.alloc(n, st); varF.alloc(n, st);
@@ -896,15 +937,6 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaMemsetAsync(out.get(), 0, 8 * sizeof(double), st));
     RNLA_CUDA(cudaMemsetAsync(yF.get(), 0, ldf * sizeof(float2), st));
     ctx.clear_status();
-    {
-        dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
-        rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, reinterpret_cast<float*>(AF.get()), ldf);
-        RNLA_LAUNCH_CHECK();
-        int g = (int)div_up(m, 256);
-        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
-        vec_split_kernel<<<g, 256, 0, st>>>(b, m, bF);
-        RNLA_LAUNCH_CHECK();
-    }
     Args a{};
     if (M) {
         MF.alloc((size_t)n * n, st);
@@ -922,8 +954,8 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
         RNLA_LAUNCH_CHECK();
         a.x0F = x0F.get();
     }
-    a.AF = AF.get(); a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.R = R; a.ST = STn; a.ntiles = div_up(m, R);
-    a.bF = bF.get();
+    a.AF = AF; a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.R = R; a.ST = STn; a.ntiles = div_up(m, R);
+    a.bF = bF;
     a.uF = uF.get(); a.yF = yF.get(); a.gF = gF.get(); a.vF = vF.get(); a.wF = wF.get(); a.xF = xF.get();
     a.vunF = vunF.get(); a.varF = varF.get(); a.partF = partF.get(); a.spF = spF.get(); a.colsq = colsq.get();
     a.x = x; a.var = var; a.arn = arnorms_dev; a.out = out.get();

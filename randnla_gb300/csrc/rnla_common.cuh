@@ -90,6 +90,10 @@ struct DevBuf {
     operator T*() const { return p; }
 };
 
+// Second stream of a device, and an event-based dependency `to` -> `from`.
+cudaStream_t side_stream(int device);
+void stream_wait(cudaStream_t to, cudaStream_t from);
+
 void* pool_alloc(size_t bytes, cudaStream_t s);
 void pool_free(void* p, cudaStream_t s);
 

@@ -84,20 +84,43 @@ struct LsqrResult {
 // Minv_rowmajor == nullptr).  A is double (a64) or float (a32), m x n, lda.
 // x0 nullable; x receives z (the solution of the preconditioned problem,
 // i.e. the caller applies M afterwards).  arnorms_dev nullable (iter_lim values).
+struct LsqrFFInput;
 LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                       int64_t lda, const double* M, const double* b, const double* x0,
                       const LsqrParams& prm, double* x, double* var, double* arnorms_dev,
-                      bool ffp);
+                      bool ffp, const LsqrFFInput* pre = nullptr);
 // CGLS (cg.rs:18-61) on A M, same conventions; returns iterations used.
 int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                    int64_t lda, const double* M, const double* b, const double* x0,
                    double tolerance, int64_t num_iterations, double* x, bool* converged);
 // Float-float LSQR (lsqr_ff.cu) on FP64 data, 1 <= n <= 1024; same contract
-// as lsqr_solve.
+// as lsqr_solve.  lsqr_ff_prepare builds the float-float copies of A and b
+// on the side stream (so they overlap earlier work on ctx.stream);
+// lsqr_ff_solve waits for them (or builds them itself when `pre` is null).
+struct LsqrFFInput {
+    DevBuf<float2> AF, bF;
+    const double* A = nullptr;
+    int64_t m = 0, n = 0, ldf = 0;
+    cudaEvent_t ready = nullptr;
+    cudaStream_t owner = nullptr;   // stream the buffers are freed on
+    LsqrFFInput() = default;
+    LsqrFFInput(const LsqrFFInput&) = delete;
+    LsqrFFInput& operator=(const LsqrFFInput&) = delete;
+    // the buffers are released only after the side-stream copies (an early
+    // error return must not free memory still being written)
+    ~LsqrFFInput() {
+        if (ready) {
+            cudaStreamWaitEvent(owner, ready, 0);
+            cudaEventDestroy(ready);
+        }
+    }
+};
 bool lsqr_ff_supported(int64_t n);
+void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* b,
+                     LsqrFFInput& in);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
-                         double* arnorms_dev);
+                         double* arnorms_dev, const LsqrFFInput* pre = nullptr);
 // Workspace-based LSQR used by the allocation-free entry point (noalloc.cu).
 size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem,
                             const void** kernel);

@@ -64,6 +64,29 @@ static int sm_count_of(int dev) {
     return c;
 }
 
+// A second, non-blocking stream per device for work that can overlap the
+// main stream (created once, never destroyed).
+cudaStream_t side_stream(int dev) {
+    static std::mutex mu;
+    static std::map<int, cudaStream_t> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    cudaStream_t st = nullptr;
+    RNLA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cache[dev] = st;
+    return st;
+}
+
+// `to` waits for the work enqueued on `from` so far.
+void stream_wait(cudaStream_t to, cudaStream_t from) {
+    cudaEvent_t ev;
+    RNLA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    RNLA_CUDA(cudaEventRecord(ev, from));
+    RNLA_CUDA(cudaStreamWaitEvent(to, ev, 0));
+    RNLA_CUDA(cudaEventDestroy(ev));
+}
+
 Ctx::Ctx(cudaStream_t s) : stream(s) {
     RNLA_CUDA(cudaGetDevice(&device));
     sm_count = sm_count_of(device);

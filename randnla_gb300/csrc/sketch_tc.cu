@@ -505,11 +505,15 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * (YD_BYTES / 2), ctx.stream);
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
+    // the sketch generator (integer ALU bound) runs on the side stream while
+    // the main stream makes the digit planes (HBM bound)
+    const cudaStream_t side = side_stream(ctx.device);
+    stream_wait(side, ctx.stream);                 // the S buffer exists
     {
         int gx = div_up((int64_t)Ks * 1024, 256);
         const int cap = 16 * sm / (tiles_m < 16 ? tiles_m : 16) + 1;
         if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, ctx.stream>>>(key, M, K, Ks, sk);
+        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, M, K, Ks, sk);
         RNLA_LAUNCH_CHECK();
     }
     if (y_f32) colexp_kernel<float><<<(unsigned)N, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, E);
@@ -525,6 +529,7 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
             slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, tiles_n, dig);
         RNLA_LAUNCH_CHECK();
     }
+    stream_wait(ctx.stream, side);                 // S is written
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
