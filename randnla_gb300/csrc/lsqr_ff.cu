@@ -49,10 +49,12 @@
 namespace rnla {
 namespace lsff {
 
-constexpr int T = 512;          // threads per CTA
+constexpr int T = 512;          // threads per CTA (split roles)
 constexpr int W = T / 32;       // warps per CTA
 constexpr int WA = 8;           // row warps (0..7); warps 8..15 are column warps
 constexpr int TB = T - 32 * WA; // column threads
+constexpr int TF = 256;         // threads per CTA (fused roles)
+constexpr int WF = TF / 32;
 constexpr int MAX_ST = 6;       // ring stages
 constexpr size_t RING_BYTES = 192 * 1024;
 constexpr int64_t MAX_N = 1024;
@@ -110,6 +112,11 @@ struct Ring {
     int ist;                    // issuer: next stage to fill
     int64_t ik;                 // issuer: next tile index (0..ntl-1)
     int inflight;               // issuer: issued and not yet consumed
+    // fused roles: per-stage release counters and the number of copies
+    // issued so far (shared memory); tiles consumed so far (every thread)
+    unsigned int* rel;
+    unsigned long long* issued;
+    unsigned long long consumed;
 };
 
 constexpr int ISSUER = 32 * WA;  // first column thread issues the bulk copies
@@ -134,6 +141,52 @@ __device__ __forceinline__ void ring_issue(const Args& a, Ring& rg) {
 
 __device__ __forceinline__ void ring_advance(const Args& a, Ring& rg) {
     if (++rg.cst == a.ST) { rg.cst = 0; rg.cph ^= 1u; }
+    ++rg.consumed;
+}
+
+// One bulk copy of this CTA's tile `ik` into stage `st`.
+__device__ __forceinline__ void ring_copy(const Args& a, const Ring& rg, int st, int64_t ik) {
+    const int64_t t = (int64_t)blockIdx.x + ik * (int64_t)gridDim.x;
+    const int64_t r0 = t * a.R;
+    const int64_t rows = min((int64_t)a.R, a.m - r0);
+    const uint32_t bytes = (uint32_t)(rows * a.ldf * 8);
+    mbar_expect_tx(&rg.full[st], bytes);
+    bulk_g2s(rg.tiles + (size_t)st * a.R * a.hp, a.AF + r0 * a.ldf, bytes, &rg.full[st]);
+}
+
+// Fused roles: the stage a warp has just read into registers is released
+// by lane 0; the last of the WF warps refills it with the tile ST places
+// further along this CTA's (cyclic) tile list.  Every thread tracks that
+// tile index in rg.ik.  Stages are released in order because every warp
+// reads the tiles in order.
+__device__ __forceinline__ void ring_release(const Args& a, Ring& rg, int st, int lane, volatile int* err) {
+    __syncwarp();
+    if (lane == 0) {
+        __threadfence_block();
+        if (atomicAdd(&rg.rel[st], 1u) == (unsigned)(WF - 1)) {
+            rg.rel[st] = 0;
+            if (*err == 0) {
+                __threadfence_block();
+                fence_proxy_async();
+                ring_copy(a, rg, st, rg.ik);
+                atomicAdd(rg.issued, 1ull);
+            }
+        }
+    }
+    rg.ik = (rg.ik + 1 == rg.ntl) ? 0 : rg.ik + 1;
+}
+
+// Fused roles, thread 0: wait (bounded) for every copy still in flight.
+__device__ void ring_drain_fused(const Args& a, Ring& rg) {
+    if (threadIdx.x != 0) return;
+    volatile int quiet = 0;
+    int st = rg.cst;
+    uint32_t ph = rg.cph;
+    const unsigned long long out = *rg.issued - rg.consumed;
+    for (unsigned long long c = 0; c < out; ++c) {
+        mbar_wait(&rg.full[st], ph, &quiet);
+        if (++st == a.ST) { st = 0; ph ^= 1u; }
+    }
 }
 
 // Issuing thread: wait (bounded) until every copy still in flight has
@@ -373,6 +426,193 @@ __device__ bool ff_pass(const Args& a, Ring& rg, ulonglong2* usm, float2 c1, flo
     return *err == 0;
 }
 
+// The same pass with fused roles (TF threads): each warp takes RW rows of
+// every tile, loads their chunks into registers and releases the stage at
+// once, forms the RW row dots (packed float-float, warp reduce-scatter), the
+// owner lane of each row forms u_r, and after a broadcast every lane adds
+// u_r times its chunks to its own A^T u accumulators (KP column pairs).  The
+// WF per-warp accumulators are summed in warp order at the end of the pass
+// through `scratch` (WF x hp float4).
+template <int KP, int RW>
+__device__ bool ff_pass_fused(const Args& a, Ring& rg, float4* scratch, float2 c1, float2 c2, float2 c3,
+                              bool dot, const float2* oldv, const float2* bvec, float2* dst, bool want_b2,
+                              bool acc_at, volatile int* err) {
+    constexpr int R = WF * RW;
+    __shared__ float2 wred[WF][2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int hp = (int)a.hp;
+    const int64_t ntl = rg.ntl;
+    f32x2 yh[KP], nyh[KP], yl[KP];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) {
+        const int p = lane + 32 * k;
+        float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
+        if (dot && p < hp) { y0 = a.yF[2 * p]; y1 = a.yF[2 * p + 1]; }
+        yh[k] = pk2(y0.x, y1.x);
+        nyh[k] = pk2(-y0.x, -y1.x);
+        yl[k] = pk2(y0.y, y1.y);
+    }
+    f32x2 ah[KP], al[KP];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) { ah[k] = 0ull; al[k] = 0ull; }
+    float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
+    // after the reduce-scatter lane l holds the dot of row slot l >> SHL; the
+    // first lane of each group (owner) forms that row's u
+    constexpr int SHL = (RW == 1) ? 5 : (RW == 2) ? 4 : (RW == 4) ? 3 : 2;
+    const bool owner = (lane & ((1 << SHL) - 1)) == 0;
+    const int rw = lane >> SHL;
+    auto row_of = [&](int64_t kk) { return ((int64_t)blockIdx.x + kk * (int64_t)gridDim.x) * R + warp + WF * rw; };
+    auto fetch = [&](int64_t kk, float2& u, float2& bv) {
+        u = make_float2(0.f, 0.f);
+        bv = make_float2(0.f, 0.f);
+        if (owner && kk < ntl) {
+            const int64_t i = row_of(kk);
+            if (i < a.m) {
+                if (oldv) u = oldv[i];
+                if (bvec) bv = bvec[i];
+            }
+        }
+    };
+    float2 qu0, qb0, qu1, qb1;
+    fetch(0, qu0, qb0);
+    fetch(1, qu1, qb1);
+#pragma unroll 1
+    for (int64_t k = 0; k < ntl; ++k) {
+        const float2 uo = qu0, bb = qb0;
+        qu0 = qu1;
+        qb0 = qb1;
+        fetch(k + 2, qu1, qb1);
+        const int st = rg.cst;
+        const bool ok = mbar_wait(&rg.full[st], rg.cph, err);
+        ring_advance(a, rg);
+        const int64_t r0 = ((int64_t)blockIdx.x + k * (int64_t)gridDim.x) * R;
+        const int rows = (int)min((int64_t)R, a.m - r0);
+        const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hp;
+        ulonglong2 v[RW][KP];
+#pragma unroll
+        for (int w = 0; w < RW; ++w) {
+            const int r = warp + WF * w;
+            const bool rv = ok && r < rows;
+#pragma unroll
+            for (int kk = 0; kk < KP; ++kk) {
+                const int p = lane + 32 * kk;
+                v[w][kk] = (rv && p < hp) ? tile[(size_t)r * hp + p] : make_ulonglong2(0ull, 0ull);
+            }
+        }
+        ring_release(a, rg, st, lane, err);
+        float tvh[RW], tvl[RW];
+#pragma unroll
+        for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
+        if (dot) {
+            f32x2 sh[RW][2], sl[RW][2];
+#pragma unroll
+            for (int w = 0; w < RW; ++w) { sh[w][0] = sh[w][1] = sl[w][0] = sl[w][1] = 0ull; }
+#pragma unroll
+            for (int kk = 0; kk < KP; ++kk) {
+#pragma unroll
+                for (int w = 0; w < RW; ++w)
+                    ff2_madd(v[w][kk].x, v[w][kk].y, yh[kk], nyh[kk], yl[kk], sh[w][kk & 1], sl[w][kk & 1]);
+            }
+#pragma unroll
+            for (int w = 0; w < RW; ++w) {
+                ff2_acc(sh[w][0], sl[w][0], sh[w][1], sl[w][1]);
+                const float2 H = upk2(sh[w][0]), L = upk2(sl[w][0]);
+                float h = H.x, l = L.x;
+                ff_acc(h, l, H.y, L.y);
+                tvh[w] = h;
+                tvl[w] = l;
+            }
+            int off = 16;
+#pragma unroll
+            for (int half = RW / 2; half >= 1; half /= 2) {
+                const bool up = (lane & off) != 0;
+#pragma unroll
+                for (int k2 = 0; k2 < half; ++k2) {
+                    const float sh_ = up ? tvh[k2] : tvh[k2 + half], sl_ = up ? tvl[k2] : tvl[k2 + half];
+                    float kh = up ? tvh[k2 + half] : tvh[k2], kl = up ? tvl[k2 + half] : tvl[k2];
+                    const float rh = __shfl_xor_sync(0xffffffffu, sh_, off);
+                    const float rl = __shfl_xor_sync(0xffffffffu, sl_, off);
+                    ff_acc(kh, kl, rh, rl);
+                    tvh[k2] = kh;
+                    tvl[k2] = kl;
+                }
+                off >>= 1;
+            }
+            for (; off >= 1; off >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, tvh[0], off);
+                const float ol = __shfl_xor_sync(0xffffffffu, tvl[0], off);
+                ff_acc(tvh[0], tvl[0], oh, ol);
+            }
+        }
+        float2 nv = make_float2(0.f, 0.f);
+        if (owner) {
+            const float2 tv = ff_norm(tvh[0], tvl[0]);
+            nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
+            const int r = warp + WF * rw;
+            if (ok && r < rows) {
+                dst[r0 + r] = nv;
+                ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
+                if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
+            }
+        }
+        if (acc_at) {
+            f32x2 uh[RW], nuh[RW], ul[RW];
+#pragma unroll
+            for (int w = 0; w < RW; ++w) {
+                const float x = __shfl_sync(0xffffffffu, nv.x, w << SHL);
+                const float y = __shfl_sync(0xffffffffu, nv.y, w << SHL);
+                uh[w] = pk2(x, x);
+                nuh[w] = pk2(-x, -x);
+                ul[w] = pk2(y, y);
+            }
+#pragma unroll
+            for (int kk = 0; kk < KP; ++kk) {
+#pragma unroll
+                for (int w = 0; w < RW; ++w) ff2_madd(v[w][kk].x, v[w][kk].y, uh[w], nuh[w], ul[w], ah[kk], al[kk]);
+            }
+        }
+    }
+    const float2 sq = ff_warp_sum(sqh, sql);
+    const float2 b2 = ff_warp_sum(b2h, b2l);
+    if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
+    if (acc_at) {
+#pragma unroll
+        for (int kk = 0; kk < KP; ++kk) {
+            const int p = lane + 32 * kk;
+            if (p < hp) {
+                const float2 H = upk2(ah[kk]), L = upk2(al[kk]);
+                scratch[(size_t)warp * hp + p] = make_float4(H.x, L.x, H.y, L.y);
+            }
+        }
+    }
+    __syncthreads();
+    if (acc_at) {
+        float4* P4 = reinterpret_cast<float4*>(a.partF) + (size_t)blockIdx.x * hp;
+        for (int p = tid; p < hp; p += TF) {
+            float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+#pragma unroll
+            for (int w = 0; w < WF; ++w) {
+                const float4 q = scratch[(size_t)w * hp + p];
+                ff_acc(h0, l0, q.x, q.y);
+                ff_acc(h1, l1, q.z, q.w);
+            }
+            const float2 c0 = ff_norm(h0, l0), c1v = ff_norm(h1, l1);
+            P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
+        }
+    }
+    if (tid == 0) {
+        float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
+        for (int w = 0; w < WF; ++w) {
+            ff_acc(h, l, wred[w][0].x, wred[w][0].y);
+            ff_acc(h2, l2, wred[w][1].x, wred[w][1].y);
+        }
+        a.spF[blockIdx.x * 4 + 0] = ff_norm(h, l);
+        a.spF[blockIdx.x * 4 + 3] = ff_norm(h2, l2);
+    }
+    __syncthreads();
+    return *err == 0;
+}
+
 // Sum over CTAs of scalar slot `slot` (warp-level, identical in every CTA).
 __device__ __forceinline__ float2 sum_slot(const Args& a, int slot, int lane) {
     float h = 0.f, l = 0.f;
@@ -383,10 +623,10 @@ __device__ __forceinline__ float2 sum_slot(const Args& a, int slot, int lane) {
     return ff_warp_sum(h, l);
 }
 
-// g_j = sum over CTAs of partF[c][j]; one warp per column, warps 1..W-1.
-__device__ void reduce_columns(const Args& a, int warp, int lane) {
-    const int64_t nw = (int64_t)gridDim.x * (W - 1);
-    for (int64_t j = (int64_t)blockIdx.x * (W - 1) + (warp - 1); j < a.n; j += nw) {
+// g_j = sum over CTAs of partF[c][j]; one warp per column, warps 1..nwc-1.
+__device__ void reduce_columns(const Args& a, int warp, int lane, int nwc) {
+    const int64_t nw = (int64_t)gridDim.x * (nwc - 1);
+    for (int64_t j = (int64_t)blockIdx.x * (nwc - 1) + (warp - 1); j < a.n; j += nw) {
         float h = 0.f, l = 0.f;
         for (int64_t c = lane; c < gridDim.x; c += 32) {
             const float2 v = a.partF[c * a.ldf + j];
@@ -399,10 +639,10 @@ __device__ void reduce_columns(const Args& a, int warp, int lane) {
 
 // vun_j = (M^T g)_j ib - [sub] beta v_j, and the squares of vun_j and w_j;
 // one warp per column, all warps.
-__device__ void update_vun(const Args& a, const Bcast& bc, bool sub, int warp, int lane) {
+__device__ void update_vun(const Args& a, const Bcast& bc, bool sub, int warp, int lane, int nwc) {
     const int64_t n = a.n;
-    const int64_t nw = (int64_t)gridDim.x * W;
-    for (int64_t j = (int64_t)blockIdx.x * W + warp; j < n; j += nw) {
+    const int64_t nw = (int64_t)gridDim.x * nwc;
+    for (int64_t j = (int64_t)blockIdx.x * nwc + warp; j < n; j += nw) {
         float2 z;
         if (a.MF) {
             float h = 0.f, l = 0.f;
@@ -441,12 +681,12 @@ __device__ __forceinline__ void sum_colsq(const Args& a, int lane, float2& s1, f
     s2 = ff_warp_sum(h2, l2);
 }
 
-// Raw rows of M src (src float-float, n): warps 1..W-1, one warp per row;
+// Raw rows of M src (src float-float, n): warps 1..nwc-1, one warp per row;
 // the raw value goes to dst[i] and is rescaled by the same lane later.
-__device__ void trmv_rows_raw(const Args& a, const float2* src, float2* dst, int warp, int lane) {
+__device__ void trmv_rows_raw(const Args& a, const float2* src, float2* dst, int warp, int lane, int nwc) {
     const int64_t n = a.n;
-    const int64_t nw = (int64_t)gridDim.x * (W - 1);
-    for (int64_t i = (int64_t)blockIdx.x * (W - 1) + (warp - 1); i < n; i += nw) {
+    const int64_t nw = (int64_t)gridDim.x * (nwc - 1);
+    for (int64_t i = (int64_t)blockIdx.x * (nwc - 1) + (warp - 1); i < n; i += nw) {
         float2 s;
         if (a.MtF) {
             float h = 0.f, l = 0.f;
@@ -463,10 +703,10 @@ __device__ void trmv_rows_raw(const Args& a, const float2* src, float2* dst, int
     }
 }
 
-__device__ void scale_rows(const Args& a, float2* dst, float2 sc, int warp, int lane) {
-    const int64_t nw = (int64_t)gridDim.x * (W - 1);
+__device__ void scale_rows(const Args& a, float2* dst, float2 sc, int warp, int lane, int nwc) {
+    const int64_t nw = (int64_t)gridDim.x * (nwc - 1);
     if (lane != 0) return;
-    for (int64_t i = (int64_t)blockIdx.x * (W - 1) + (warp - 1); i < a.n; i += nw) dst[i] = ff_mul(dst[i], sc);
+    for (int64_t i = (int64_t)blockIdx.x * (nwc - 1) + (warp - 1); i < a.n; i += nw) dst[i] = ff_mul(dst[i], sc);
 }
 
 __device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
@@ -477,10 +717,16 @@ __device__ __forceinline__ double lane_rsqrt(double arg) { return arg > 0.0 ? rs
 
 __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-template <int KP, int RW>
-__global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
+// FUSED selects the pass: fused roles on TF threads, or split row/column
+// roles on T threads.
+template <int KP, int RW, bool FUSED>
+__global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
+    constexpr int NT = FUSED ? TF : T;
+    constexpr int NWC = NT / 32;
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t full[MAX_ST];
+    __shared__ unsigned int rel[MAX_ST];
+    __shared__ unsigned long long issued;
     __shared__ Bcast bc;
     __shared__ Scal sc;
     __shared__ int err_s;
@@ -489,7 +735,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     const int64_t G = gridDim.x;
     const double eps = 2.220446049250313e-16;
     const double dampsq = a.damp * a.damp;
-    const int XW = T - 32;                 // threads of warps 1..W-1 (elementwise work)
+    const int XW = NT - 32;                // threads of warps 1.. (elementwise work)
 
     Ring rg;
     rg.full = full;
@@ -500,34 +746,70 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
     rg.ist = 0;
     rg.ik = 0;
     rg.inflight = 0;
-    ulonglong2* usm = reinterpret_cast<ulonglong2*>(dsm + (size_t)a.ST * a.R * a.ldf * 8);
+    rg.rel = rel;
+    rg.issued = &issued;
+    rg.consumed = 0;
+    // split roles: the u hand-off buffers; fused roles: the column scratch
+    unsigned char* extra = dsm + (size_t)a.ST * a.R * a.ldf * 8;
+    ulonglong2* usm = reinterpret_cast<ulonglong2*>(extra);
+    float4* scratch = reinterpret_cast<float4*>(extra);
     volatile int* err = &err_s;
     if (tid == 0) {
         err_s = 0;
-        for (int s = 0; s < a.ST; ++s) mbar_init(&full[s], 1);
+        issued = 0;
+        for (int s = 0; s < a.ST; ++s) {
+            mbar_init(&full[s], 1);
+            rel[s] = 0;
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == ISSUER) ring_issue(a, rg);
+    if (FUSED) {
+        if (rg.ntl > 0) {
+            if (tid == 0) {
+                int64_t ik = 0;
+                for (int s = 0; s < a.ST; ++s) {
+                    ring_copy(a, rg, s, ik);
+                    ik = (ik + 1 == rg.ntl) ? 0 : ik + 1;
+                }
+                issued = (unsigned long long)a.ST;
+            }
+            rg.ik = a.ST % rg.ntl;
+        }
+    } else if (tid == ISSUER) {
+        ring_issue(a, rg);
+    }
 
+#define LSFF_DRAIN()                                   \
+    do {                                               \
+        if (FUSED) {                                   \
+            __syncthreads();                           \
+            ring_drain_fused(a, rg);                   \
+        } else {                                       \
+            ring_drain(a, rg);                         \
+        }                                              \
+    } while (0)
 #define LSFF_SYNC()                    \
     do {                               \
         if (!grid_sync(a.bar)) {       \
-            ring_drain(a, rg);         \
+            LSFF_DRAIN();              \
             return;                    \
         }                              \
     } while (0)
-#define LSFF_PASS(...)                                             \
-    do {                                                           \
-        if (!ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err)) {      \
-            set_status(a, KSTATUS_BARRIER_TIMEOUT);                \
-            ring_drain(a, rg);                                     \
-            return;                                                \
-        }                                                          \
+#define LSFF_PASS(...)                                                                 \
+    do {                                                                               \
+        bool pass_ok;                                                                  \
+        if constexpr (FUSED) pass_ok = ff_pass_fused<KP, RW>(a, rg, scratch, __VA_ARGS__, err); \
+        else pass_ok = ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err);                  \
+        if (!pass_ok) {                                                                \
+            set_status(a, KSTATUS_BARRIER_TIMEOUT);                                    \
+            LSFF_DRAIN();                                                              \
+            return;                                                                    \
+        }                                                                              \
     } while (0)
 
-    const int64_t gt = (int64_t)blockIdx.x * T + tid;
-    const int64_t gthreads = G * T;
+    const int64_t gt = (int64_t)blockIdx.x * NT + tid;
+    const int64_t gthreads = G * NT;
     const float2 zero2 = make_float2(0.f, 0.f), one2 = make_float2(1.f, 0.f), mone2 = make_float2(-1.f, 0.f);
 
     // ---- initialisation (solvers.rs:141-182) ----
@@ -538,7 +820,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
         if (a.calc_var) a.varF[j] = zero2;
     }
     if (a.x0F) {
-        if (warp > 0) trmv_rows_raw(a, a.x0F, a.yF, warp, lane);
+        if (warp > 0) trmv_rows_raw(a, a.x0F, a.yF, warp, lane, NWC);
         LSFF_SYNC();
     }
     // u = b - A M x0 (or b); beta^2, ||b||^2, A^T u partials
@@ -560,10 +842,10 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             bc.beta = ff_split(sc.beta);
         }
     } else {
-        reduce_columns(a, warp, lane);
+        reduce_columns(a, warp, lane, NWC);
     }
     LSFF_SYNC();
-    update_vun(a, bc, false, warp, lane);
+    update_vun(a, bc, false, warp, lane, NWC);
     LSFF_SYNC();
     if (warp == 0) {
         float2 A2, W2;
@@ -575,11 +857,11 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             bc.ia = ff_split(ia);
         }
     } else {
-        trmv_rows_raw(a, a.vunF, a.yF, warp, lane);
+        trmv_rows_raw(a, a.vunF, a.yF, warp, lane, NWC);
     }
     __syncthreads();
     if (warp > 0) {
-        scale_rows(a, a.yF, bc.ia, warp, lane);
+        scale_rows(a, a.yF, bc.ia, warp, lane, NWC);
         for (int64_t j = (int64_t)blockIdx.x * XW + (tid - 32); j < n; j += G * XW) {
             const float2 vv = ff_mul(a.vunF[j], bc.ia);
             a.vF[j] = vv;
@@ -605,7 +887,7 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
             a.x[j] = ff_to_double(a.xF[j]);
             if (a.calc_var && a.var) a.var[j] = 0.0;
         }
-        ring_drain(a, rg);
+        LSFF_DRAIN();
         return;
     }
     const double ctol = a.conlim > 0.0 ? 1.0 / a.conlim : 0.0;
@@ -668,11 +950,11 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
                 bc.irho = ff_split(irho);
             }
         } else {
-            reduce_columns(a, warp, lane);
+            reduce_columns(a, warp, lane, NWC);
         }
         LSFF_SYNC();
         // v = M^T A^T u / beta - beta v  (solvers.rs:197-204)
-        if (bc.beta_pos) update_vun(a, bc, true, warp, lane);
+        if (bc.beta_pos) update_vun(a, bc, true, warp, lane, NWC);
         else {
             // keep v; ||w||^2 is still needed
             for (int64_t j = gt; j < n; j += gthreads) {
@@ -705,12 +987,12 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
                 bc.c2 = ff_split(-alfa * sc.us);
             }
         } else if (bp) {
-            trmv_rows_raw(a, a.vunF, a.yF, warp, lane);
+            trmv_rows_raw(a, a.vunF, a.yF, warp, lane, NWC);
         }
         __syncthreads();
         if (warp > 0) {
             // x += t1 w ; w = v + t2 w ; var += (w / rho)^2 ; y = M v  (solvers.rs:222-232)
-            if (bp) scale_rows(a, a.yF, bc.ia, warp, lane);
+            if (bp) scale_rows(a, a.yF, bc.ia, warp, lane, NWC);
             const float2 t1 = bc.t1, t2 = bc.t2, ia = bc.ia, ir = bc.irho;
             for (int64_t j = (int64_t)blockIdx.x * XW + (tid - 32); j < n; j += G * XW) {
                 const float2 vv = bp ? ff_mul(a.vunF[j], ia) : a.vF[j];
@@ -791,7 +1073,8 @@ __global__ void __launch_bounds__(T, 1) lsqr_ff_kernel(Args a) {
         a.out[0] = sc.istop; a.out[1] = (double)itn; a.out[2] = sc.r1norm; a.out[3] = sc.r2norm;
         a.out[4] = sc.anorm; a.out[5] = sc.acond; a.out[6] = sc.xnorm; a.out[7] = sc.arnorm;
     }
-    ring_drain(a, rg);
+    LSFF_DRAIN();
+#undef LSFF_DRAIN
 #undef LSFF_SYNC
 #undef LSFF_PASS
 }
@@ -838,18 +1121,25 @@ __global__ void msplit_kernel(const double* __restrict__ M, int64_t n, int64_t l
     }
 }
 
-template <int KP, int RW>
-static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW>; }
+template <int KP, int RW, bool FUSED>
+static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW, FUSED>; }
 
-// (kernel, rows per row-warp) for hp column pairs: the y registers cover hp,
-// and a tile (8 RW rows) is at most 64 KB, so the ring holds 3 or more tiles.
-static const void* pick_kernel(int64_t hp, int& RW) {
-    if (hp <= 32) { RW = 4; return kernel_kp<1, 4>(); }
-    if (hp <= 64) { RW = 4; return kernel_kp<2, 4>(); }
-    if (hp <= 128) { RW = 4; return kernel_kp<4, 4>(); }
-    if (hp <= 256) { RW = 2; return kernel_kp<8, 2>(); }
-    RW = 1;
-    return kernel_kp<16, 1>();
+// Kernel for hp column pairs: the y registers cover hp (KP chunks of 32
+// pairs per lane) and a tile (R rows) is at most 64 KB, so the ring holds 3
+// or more tiles.  Up to 256 pairs the fused roles (registers hold y, the A^T u
+// accumulators and RW rows of chunks: RW KP <= 16); above, the split roles.
+struct KernelPick {
+    const void* fn;
+    int R;          // rows per tile
+    int threads;
+    bool fused;
+};
+static KernelPick pick_kernel(int64_t hp) {
+    if (hp <= 32) return {kernel_kp<1, 8, true>(), WF * 8, TF, true};
+    if (hp <= 64) return {kernel_kp<2, 8, true>(), WF * 8, TF, true};
+    if (hp <= 128) return {kernel_kp<4, 4, true>(), WF * 4, TF, true};
+    if (hp <= 256) return {kernel_kp<8, 2, true>(), WF * 2, TF, true};
+    return {kernel_kp<16, 1, false>(), WA * 1, T, false};
 }
 
 }  // namespace lsff
@@ -894,17 +1184,19 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     cudaStream_t st = ctx.stream;
     const int64_t ldf = (n + 1) & ~1LL;
     const int64_t hp = ldf / 2;
-    int RW = 1;
-    const void* k = pick_kernel(hp, RW);
-    const int R = WA * RW;
+    const KernelPick kp = pick_kernel(hp);
+    const void* k = kp.fn;
+    const int R = kp.R;
     const size_t stage = (size_t)R * ldf * 8;
     int STn = (int)(RING_BYTES / stage);
     STn = STn > MAX_ST ? MAX_ST : STn;
     if (STn < 3) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): tile ring does not fit");
-    const size_t smem = (size_t)STn * stage + (size_t)2 * R * 16;
+    // fused: per-warp column scratch; split: the two u hand-off buffers
+    const size_t extra = kp.fused ? (size_t)WF * hp * 16 : (size_t)2 * R * 16;
+    const size_t smem = (size_t)STn * stage + extra;
     RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
-    RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, T, smem));
+    RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, kp.threads, smem));
     if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): kernel does not fit on an SM");
     const int G = ctx.sm_count;
 
@@ -969,7 +1261,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaEventCreate(&ev[0]));
     RNLA_CUDA(cudaEventCreate(&ev[1]));
     RNLA_CUDA(cudaEventRecord(ev[0], st));
-    RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(T), params, smem, st));
+    RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(kp.threads), params, smem, st));
     count_launch();
     RNLA_CUDA(cudaEventRecord(ev[1], st));
     double h[8];

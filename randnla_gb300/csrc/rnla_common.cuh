@@ -170,34 +170,51 @@ struct GridBarrier {
     unsigned int* status;
 };
 
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int atom_add_acqrel_gpu(unsigned int* p, unsigned int v) {
+    unsigned int old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned int* p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One thread per CTA arrives with a release-acquire atomic (after the CTA's
+// __syncthreads, so it publishes the whole CTA's writes); the last arriver
+// resets the count and publishes the next generation with a release store;
+// the others poll the generation with acquire loads.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned long long limit_ns = 2000000000ull) {
     __syncthreads();
     __shared__ int ok_s;
     if (threadIdx.x == 0) {
         ok_s = 1;
         const unsigned int nblocks = gridDim.x * gridDim.y * gridDim.z;
-        volatile unsigned int* vgen = b.gen;
-        const unsigned int my_gen = *vgen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(b.count, 1u);
+        const unsigned int my_gen = ld_acquire_gpu(b.gen);
+        const unsigned int arrived = atom_add_acqrel_gpu(b.count, 1u);
         if (arrived == nblocks - 1) {
             *b.count = 0;
-            __threadfence();
-            atomicAdd(b.gen, 1u);
+            st_release_gpu(b.gen, my_gen + 1u);
         } else {
-            const unsigned long long t0 = globaltimer_ns();
+            unsigned long long t0 = 0;
             unsigned int spins = 0;
-            while (*vgen == my_gen) {
-                if (*((volatile unsigned int*)b.status) != 0u) { ok_s = 0; break; }
-                if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > limit_ns) {
-                    atomicCAS(b.status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
-                    ok_s = 0;
-                    break;
+            while (ld_acquire_gpu(b.gen) == my_gen) {
+                if ((++spins & 31u) == 0u) {
+                    if (*((volatile unsigned int*)b.status) != 0u) { ok_s = 0; break; }
+                    const unsigned long long now = globaltimer_ns();
+                    if (t0 == 0) t0 = now;
+                    else if (now - t0 > limit_ns) {
+                        atomicCAS(b.status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+                        ok_s = 0;
+                        break;
+                    }
                 }
-                __nanosleep(64);
             }
         }
-        __threadfence();
     }
     __syncthreads();
     return ok_s != 0;
