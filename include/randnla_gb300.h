@@ -136,7 +136,7 @@ typedef struct {
     double atol;              /* LSQR atol/btol for blendenpik with RNLA_SOLVER_LSQR; */
     double btol;              /*   0 means: stop when ||(A M)^T r|| < epsilon, as CGLS does */
     double conlim;            /* LSQR conlim (0 -> 1e8) */
-    int32_t digits_a;         /* bf16 digits of the data matrix for RNLA_PREC_BF16X (0 = auto) */
+    int32_t digits_a;         /* 8-bit bf16 digits of the data matrix for RNLA_PREC_BF16X, 1..4 (0 = auto: 4) */
     int32_t digits_b;         /* bf16 digits of the second operand when it is a matrix (0 = auto) */
     int32_t orth;             /* 0 = CholeskyQR2 with Householder fallback, 1 = Householder */
     int32_t reserved;
@@ -301,8 +301,8 @@ RNLA_API int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_
 /* Y (ldy) = S X: the sketch S (d x m, Gaussian, generator rng) applied to
  * X (m x n, ldx) without materialising S.  precision RNLA_PREC_BF16X uses
  * the tensor-core digit-sliced kernel with the quantised Gaussian
- * (rnla_sketching_operator_f32_dev with quantized = 1); digits = bf16
- * digits of X (0 = auto).  x_is_f32 selects float or double X. */
+ * (rnla_sketching_operator_f32_dev with quantized = 1); digits = 8-bit
+ * bf16 digits of X, 1..4 (0 = auto: 4).  x_is_f32 selects float or double X. */
 RNLA_API int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
                           int64_t d, const rnla_rng* rng, int32_t precision, int32_t digits,
                           double* y_dev, int64_t ldy, void* stream);

@@ -6,19 +6,20 @@
 //   FP32 matrix, K = rows of the data (the sketch_and_precondition.rs:51-52
 //   products S a and S b, and A Omega of the range finder).
 //
-// Exactness.  Y is cut into P bf16 "digits" per element: with E_j the
-// exponent of the largest |Y[:, j]| (|y| < 2^E_j), T = round(|y| 2^(7P-E_j))
-// < 2^(7P)+1 is split into base-128 digits d_1..d_P (d_1 <= 128), each
-// carrying the sign of y.  A digit times a sketch entry is an integer of
-// magnitude <= 63*128 < 2^13, so the FP32 tensor-core accumulation of 2048
-// consecutive K (one "window") is an integer below 2^24: exact.  After each
-// window the drain warps read the P accumulators from TMEM and fold
-// D_1 2^(7(P-1)) + ... + D_P exactly into the CTA's int64 partial tile
-// (|window| < 2^52.01; at most 2000 windows per CTA keep the sum below
-// 2^63).  The split-K partials are added in a fixed order (in int64 when all
-// windows together fit) and scaled once by 2^(E_j - 7P - 3).  The only
-// roundings are the digit truncation (|error| <= 2^(E_j - 7P - 1) per entry
-// of Y) and the final conversion to FP64; S is applied exactly.
+// Exactness.  Y is cut into P <= 4 bf16 "digits" per element: with E_j the
+// exponent of the largest |Y[:, j]| (|y| < 2^E_j), T = round(|y| 2^(8P-E_j))
+// <= 2^(8P) is split into base-256 digits d_1..d_P (d_1 <= 256), each
+// carrying the sign of y (an integer of at most 8 significant bits: exact in
+// bf16).  A digit times a sketch entry is an integer of magnitude
+// <= 256*63 < 2^14, so the FP32 tensor-core accumulation of 1024 consecutive
+// K (one "window") is an integer below 2^24: exact.  After each window the
+// drain warps read the P accumulators from TMEM and fold
+// D_1 2^(8(P-1)) + ... + D_P exactly into int64 accumulators held in their
+// registers (|window| < 2^48.01); a work unit ends with one store of its
+// int64 tile.  The split-K partials are added in a fixed order (in int64
+// when all windows together fit) and scaled once by 2^(E_j - 8P - 3).  The
+// only roundings are the digit truncation (|error| <= 2^(E_j - 8P - 1) per
+// entry of Y) and the final conversion to FP64; S is applied exactly.
 //
 // Pipeline.
 //   sketch_gen_kernel  writes S once as bf16 tile images [m tile][K stage]
@@ -27,15 +28,19 @@
 //                      instead of generating S inside the GEMM;
 //   slice_kernel       writes the digit planes of Y as tile images
 //                      [n tile][K stage][digit] (64 x 64 bf16, 8 KB);
-//   sketch_mma_kernel  one CTA per (m tile, n tile, K chunk), 192 threads:
-//                      warp 0 streams the S tile and the P digit tiles of each
-//                      stage with cp.async.bulk into a 4-stage mbarrier ring;
+//   sketch_mma_kernel  persistent: one CTA per SM walks the work units
+//                      (m tile, n tile, K chunk) u = blockIdx.x, + gridDim.x,
+//                      ...; 192 threads: warp 0 streams the S tile and the P
+//                      digit tiles of each stage with cp.async.bulk into a
+//                      4-stage mbarrier ring that runs on across units;
 //                      warp 1 allocates TMEM and issues tcgen05.mma
 //                      (M = 128, N = 64, K = 16, bf16 x bf16 -> f32, one
-//                      accumulator per digit) from one lane; warps 2-5 drain
-//                      TMEM after each window.  CTAs that share an S tile are
-//                      adjacent in launch order, so S is read from HBM about
-//                      once and served from L2 to the other column tiles;
+//                      accumulator per digit, two accumulator sets so the
+//                      MMAs of a window overlap the drain of the previous
+//                      one) from one lane; warps 2-5 drain TMEM after each
+//                      window.  Units that share an S tile are adjacent in
+//                      the walk, so S is read from HBM about once and served
+//                      from L2 to the other column tiles;
 //   splitk_sum_kernel  adds the K chunks and scales.
 //
 // Every mbarrier wait is bounded (2 s of globaltimer); on timeout the CTA
@@ -53,7 +58,9 @@ namespace tc {
 constexpr int BM = 128;           // sketch rows per CTA tile (TMEM lanes)
 constexpr int BN = 64;            // data columns per CTA tile
 constexpr int BK = 64;            // K per pipeline stage (one 128-byte bf16 row)
-constexpr int WIN = 32;           // stages per exact window (2048 K values)
+constexpr int WIN = 16;           // stages per exact window (1024 K values)
+constexpr int MAXP = 4;           // digits
+constexpr int ACC_COLS = MAXP * BN;                  // TMEM columns of one accumulator set
 constexpr int STAGES = 4;
 constexpr int DRAIN_WARPS = 4;
 constexpr int THREADS = 64 + 32 * DRAIN_WARPS;       // loader warp + MMA warp + drain warps
@@ -114,9 +121,16 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
+// acc += (integer value of the FP32 word f) * 2^sh, exact in int64 (sh < 31)
+__device__ __forceinline__ void acc_digit(long long& acc, uint32_t f, int sh) {
+    const int d = __float2int_rn(__uint_as_float(f));
+    asm("mad.wide.s32 %0, %1, %2, %0;" : "+l"(acc) : "r"(d), "r"(1 << sh));
+}
+
 struct Params {
     int64_t M, N, K;          // C is M x N, reduction length K
     int tiles_m, tiles_n, Ks, kc_count, stages_per_kc;
+    int units;                // tiles_m * tiles_n * kc_count
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
     const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
     long long* partial;       // [kc][tile][BN][BM] exact integer sums (row fastest)
@@ -169,8 +183,22 @@ __global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int64_t M, 
     }
 }
 
-// C tile (it, jt) partial over K chunk kc.  blockIdx.x = jt + tiles_n (it +
-// tiles_m kc): the column tiles sharing an S tile run side by side.
+// Work unit u: C tile (it, jt) partial over K chunk kc, with jt fastest:
+// the column tiles sharing an S tile are processed side by side.
+struct Unit {
+    int jt, it, kc, s_begin, nst;
+};
+__device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
+    Unit w;
+    w.jt = u % prm.tiles_n;
+    const int rest = u / prm.tiles_n;
+    w.it = rest % prm.tiles_m;
+    w.kc = rest / prm.tiles_m;
+    w.s_begin = w.kc * prm.stages_per_kc;
+    w.nst = min(prm.Ks, w.s_begin + prm.stages_per_kc) - w.s_begin;
+    return w;
+}
+
 template <int P>
 __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm) {
     extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -180,28 +208,23 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
     uint64_t* bars = (uint64_t*)(sY + STAGES * P * YD_BYTES);
     uint64_t* full = bars;                                        // stage landed (tx)
     uint64_t* empty = bars + STAGES;                              // MMAs done with the stage
-    uint64_t* accFull = bars + 2 * STAGES;
-    uint64_t* accEmpty = accFull + 1;
-    uint64_t* drain = accEmpty + 1;
+    uint64_t* accFull = bars + 2 * STAGES;                        // [2] window accumulated
+    uint64_t* accEmpty = accFull + 2;                             // [2] window drained
+    uint64_t* drain = accEmpty + 2;
     uint32_t* tmem_slot = (uint32_t*)(drain + 1);
     volatile int* err = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int jt = blockIdx.x % prm.tiles_n;
-    const int rest = blockIdx.x / prm.tiles_n;
-    const int it = rest % prm.tiles_m;
-    const int kc = rest / prm.tiles_m;
-    const int s_begin = kc * prm.stages_per_kc;
-    const int s_end = min(prm.Ks, s_begin + prm.stages_per_kc);
-    const int nst = s_end - s_begin;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accFull, 1);
-        mbar_init(accEmpty, DRAIN_WARPS);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&accFull[b], 1);
+            mbar_init(&accEmpty[b], DRAIN_WARPS);
+        }
         mbar_init(drain, 1);
         *err = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -220,26 +243,34 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
     if (warp == 0) {
         // ---------------- loader: S tile + P digit tiles per stage ----------------
         if (lane == 0) {
-            int issued = 0;
-            const uint8_t* sk = prm.sk + ((size_t)it * prm.Ks + s_begin) * S_BYTES;
-            const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)jt * prm.Ks + s_begin) * (size_t)(P * YD_BYTES);
-            for (int i = 0; i < nst; ++i) {
-                const int slot = i % STAGES;
-                if (i >= STAGES && !mbar_wait(&empty[slot], ((i / STAGES) - 1) & 1, err)) break;
-                mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YD_BYTES));
-                bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
+            int g = 0;                    // stages issued
+            bool ok = true;
+            for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
+                const Unit w = unit_of(prm, u);
+                const uint8_t* sk = prm.sk + ((size_t)w.it * prm.Ks + w.s_begin) * S_BYTES;
+                const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)w.jt * prm.Ks + w.s_begin) * (size_t)(P * YD_BYTES);
+                for (int i = 0; i < w.nst; ++i) {
+                    const int slot = g % STAGES;
+                    if (g >= STAGES && !mbar_wait(&empty[slot], (uint32_t)((g / STAGES) - 1) & 1u, err)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YD_BYTES));
+                    bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
 #pragma unroll
-                for (int p = 0; p < P; ++p)
-                    bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * P + p) * YD_BYTES, YD_BYTES,
-                             &full[slot]);
-                ++issued;
+                    for (int p = 0; p < P; ++p)
+                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * P + p) * YD_BYTES, YD_BYTES,
+                                 &full[slot]);
+                    ++g;
+                }
             }
             // let every copy this warp issued land before the CTA can exit
-            for (int i = (issued > STAGES ? issued - STAGES : 0); i < issued; ++i) {
-                const int slot = i % STAGES;
-                if (!mbar_try(&full[slot], (i / STAGES) & 1)) {
+            for (int i = (g > STAGES ? g - STAGES : 0); i < g; ++i) {
+                const int sl = i % STAGES;
+                const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+                if (!mbar_try(&full[sl], ph)) {
                     const unsigned long long t0 = globaltimer_ns();
-                    while (!mbar_try(&full[slot], (i / STAGES) & 1))
+                    while (!mbar_try(&full[sl], ph))
                         if (globaltimer_ns() - t0 > WAIT_NS) break;
                 }
             }
@@ -248,29 +279,42 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             constexpr uint32_t idesc = idesc_bf16(BM, BN);
-            int win_count = 0;
-            for (int i = 0; i < nst; ++i) {
-                const int slot = i % STAGES;
-                const int in_win = i % WIN;
-                if (in_win == 0 && win_count > 0) {
-                    if (!mbar_wait(accEmpty, (win_count - 1) & 1, err)) break;
+            int g = 0, slot = 0;          // stages consumed; ring slot
+            uint32_t fph = 0;             // full-barrier parity of slot
+            int win = 0;                  // windows started
+            bool ok = true;
+            for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
+                const Unit w = unit_of(prm, u);
+                int in_win = 0;
+                uint32_t acc = 0;
+                for (int i = 0; i < w.nst; ++i) {
+                    if (in_win == 0) {
+                        const int b = win & 1;
+                        acc = tmem + (uint32_t)(b * ACC_COLS);
+                        if (win >= 2) {
+                            if (!mbar_wait(&accEmpty[b], (uint32_t)((win >> 1) - 1) & 1u, err)) { ok = false; break; }
+                            tc_after();
+                        }
+                    }
+                    if (!mbar_wait(&full[slot], fph, err)) { ok = false; break; }
                     tc_after();
-                }
-                if (!mbar_wait(&full[slot], (i / STAGES) & 1, err)) break;
-                tc_after();
-                const uint32_t a0 = smem_u32(sS + slot * S_BYTES);
+                    const uint32_t a0 = smem_u32(sS + slot * S_BYTES);
 #pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const uint32_t b0 = smem_u32(sY + (slot * P + p) * YD_BYTES);
+                    for (int p = 0; p < P; ++p) {
+                        const uint32_t b0 = smem_u32(sY + (slot * P + p) * YD_BYTES);
 #pragma unroll
-                    for (int kk = 0; kk < BK / 16; ++kk)
-                        mma_bf16(tmem + p * BN, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
-                                 (in_win > 0 || kk > 0) ? 1u : 0u);
-                }
-                mma_commit(&empty[slot]);
-                if (in_win == WIN - 1 || i == nst - 1) {
-                    mma_commit(accFull);
-                    ++win_count;
+                        for (int kk = 0; kk < BK / 16; ++kk)
+                            mma_bf16(acc + p * BN, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
+                                     (in_win > 0 || kk > 0) ? 1u : 0u);
+                    }
+                    mma_commit(&empty[slot]);
+                    if (++slot == STAGES) { slot = 0; fph ^= 1u; }
+                    ++g;
+                    if (++in_win == WIN || i == w.nst - 1) {
+                        mma_commit(&accFull[win & 1]);
+                        ++win;
+                        in_win = 0;
+                    }
                 }
             }
             mma_commit(drain);
@@ -282,37 +326,45 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
         // ---------------- drain: TMEM lane quarter (warp & 3), all BN columns ----------------
         const int q = warp & 3;
         const int row = 32 * q + lane;
-        const int tile = it + prm.tiles_m * jt;
-        long long* out = prm.partial + ((size_t)kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BN);
-        const int nwin = (nst + WIN - 1) / WIN;
-        for (int win = 0; win < nwin; ++win) {
-            if (!mbar_wait(accFull, win & 1, err)) break;
-            tc_after();
-#pragma unroll 1
-            for (int c16 = 0; c16 < BN; c16 += 16) {
-                long long v[16];
+        int win = 0;
+        bool ok = true;
+        for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
+            const Unit w = unit_of(prm, u);
+            const int tile = w.it + prm.tiles_m * w.jt;
+            long long v[BN];
 #pragma unroll
-                for (int c = 0; c < 16; ++c) v[c] = 0;
+            for (int c = 0; c < BN; ++c) v[c] = 0;
+            const int nwin = (w.nst + WIN - 1) / WIN;
+            for (int wi = 0; wi < nwin; ++wi, ++win) {
+                const int b = win & 1;
+                if (!mbar_wait(&accFull[b], (uint32_t)(win >> 1) & 1u, err)) { ok = false; break; }
+                tc_after();
+                const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * ACC_COLS);
+                // two digit planes per TMEM round trip (registers: v holds the
+                // unit's int64 tile row)
 #pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    uint32_t r[16];
-                    tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(p * BN + c16), r);
-                    tmem_ld_wait();
+                for (int c16 = 0; c16 < BN; c16 += 16) {
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) {
-                        const long long d = (long long)__float2int_rn(__uint_as_float(r[c]));
-                        v[c] += d * (1LL << (7 * (P - 1 - p)));
+                    for (int p0 = 0; p0 < P; p0 += 2) {
+                        uint32_t r0[16], r1[16];
+                        tmem_ld16(base + (uint32_t)(p0 * BN + c16), r0);
+                        if (p0 + 1 < P) tmem_ld16(base + (uint32_t)((p0 + 1) * BN + c16), r1);
+                        tmem_ld_wait();
+#pragma unroll
+                        for (int c = 0; c < 16; ++c) {
+                            acc_digit(v[c16 + c], r0[c], 8 * (P - 1 - p0));
+                            if (p0 + 1 < P) acc_digit(v[c16 + c], r1[c], 8 * (P - 2 - p0));
+                        }
                     }
                 }
-#pragma unroll
-                for (int c = 0; c < 16; ++c) {
-                    long long* o = out + (size_t)(c16 + c) * BM + row;
-                    *o = (win == 0) ? v[c] : *o + v[c];
-                }
+                tc_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&accEmpty[b]);
             }
-            tc_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(accEmpty);
+            if (!ok) break;
+            long long* out = prm.partial + ((size_t)w.kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BN);
+#pragma unroll
+            for (int c = 0; c < BN; ++c) out[(size_t)c * BM + row] = v[c];
         }
     }
     tc_before();
@@ -385,7 +437,7 @@ __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int
 }
 
 __device__ __forceinline__ uint16_t digit_bf16(uint32_t d, bool neg) {
-    // d <= 128: the float of d has at most 8 significant bits, so its top 16 bits are the bf16
+    // d <= 256: the float of d has at most 8 significant bits, so its top 16 bits are the bf16
     const float f = (float)d;
     return (uint16_t)((__float_as_uint(f) >> 16) | (neg && d ? 0x8000u : 0u));
 }
@@ -415,14 +467,14 @@ __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int6
             if (j < Ntot && k < K) load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
             uint64_t Tq = 0;
             if (M) {
-                const int sh = Ej - 7 * P - e2;
+                const int sh = Ej - 8 * P - e2;
                 if (sh <= 0) Tq = M << (-sh);
                 else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
             }
 #pragma unroll
             for (int p = 0; p < P; ++p) {
-                const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (7 * (P - 1)))
-                                            : (uint32_t)((Tq >> (7 * (P - 1 - p))) & 127u);
+                const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (8 * (P - 1)))
+                                            : (uint32_t)((Tq >> (8 * (P - 1 - p))) & 255u);
                 dg[p][t] = digit_bf16(d, neg);
             }
         }
@@ -480,25 +532,29 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     const size_t smem = smem_bytes<P>();
     const int Ks = div_up(K, BK);
     const int wins = div_up(Ks, WIN);
-    // choose the K split: minimise waves x (windows per CTA + the CTA's fixed
-    // cost -- setup, final drain, partial tile -- about half a window) plus
-    // the partial traffic; a CTA sums at most WIN_MAX windows in int64
-    // (|window value| < 2^52.01, so WIN_MAX windows stay below 2^63)
-    constexpr int WIN_MAX = 2000;
+    // choose the K split for the persistent walk: about
+    //   rounds x stages per unit x (time of one stage)  +  units x (int64 tile
+    //   store and reload, 128 KB of HBM traffic)
+    // with rounds = ceil(units / SMs); a unit sums at most WIN_MAX windows in
+    // int64 (|window value| < 2^48.01, so WIN_MAX windows stay below 2^63)
+    constexpr int WIN_MAX = 32000;
     const int sm = ctx.sm_count;
     const int64_t tiles = (int64_t)tiles_m * tiles_n;
+    const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
+    const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
     double best_cost = 1e300;
-    for (int kcn = div_up(wins, WIN_MAX); kcn <= wins; ++kcn) {
-        const int wpk = div_up(wins, kcn);
-        const int kc_eff = div_up(wins, wpk);
-        const int64_t ctas = tiles * kc_eff;
-        const int64_t waves = (ctas + sm - 1) / sm;
-        const double cost = (double)waves * (wpk + 0.5) + 0.02 * (double)kc_eff * tiles / sm;
+    for (int kcn = div_up(wins, WIN_MAX); kcn <= Ks && kcn <= 64; ++kcn) {
+        const int spk_n = div_up(Ks, kcn);
+        const int kc_eff = div_up(Ks, spk_n);
+        const int64_t units = tiles * kc_eff;
+        const int64_t rounds = (units + sm - 1) / sm;
+        const double cost = (double)rounds * spk_n * t_stage + (double)units * t_unit;
         if (cost < best_cost - 1e-9) { best_cost = cost; best_kc = kc_eff; }
     }
     const int spk = div_up(Ks, best_kc);
     const int kc_count = div_up(Ks, spk);
+    const int64_t units = tiles * kc_count;
 
     DevBuf<int> E((size_t)tiles_n * BN, ctx.stream);
     RNLA_CUDA(cudaMemsetAsync(E.get(), 0, sizeof(int) * tiles_n * BN, ctx.stream));
@@ -533,20 +589,20 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
-    prm.kc_count = kc_count; prm.stages_per_kc = spk;
+    prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
     prm.sk = sk; prm.ydig = dig; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
     {
         auto kfn = sketch_mma_kernel<P>;
         RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const int64_t grid = tiles * kc_count;
+        const int64_t grid = units < sm ? units : sm;
         kfn<<<(unsigned)grid, THREADS, smem, ctx.stream>>>(prm);
         RNLA_LAUNCH_CHECK();
     }
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
-    const int exact_sum = (int64_t)wins <= WIN_MAX ? 1 : 0;      // all windows together fit int64
-    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 7 * P + 3,
+    const int exact_sum = (int64_t)wins + kc_count <= WIN_MAX ? 1 : 0;   // all windows together fit int64
+    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 8 * P + 3,
                                                  exact_sum, C, ldc);
     RNLA_LAUNCH_CHECK();
     ctx.check_status("tensor-core sketch");
@@ -564,14 +620,13 @@ bool tc_available(Ctx& ctx) {
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
-    if (digits <= 0) digits = x_f32 ? 4 : 5;
+    if (digits <= 0) digits = 4;
     switch (digits) {
         case 1: tc::run<1>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
         case 2: tc::run<2>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
         case 3: tc::run<3>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
         case 4: tc::run<4>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
-        case 5: tc::run<5>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
-        default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..5");
+        default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..4");
     }
 }
 

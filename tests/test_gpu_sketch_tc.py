@@ -47,7 +47,7 @@ def test_gaussian_fp64_data(rnla):
     assert err < 1e-9, err
 
 
-def test_float32_data_four_digits(rnla):
+def test_float32_data_default_digits(rnla):
     import torch
     g = torch.Generator(device="cuda").manual_seed(6)
     d, m, n = 256, 9000, 200
@@ -58,7 +58,7 @@ def test_float32_data_four_digits(rnla):
     assert err < 1e-7, err
 
 
-@pytest.mark.parametrize("digits,bound", [(1, 2e-2), (2, 4e-4), (3, 4e-6), (5, 1e-9)])
+@pytest.mark.parametrize("digits,bound", [(1, 2e-2), (2, 4e-4), (3, 4e-6), (4, 1e-9)])
 def test_digit_count_controls_accuracy(rnla, digits, bound):
     import torch
     g = torch.Generator(device="cuda").manual_seed(7)
@@ -68,6 +68,13 @@ def test_digit_count_controls_accuracy(rnla, digits, bound):
     ref = _quantized_sketch(d, m, 9) @ Y
     err = (C - ref).abs().max().item() / ref.abs().max().item()
     assert err < bound, (digits, err)
+
+
+def test_digit_count_out_of_range_is_an_error(rnla):
+    import torch
+    Y = torch.randn((8, 256), device="cuda", dtype=torch.float64).t()
+    with pytest.raises(rnla.RandNLAError):
+        _tc(Y, 16, seed=1, digits=5)
 
 
 def test_blendenpik_bf16x_vs_lapack(rnla):
