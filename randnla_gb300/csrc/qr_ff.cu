@@ -35,7 +35,7 @@ namespace qrff {
 
 constexpr int T = 512;
 constexpr int W = T / 32;
-constexpr int KB = 4;
+constexpr int KB = 2;
 constexpr int MAX_OWNB = 4;
 
 struct Args {
@@ -108,24 +108,46 @@ __device__ __forceinline__ float2 vval(const float2* col, int64_t i, int64_t t) 
 
 // Applies Q_b^T = I - V T^T V^T of reflector block b (V: the KB columns at
 // vb with stride vs, heads at rows b*KB + r; Tm: 4 x 4 column-major) to the
-// KB columns at c (stride m).  nr = reflectors in the block.
+// KB columns at c (stride m).  nr = reflectors in the block.  Both row
+// loops run on packed pairs: W = V^T C pairs reflectors (r, r+1), the
+// update pairs columns (q, q+1).
 __device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int64_t b, int nr, float2* c,
                             int64_t m, float2* red, float2* tot, float2* wsm) {
     const int64_t t0 = b * KB;
-    float h[KB * KB], l[KB * KB];        // [column q][reflector r]
+    f32x2 ah[KB][KB / 2], al[KB][KB / 2];     // [column q][reflector pair]
 #pragma unroll
-    for (int k = 0; k < KB * KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
+    for (int q = 0; q < KB; ++q)
+#pragma unroll
+        for (int k = 0; k < KB / 2; ++k) { ah[q][k] = 0ull; al[q][k] = 0ull; }
     for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
-        float2 v[KB], x[KB];
+        float2 v[KB];
 #pragma unroll
         for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
+        f32x2 vh[KB / 2], vl[KB / 2];
 #pragma unroll
-        for (int q = 0; q < KB; ++q) x[q] = c[(size_t)q * m + i];
+        for (int k = 0; k < KB / 2; ++k) {
+            vh[k] = pk2(v[2 * k].x, v[2 * k + 1].x);
+            vl[k] = pk2(v[2 * k].y, v[2 * k + 1].y);
+        }
 #pragma unroll
-        for (int q = 0; q < KB; ++q)
+        for (int q = 0; q < KB; ++q) {
+            const float2 x = c[(size_t)q * m + i];
+            const f32x2 xh = pk2(x.x, x.x), nxh = pk2(-x.x, -x.x), xl = pk2(x.y, x.y);
 #pragma unroll
-            for (int r = 0; r < KB; ++r) ff_madd(v[r].x, v[r].y, x[q].x, x[q].y, h[q * KB + r], l[q * KB + r]);
+            for (int k = 0; k < KB / 2; ++k) ff2_madd(vh[k], vl[k], xh, nxh, xl, ah[q][k], al[q][k]);
+        }
     }
+    float h[KB * KB], l[KB * KB];        // [column q][reflector r]
+#pragma unroll
+    for (int q = 0; q < KB; ++q)
+#pragma unroll
+        for (int k = 0; k < KB / 2; ++k) {
+            const float2 H = upk2(ah[q][k]), L = upk2(al[q][k]);
+            h[q * KB + 2 * k] = H.x;
+            l[q * KB + 2 * k] = L.x;
+            h[q * KB + 2 * k + 1] = H.y;
+            l[q * KB + 2 * k + 1] = L.y;
+        }
     block_sums<KB * KB>(h, l, red, tot);
     // w'[q][s] = sum_r T[r][s] w[q][r]  (T^T w), one thread per (q, s)
     if ((int)threadIdx.x < KB * KB) {
@@ -135,20 +157,34 @@ __device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int6
         wsm[q * KB + s] = acc;
     }
     __syncthreads();
-    float2 wv[KB * KB];
+    // c_q -= sum_r v_r w'[q][r]: packed over column pairs (q, q+1)
+    f32x2 bh[KB / 2][KB], nbh[KB / 2][KB], bl[KB / 2][KB];
 #pragma unroll
-    for (int k = 0; k < KB * KB; ++k) wv[k] = ff_neg(wsm[k]);
+    for (int k = 0; k < KB / 2; ++k)
+#pragma unroll
+        for (int r = 0; r < KB; ++r) {
+            const float2 w0 = wsm[(2 * k) * KB + r], w1 = wsm[(2 * k + 1) * KB + r];
+            bh[k][r] = pk2(-w0.x, -w1.x);
+            nbh[k][r] = pk2(w0.x, w1.x);
+            bl[k][r] = pk2(-w0.y, -w1.y);
+        }
     for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
-        float2 v[KB];
+        f32x2 vh[KB], vl[KB];
 #pragma unroll
-        for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
+        for (int r = 0; r < KB; ++r) {
+            const float2 v = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
+            vh[r] = pk2(v.x, v.x);
+            vl[r] = pk2(v.y, v.y);
+        }
 #pragma unroll
-        for (int q = 0; q < KB; ++q) {
-            const float2 x = c[(size_t)q * m + i];
-            float xh = x.x, xl = x.y;                 // unnormalised accumulator, one renormalisation
+        for (int k = 0; k < KB / 2; ++k) {
+            const float2 x0 = c[(size_t)(2 * k) * m + i], x1 = c[(size_t)(2 * k + 1) * m + i];
+            f32x2 xh = pk2(x0.x, x1.x), xl = pk2(x0.y, x1.y);   // unnormalised accumulator
 #pragma unroll
-            for (int r = 0; r < KB; ++r) ff_madd(v[r].x, v[r].y, wv[q * KB + r].x, wv[q * KB + r].y, xh, xl);
-            c[(size_t)q * m + i] = ff_norm(xh, xl);
+            for (int r = 0; r < KB; ++r) ff2_madd(vh[r], vl[r], bh[k][r], nbh[k][r], bl[k][r], xh, xl);
+            const float2 H = upk2(xh), L = upk2(xl);
+            c[(size_t)(2 * k) * m + i] = ff_norm(H.x, L.x);
+            c[(size_t)(2 * k + 1) * m + i] = ff_norm(H.y, L.y);
         }
     }
     __syncthreads();
@@ -156,10 +192,13 @@ __device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int6
 
 // Factors the block b held at c (KB columns, stride m; columns >= nc are
 // absent), writing each reflector to global memory as soon as it is formed;
-// then forms T and publishes T, tau and the flag.  The Gram entries
-// g_qr = v_q^T v_r that T needs ride in column r's norm reduction:
-// sum_{i>t} v_q[i] c_r[i] is reduced with ||c_r[t+1:]||^2, and
-// g_qr = v_q[t] + scale_r * that sum once v_r = c_r scale_r is known.
+// then forms T and publishes T, tau and the flag.  One block reduction per
+// column t = b*KB + r gathers, over rows i > t, ||c_r||^2 and
+// S_q = sum c_q[i] c_r[i] for every other column q of the block: for q < r
+// (c_q holds v_q there) they give the Gram entries g_qr = v_q^T v_r that T
+// needs, g_qr = v_q[t] + scale * S_q; for q > r the reflector's dot
+// v_r^T c_q = c_q[t] + scale * S_q, so H_t is applied to the later columns
+// in the same row sweep that scales and publishes v_r.
 __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, float2* tot, float2* tsm) {
     const int64_t m = a.m, n = a.n, nc = a.nc;
     const int64_t t0 = b * KB;
@@ -176,21 +215,22 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
         if (r >= nr) break;
         const int64_t t = t0 + r;
         float2* col = c + (size_t)r * m;
-        // ||c_r[t+1:]||^2 (slot 0) and sum_{i>t} v_q[i] c_r[i] for q < r (slots 1 + q)
-        float h[KB], l[KB];
+        // slot 0: ||c_r[t+1:]||^2; slot 1 + q: sum_{i>t} c_q[i] c_r[i] (q != r, q < ncol)
+        constexpr int NV = 8;
+        float h[NV], l[NV];
 #pragma unroll
-        for (int k = 0; k < KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
+        for (int k = 0; k < NV; ++k) { h[k] = 0.f; l[k] = 0.f; }
         for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
             const float2 x = col[i];
             ff_madd(x.x, x.y, x.x, x.y, h[0], l[0]);
 #pragma unroll
-            for (int q = 0; q < KB - 1; ++q)
-                if (q < r) {
-                    const float2 vq = c[(size_t)q * m + i];
-                    ff_madd(vq.x, vq.y, x.x, x.y, h[1 + q], l[1 + q]);
+            for (int q = 0; q < KB; ++q)
+                if (q != r && q < ncol) {
+                    const float2 y = c[(size_t)q * m + i];
+                    ff_madd(y.x, y.y, x.x, x.y, h[1 + q], l[1 + q]);
                 }
         }
-        block_sums<KB>(h, l, red, tot);
+        block_sums<NV>(h, l, red, tot);
         const float2 xn2 = tot[0];
         const float2 alpha = col[t];
         float2 tau = make_float2(0.f, 0.f), beta = alpha, scale = make_float2(0.f, 0.f);
@@ -200,51 +240,38 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
             scale = ff_div(make_float2(1.f, 0.f), ff_add(alpha, ff_neg(beta)));
             tau = ff_div(ff_add(beta, ff_neg(alpha)), beta);
         }
+        // g[q][r] (q < r) and the update coefficients f_q = -tau v_r^T c_q (q > r)
+        float2 f[KB];
 #pragma unroll
-        for (int q = 0; q < KB - 1; ++q)
+        for (int q = 0; q < KB; ++q) {
+            f[q] = make_float2(0.f, 0.f);
             if (q < r) g[q][r] = ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[1 + q]));
-        // scale into the reflector and publish it (rows > t)
+            if (q > r && q < ncol && tau.x != 0.f)
+                f[q] = ff_neg(ff_mul(tau, ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[1 + q]))));
+        }
+        // one row sweep: scale v_r, publish it, apply H_t to the later columns
+        const bool scl = xn2.x != 0.f;
         for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
-            const float2 v = (xn2.x != 0.f) ? ff_mul(col[i], scale) : col[i];
+            const float2 v = scl ? ff_mul(col[i], scale) : col[i];
             col[i] = v;
             a.VF[i + t * a.ldv] = v;
+#pragma unroll
+            for (int q = 0; q < KB; ++q)
+                if (q > r && q < ncol) {
+                    const float2 x = c[(size_t)q * m + i];
+                    float xh = x.x, xl = x.y;
+                    ff_madd(f[q].x, f[q].y, v.x, v.y, xh, xl);
+                    c[(size_t)q * m + i] = ff_norm(xh, xl);
+                }
         }
+        // row t after every thread has read it (the next column reads rows > t)
         __syncthreads();
         if (threadIdx.x == 0) {
             col[t] = beta;
             taus[r] = tau;
-        }
-        __syncthreads();
-        // H_t on the block's later columns
-        if (r + 1 < ncol && tau.x != 0.f) {
-            float hh[KB], ll[KB];
 #pragma unroll
-            for (int q = 0; q < KB; ++q) { hh[q] = 0.f; ll[q] = 0.f; }
-            for (int64_t i = t + threadIdx.x; i < m; i += T) {
-                const float2 vi = (i == t) ? make_float2(1.f, 0.f) : col[i];
-#pragma unroll
-                for (int q = 0; q < KB; ++q)
-                    if (q > r && q < ncol) {
-                        const float2 x = c[(size_t)q * m + i];
-                        ff_madd(vi.x, vi.y, x.x, x.y, hh[q], ll[q]);
-                    }
-            }
-            block_sums<KB>(hh, ll, red, tot);
-            float2 f[KB];
-#pragma unroll
-            for (int q = 0; q < KB; ++q) f[q] = ff_neg(ff_mul(tau, tot[q]));
-            for (int64_t i = t + threadIdx.x; i < m; i += T) {
-                const float2 vi = (i == t) ? make_float2(1.f, 0.f) : col[i];
-#pragma unroll
-                for (int q = 0; q < KB; ++q)
-                    if (q > r && q < ncol) {
-                        const float2 x = c[(size_t)q * m + i];
-                        float xh = x.x, xl = x.y;
-                        ff_madd(f[q].x, f[q].y, vi.x, vi.y, xh, xl);
-                        c[(size_t)q * m + i] = ff_norm(xh, xl);
-                    }
-            }
-            __syncthreads();
+            for (int q = 0; q < KB; ++q)
+                if (q > r && q < ncol) c[(size_t)q * m + t] = ff_add(c[(size_t)q * m + t], f[q]);
         }
     }
     // T (dlarft, forward, columnwise): T[s][s] = tau_s,
