@@ -313,9 +313,13 @@ static void blendenpik_validate(int64_t m, int64_t n, double epsilon, int64_t l,
     if (n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must have at least one column");
 }
 
+// With a feed, A is still arriving from the host in column chunks: the
+// tensor-core sketch consumes each column tile as it lands; every other
+// path waits for the whole matrix first.
 static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
                             const double* b, double epsilon, int64_t l, double sf,
-                            const rnla_options& o, double* x, rnla_stats* st) {
+                            const rnla_options& o, double* x, rnla_stats* st,
+                            const ColumnFeed* feed = nullptr) {
     blendenpik_validate(m, n, epsilon, l, sf);
     const int64_t d = sketch_rows(m, n, sf);
     if (d < n) fail(RNLA_ERR_SINGULAR_MATRIX, "sketch has fewer rows than columns");
@@ -325,6 +329,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     const int64_t nc = n + 1;
     DevBuf<double> SK((size_t)d * nc, ctx.stream);
     if (o.precision == RNLA_PREC_FP64) {
+        if (feed) feed->wait_all(ctx.stream);
         // the reference's data flow: dense S (line 50), S a and S b (lines 51-52)
         DevBuf<double> S((size_t)d * m, ctx.stream);
         sketch_fill_f64(ctx, DIST_GAUSSIAN, key, d, m, S, d);
@@ -346,7 +351,8 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // synchronisation; the device status is checked once at the end
         ctx.deferred = true;
         // S [a b] in one pass: b rides along as column n of the digit planes
-        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d);
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed);
+        if (feed) feed->wait_all(ctx.stream);
     }
     tm.mark();
     // BF16X + LSQR: the float-float copies of A and b for the solver are built
@@ -373,6 +379,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     const float* a32 = a_f32 ? static_cast<const float*>(Av) : nullptr;
     int64_t iters = 0, istop = 0;
     LsqrResult lr;
+    LsqrPending pend;
     if (o.inner_solver == RNLA_SOLVER_CGLS) {
         bool conv = false;
         iters = cgls_solve(ctx, a64, a32, m, n, lda, Mi, b, z0, epsilon, l, z, &conv);   // line 57
@@ -385,13 +392,16 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         p.iter_lim = l;
         if (o.atol == 0.0 && o.btol == 0.0) p.abs_arnorm_tol = epsilon;
         lr = lsqr_solve(ctx, a64, a32, m, n, lda, Mi, b, z0, p, z, nullptr, nullptr,
-                        o.precision != RNLA_PREC_FP64, lsqr_in.ready ? &lsqr_in : nullptr);
-        iters = lr.itn;
-        istop = lr.istop;
+                        o.precision != RNLA_PREC_FP64, lsqr_in.ready ? &lsqr_in : nullptr, &pend);
     }
     trmv_upper(ctx, Mi, n, n, z, x);                                // line 58
     tm.mark();
     if (ctx.deferred) ctx.finish("blendenpik (BF16X)");
+    if (o.inner_solver != RNLA_SOLVER_CGLS) {
+        pend.resolve(lr);              // after the synchronisation in finish()
+        iters = lr.itn;
+        istop = lr.istop;
+    }
     if (st) {
         st->iterations = iters;
         st->istop = istop;
@@ -705,11 +715,15 @@ int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64_t n, int
     blendenpik_validate(m, n, epsilon, l, sampling_factor);
     cudaStream_t s = host_stream();
     DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
-    h2d_matrix(A, m, a, lda, m, n, s);
     RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
-    int rc = rnla_blendenpik_overdetermined_dev(A, 0, m, n, m, B, epsilon, l, sampling_factor, opt, X,
-                                                stats, s);
-    if (rc != RNLA_OK) return rc;
+    // A goes up in column tiles on the copy stream; the solve starts on the
+    // first tile while the rest is in flight
+    ColumnFeed feed;
+    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
+    Ctx ctx(s);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed);
     RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
     RNLA_CUDA(cudaStreamSynchronize(s));
     RNLA_API_END

@@ -1004,11 +1004,11 @@ static const void* prepare(Ctx& ctx, bool lsqr, IterArgs& a, IterBufs& B, const 
 LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                       int64_t lda, const double* M, const double* b, const double* x0,
                       const LsqrParams& prm, double* x, double* var, double* arnorms_dev, bool ffp,
-                      const LsqrFFInput* pre) {
+                      const LsqrFFInput* pre, LsqrPending* pend) {
     if (n > (int64_t)IT_THREADS * IT_MAXACC)
         fail(RNLA_ERR_UNSUPPORTED, "lsqr: n > 4096 is not supported by the fused kernel");
     if (ffp && a64 && lsqr_ff_supported(n))
-        return lsqr_ff_solve(ctx, a64, m, n, lda, M, b, x0, prm, x, var, arnorms_dev, pre);
+        return lsqr_ff_solve(ctx, a64, m, n, lda, M, b, x0, prm, x, var, arnorms_dev, pre, pend);
     IterArgs a;
     IterBufs B;
     int G;

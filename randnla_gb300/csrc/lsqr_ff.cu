@@ -1177,7 +1177,7 @@ void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t ld
 
 LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
-                         double* arnorms_dev, const LsqrFFInput* pre) {
+                         double* arnorms_dev, const LsqrFFInput* pre, LsqrPending* pend) {
     using namespace lsff;
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
     if (pre && (pre->A != A || pre->m != m || pre->n != n)) pre = nullptr;
@@ -1264,6 +1264,18 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3(G), dim3(kp.threads), params, smem, st));
     count_launch();
     RNLA_CUDA(cudaEventRecord(ev[1], st));
+    if (pend && ctx.deferred) {
+        // no host synchronisation: the scalars go to pinned memory and are
+        // read after the caller's final synchronisation
+        static thread_local double* pinned = nullptr;
+        if (!pinned) RNLA_CUDA(cudaMallocHost(&pinned, 8 * sizeof(double)));
+        pend->host = pinned;
+        pend->ev[0] = ev[0];
+        pend->ev[1] = ev[1];
+        pend->armed = true;
+        RNLA_CUDA(cudaMemcpyAsync(pinned, out.get(), 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        return LsqrResult{};
+    }
     double h[8];
     RNLA_CUDA(cudaMemcpyAsync(h, out.get(), sizeof h, cudaMemcpyDeviceToHost, st));
     RNLA_CUDA(cudaStreamSynchronize(st));
@@ -1277,6 +1289,15 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     r.istop = (int64_t)h[0]; r.itn = (int64_t)h[1];
     r.r1norm = h[2]; r.r2norm = h[3]; r.anorm = h[4]; r.acond = h[5]; r.xnorm = h[6]; r.arnorm = h[7];
     return r;
+}
+
+void LsqrPending::resolve(LsqrResult& r) const {
+    if (!armed) return;
+    const double* h = host;
+    r.istop = (int64_t)h[0]; r.itn = (int64_t)h[1];
+    r.r1norm = h[2]; r.r2norm = h[3]; r.anorm = h[4]; r.acond = h[5]; r.xnorm = h[6]; r.arnorm = h[7];
+    float kms = 0.f;
+    if (cudaEventElapsedTime(&kms, ev[0], ev[1]) == cudaSuccess) r.ms_kernel = kms;
 }
 
 }  // namespace rnla

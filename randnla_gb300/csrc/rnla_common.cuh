@@ -92,6 +92,7 @@ struct DevBuf {
 
 // Second stream of a device, and an event-based dependency `to` -> `from`.
 cudaStream_t side_stream(int device);
+cudaStream_t copy_stream(int device);
 void stream_wait(cudaStream_t to, cudaStream_t from);
 
 void* pool_alloc(size_t bytes, cudaStream_t s);

@@ -2,6 +2,7 @@
 // Everything here works on device pointers, column-major storage, and is
 // enqueued on ctx.stream.
 #pragma once
+#include <vector>
 #include "rnla_common.cuh"
 #include "rnla_rng.cuh"
 
@@ -80,6 +81,22 @@ struct LsqrResult {
     double r1norm = 0, r2norm = 0, anorm = 0, acond = 0, xnorm = 0, arnorm = 0;
     double ms_kernel = 0;   // device time of the persistent kernel
 };
+// Result of a solve enqueued without a host synchronisation: the solver's
+// scalars land in pinned host memory and are read by resolve() once the
+// caller has synchronised the stream.
+struct LsqrPending {
+    double* host = nullptr;                 // 8 values (pinned, per thread)
+    cudaEvent_t ev[2] = {nullptr, nullptr}; // around the kernel
+    bool armed = false;
+    LsqrPending() = default;
+    LsqrPending(const LsqrPending&) = delete;
+    LsqrPending& operator=(const LsqrPending&) = delete;
+    ~LsqrPending() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    void resolve(LsqrResult& r) const;
+};
 // LSQR on the operator A M (M upper-triangular n x n, or identity if
 // Minv_rowmajor == nullptr).  A is double (a64) or float (a32), m x n, lda.
 // x0 nullable; x receives z (the solution of the preconditioned problem,
@@ -88,7 +105,7 @@ struct LsqrFFInput;
 LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                       int64_t lda, const double* M, const double* b, const double* x0,
                       const LsqrParams& prm, double* x, double* var, double* arnorms_dev,
-                      bool ffp, const LsqrFFInput* pre = nullptr);
+                      bool ffp, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
 // CGLS (cg.rs:18-61) on A M, same conventions; returns iterations used.
 int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                    int64_t lda, const double* M, const double* b, const double* x0,
@@ -120,7 +137,7 @@ void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t ld
                      LsqrFFInput& in);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
-                         double* arnorms_dev, const LsqrFFInput* pre = nullptr);
+                         double* arnorms_dev, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
 // Workspace-based LSQR used by the allocation-free entry point (noalloc.cu).
 size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem,
                             const void** kernel);
@@ -132,12 +149,50 @@ void trmv_upper(Ctx& ctx, const double* M, int64_t n, int64_t ldm, const double*
 
 // ---- tensor-core digit-sliced products (sketch_tc.cu) ----
 // Returns true if the sm_103a tensor-core kernels are usable on this device.
+// A matrix arriving from the host in chunks of `cols` columns: chunk c is
+// on the device once `ready[c]` (recorded on the copy stream) has fired.
+struct ColumnFeed {
+    int64_t cols = 0;
+    std::vector<cudaEvent_t> ready;
+    cudaStream_t owner = nullptr;   // stream that frees the destination buffer
+    ColumnFeed() = default;
+    ColumnFeed(const ColumnFeed&) = delete;
+    ColumnFeed& operator=(const ColumnFeed&) = delete;
+    // the owner stream waits for every copy before the destination can be
+    // freed (an early error return must not free memory still being written)
+    ~ColumnFeed() {
+        for (cudaEvent_t e : ready) {
+            if (owner) cudaStreamWaitEvent(owner, e, 0);
+            cudaEventDestroy(e);
+        }
+    }
+    // `s` waits for the chunks holding columns [j0, j1)
+    void wait_cols(cudaStream_t s, int64_t j0, int64_t j1) const {
+        if (j1 <= j0 || cols <= 0) return;
+        const int64_t c1 = (j1 - 1) / cols;
+        for (int64_t c = j0 / cols; c <= c1 && c < (int64_t)ready.size(); ++c)
+            RNLA_CUDA(cudaStreamWaitEvent(s, ready[(size_t)c], 0));
+    }
+    void wait_all(cudaStream_t s) const {
+        for (cudaEvent_t e : ready) RNLA_CUDA(cudaStreamWaitEvent(s, e, 0));
+    }
+};
+// Copies the host matrix a (m x n, lda) to dev (ld m) in column chunks on
+// the device's copy stream, after the work already enqueued on `s`.
+void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64_t lda, int64_t chunk,
+                       cudaStream_t s, ColumnFeed& feed);
+
 bool tc_available(Ctx& ctx);
 // C (M x N', ldc, FP64) = S [X extra] where S (M x K) is the quantised
 // Gaussian sketch of `key` (entry (i,k) = word i + k*round_up(M,4)), X (K x N)
 // and the optional double column `extra` (K values) appended as column N.
+// With a feed, X arrives from the host in column chunks and each column tile
+// of the product is started as soon as its columns are on the device.
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
-                     int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc);
+                     int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
+                     const ColumnFeed* feed = nullptr);
+// Column tile width of the tensor-core sketch (the natural feed chunk).
+constexpr int64_t TC_TILE_COLS = 64;
 // C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.
 void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                 int64_t NN, int64_t ldy, int dx, int dy, double* C, int64_t ldc);

@@ -1,5 +1,6 @@
 // Library runtime: device memory pool, per-call context, error reporting,
 // generator kernels and their C entry points.
+#include <algorithm>
 #include "rnla_internal.h"
 #include "rnla_abi.h"
 #include <mutex>
@@ -76,6 +77,38 @@ cudaStream_t side_stream(int dev) {
     RNLA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     cache[dev] = st;
     return st;
+}
+
+// A third stream per device for host <-> device copies that overlap compute.
+cudaStream_t copy_stream(int dev) {
+    static std::mutex mu;
+    static std::map<int, cudaStream_t> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(dev);
+    if (it != cache.end()) return it->second;
+    cudaStream_t st = nullptr;
+    RNLA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cache[dev] = st;
+    return st;
+}
+
+void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64_t lda, int64_t chunk,
+                       cudaStream_t s, ColumnFeed& feed) {
+    int d = 0;
+    RNLA_CUDA(cudaGetDevice(&d));
+    const cudaStream_t cp = copy_stream(d);
+    stream_wait(cp, s);                            // the device buffer exists
+    feed.cols = chunk;
+    feed.owner = s;
+    for (int64_t j0 = 0; j0 < n; j0 += chunk) {
+        const int64_t c = std::min(chunk, n - j0);
+        RNLA_CUDA(cudaMemcpy2DAsync(dev + j0 * m, m * sizeof(double), a + j0 * lda, lda * sizeof(double),
+                                    m * sizeof(double), c, cudaMemcpyHostToDevice, cp));
+        cudaEvent_t ev;
+        RNLA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        feed.ready.push_back(ev);
+        RNLA_CUDA(cudaEventRecord(ev, cp));
+    }
 }
 
 // `to` waits for the work enqueued on `from` so far.

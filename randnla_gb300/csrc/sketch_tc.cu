@@ -49,6 +49,7 @@
 #include "rnla_async.cuh"
 #include <cuda_bf16.h>
 #include <vector>
+#include <algorithm>
 #include <cstring>
 
 namespace rnla {
@@ -56,7 +57,7 @@ namespace rnla {
 namespace tc {
 
 constexpr int BM = 128;           // sketch rows per CTA tile (TMEM lanes)
-constexpr int BN = 64;            // data columns per CTA tile
+constexpr int BN = (int)TC_TILE_COLS; // data columns per CTA tile
 constexpr int BK = 64;            // K per pipeline stage (one 128-byte bf16 row)
 constexpr int WIN = 16;           // stages per exact window (1024 K values)
 constexpr int MAXP = 4;           // digits
@@ -130,7 +131,8 @@ __device__ __forceinline__ void acc_digit(long long& acc, uint32_t f, int sh) {
 struct Params {
     int64_t M, N, K;          // C is M x N, reduction length K
     int tiles_m, tiles_n, Ks, kc_count, stages_per_kc;
-    int units;                // tiles_m * tiles_n * kc_count
+    int units;                // work units of this launch
+    int jt_only;              // >= 0: only column tile jt_only (units = tiles_m * kc_count)
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
     const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
     long long* partial;       // [kc][tile][BN][BM] exact integer sums (row fastest)
@@ -190,8 +192,14 @@ struct Unit {
 };
 __device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
     Unit w;
-    w.jt = u % prm.tiles_n;
-    const int rest = u / prm.tiles_n;
+    int rest;
+    if (prm.jt_only >= 0) {
+        w.jt = prm.jt_only;
+        rest = u;
+    } else {
+        w.jt = u % prm.tiles_n;
+        rest = u / prm.tiles_n;
+    }
     w.it = rest % prm.tiles_m;
     w.kc = rest / prm.tiles_m;
     w.s_begin = w.kc * prm.stages_per_kc;
@@ -411,12 +419,23 @@ __device__ __forceinline__ void load_elem(const T* __restrict__ Y, int64_t ldy, 
     }
 }
 
+// E[j] = -1074 (the exponent of an all-zero column) before colexp_kernel.
+__global__ void exp_init_kernel(int* __restrict__ E, int64_t n) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
+        E[j] = -1074;
+}
+
+// Block (x, y): rows [x * rows_per_block, ...) of column j0 + y; the block
+// maximum goes into E[j] with atomicMax (the maximum is order independent).
 template <typename T>
 __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
-                              const double* __restrict__ extra, int* __restrict__ E) {
-    const int64_t j = blockIdx.x;
-    int best = -100000;
-    for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
+                              const double* __restrict__ extra, int* __restrict__ E, int64_t j0,
+                              int64_t rows_per_block) {
+    const int64_t j = j0 + blockIdx.y;
+    const int64_t k0 = (int64_t)blockIdx.x * rows_per_block;
+    const int64_t k1 = min(K, k0 + rows_per_block);
+    int best = -1074;
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         uint64_t M;
         int e2;
         bool neg;
@@ -429,10 +448,10 @@ __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
     __syncthreads();
     if (threadIdx.x < 32) {
-        best = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : -100000;
+        best = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : -1074;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
-        if (threadIdx.x == 0) E[j] = (best == -100000) ? -1074 : best;
+        if (threadIdx.x == 0 && best > -1074) atomicMax(&E[j], best);
     }
 }
 
@@ -447,12 +466,12 @@ __device__ __forceinline__ uint16_t digit_bf16(uint32_t d, bool neg) {
 template <typename T, int P>
 __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
                              const double* __restrict__ extra, int64_t Ntot, const int* __restrict__ E,
-                             int Ks, int tiles_n, uint16_t* __restrict__ out) {
+                             int Ks, int jt0, int jt_count, uint16_t* __restrict__ out) {
     const int64_t chunks_per_col = (int64_t)Ks * 8;
-    const int64_t total = chunks_per_col * (int64_t)tiles_n * BN;
+    const int64_t total = chunks_per_col * (int64_t)jt_count * BN;
     for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = u / chunks_per_col;
+        const int64_t j = (int64_t)jt0 * BN + u / chunks_per_col;
         const int64_t cc = u % chunks_per_col;
         const int s = (int)(cc >> 3), c8 = (int)(cc & 7);
         const int jt = (int)(j / BN), jl = (int)(j % BN);
@@ -526,7 +545,7 @@ static size_t smem_bytes() {
 
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t K, int64_t N0, int64_t ldy,
-                const double* extra, int64_t M, double* C, int64_t ldc) {
+                const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
     const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
     const size_t smem = smem_bytes<P>();
@@ -540,6 +559,8 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     constexpr int WIN_MAX = 32000;
     const int sm = ctx.sm_count;
     const int64_t tiles = (int64_t)tiles_m * tiles_n;
+    // with a feed, each column tile is its own launch as its columns arrive
+    const int64_t tiles_launch = feed ? (int64_t)tiles_m : tiles;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -547,17 +568,18 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     for (int kcn = div_up(wins, WIN_MAX); kcn <= Ks && kcn <= 64; ++kcn) {
         const int spk_n = div_up(Ks, kcn);
         const int kc_eff = div_up(Ks, spk_n);
-        const int64_t units = tiles * kc_eff;
+        const int64_t units = tiles_launch * kc_eff;
         const int64_t rounds = (units + sm - 1) / sm;
         const double cost = (double)rounds * spk_n * t_stage + (double)units * t_unit;
         if (cost < best_cost - 1e-9) { best_cost = cost; best_kc = kc_eff; }
     }
     const int spk = div_up(Ks, best_kc);
     const int kc_count = div_up(Ks, spk);
-    const int64_t units = tiles * kc_count;
+    const int64_t units = tiles_launch * kc_count;
 
     DevBuf<int> E((size_t)tiles_n * BN, ctx.stream);
-    RNLA_CUDA(cudaMemsetAsync(E.get(), 0, sizeof(int) * tiles_n * BN, ctx.stream));
+    exp_init_kernel<<<(unsigned)div_up((int64_t)tiles_n * BN, 256), 256, 0, ctx.stream>>>(E, (int64_t)tiles_n * BN);
+    RNLA_LAUNCH_CHECK();
     DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * (YD_BYTES / 2), ctx.stream);
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
@@ -572,32 +594,51 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
         sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, M, K, Ks, sk);
         RNLA_LAUNCH_CHECK();
     }
-    if (y_f32) colexp_kernel<float><<<(unsigned)N, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, E);
-    else colexp_kernel<double><<<(unsigned)N, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, E);
-    RNLA_LAUNCH_CHECK();
-    {
-        const int64_t units = (int64_t)Ks * 8 * tiles_n * BN;
-        int g = div_up(units, 256);
-        if (g > 32 * sm) g = 32 * sm;
-        if (y_f32)
-            slice_kernel<float, P><<<g, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, tiles_n, dig);
-        else
-            slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, tiles_n, dig);
-        RNLA_LAUNCH_CHECK();
-    }
-    stream_wait(ctx.stream, side);                 // S is written
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
     prm.sk = sk; prm.ydig = dig; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
-    {
-        auto kfn = sketch_mma_kernel<P>;
-        RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const int64_t grid = units < sm ? units : sm;
-        kfn<<<(unsigned)grid, THREADS, smem, ctx.stream>>>(prm);
+    auto kfn = sketch_mma_kernel<P>;
+    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)(units < sm ? units : sm);
+    // exponents and digit planes of column tiles [jt0, jt0 + cnt)
+    auto digits = [&](int jt0, int cnt) {
+        const int64_t j0 = (int64_t)jt0 * BN;
+        const int64_t j1 = std::min((int64_t)N, (int64_t)(jt0 + cnt) * BN);
+        // about 16 values per thread: K / 4096 blocks per column
+        const int64_t rpb = 4096;
+        const dim3 cg((unsigned)div_up(K, rpb), (unsigned)(j1 - j0));
+        if (y_f32)
+            colexp_kernel<float><<<cg, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, E, j0, rpb);
+        else
+            colexp_kernel<double><<<cg, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, E, j0, rpb);
         RNLA_LAUNCH_CHECK();
+        const int64_t su = (int64_t)Ks * 8 * cnt * BN;
+        int g = div_up(su, 256);
+        if (g > 32 * sm) g = 32 * sm;
+        if (y_f32)
+            slice_kernel<float, P><<<g, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
+        else
+            slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
+        RNLA_LAUNCH_CHECK();
+    };
+    if (!feed) {
+        digits(0, tiles_n);
+        stream_wait(ctx.stream, side);             // S is written
+        prm.jt_only = -1;
+        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+        RNLA_LAUNCH_CHECK();
+    } else {
+        for (int jt = 0; jt < tiles_n; ++jt) {
+            feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
+            digits(jt, 1);
+            if (jt == 0) stream_wait(ctx.stream, side);
+            prm.jt_only = jt;
+            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+            RNLA_LAUNCH_CHECK();
+        }
     }
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
@@ -618,14 +659,15 @@ bool tc_available(Ctx& ctx) {
 }
 
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
-                     int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc) {
+                     int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
+                     const ColumnFeed* feed) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
     if (digits <= 0) digits = 4;
     switch (digits) {
-        case 1: tc::run<1>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
-        case 2: tc::run<2>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
-        case 3: tc::run<3>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
-        case 4: tc::run<4>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc); break;
+        case 1: tc::run<1>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 2: tc::run<2>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 3: tc::run<3>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 4: tc::run<4>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
         default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..4");
     }
 }
