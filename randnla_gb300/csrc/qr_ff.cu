@@ -10,14 +10,22 @@
 // strided over the threads).  The owner of a block factors it column by
 // column (LAPACK dlarfg reflectors: beta = -sign(alpha) ||(alpha, x)||,
 // v = x / (alpha - beta), tau = (beta - alpha) / beta, tau = 0 when x is
-// exactly zero), forms the block's triangular factor T (dlarft, forward,
-// columnwise) so that H_0 H_1 H_2 H_3 = I - V T V^T, publishes V, T and a
-// flag.  On seeing flag rb a CTA bulk-copies V and T of block rb into shared
-// memory and applies Q_rb^T = I - V T^T V^T to its later blocks -- the owner
-// of block rb + 1 first, which then factors that block (look-ahead).  One
-// cross-CTA hand-off and one batched reduction per block of 4 columns sit on
-// the critical path.  Flag and copy waits are bounded (2 s) and end the
-// kernel with a status code.
+// exactly zero) and writes each reflector v_t and tau_t to global memory as
+// soon as it is formed.  Every CTA applies every reflector to the blocks it
+// still holds, in order, as the reflector lands: there is no flag -- the
+// reflector buffers start filled with a value no arithmetic produces, and a
+// reader re-loads an entry until it has been written.  A block's owner
+// factors it once all earlier reflectors are applied, so the critical path
+// per block is its KB column steps plus one cross-SM hand-off (the last
+// reflector of the previous block reaching the next owner), and every other
+// CTA's updates overlap it.  All waits are bounded (2 s) and end the kernel
+// with a status code.
+//
+// A column step is one block reduction (the column's norm below the
+// diagonal and its dots with the block's later columns, all accumulated
+// during the previous step's row sweep) and one row sweep (scale v, publish
+// it, apply H_t to the later columns of the block, accumulate the next
+// step's reduction).
 //
 // Reductions are float-float: a reduce-scatter butterfly inside each warp
 // (NV values: each exchange level halves the values a lane keeps), then the
@@ -35,7 +43,7 @@ namespace qrff {
 
 constexpr int T = 512;
 constexpr int W = T / 32;
-constexpr int KB = 2;
+constexpr int KB = 4;
 constexpr int MAX_OWNB = 4;
 
 struct Args {
@@ -43,13 +51,39 @@ struct Args {
     int64_t m, n, nc, ld;
     int64_t ldv;            // m rounded up to even: leading dimension of VF
     float2* VF;             // ldv x n reflectors (column t: rows t+1..m-1)
-    float2* TF;             // per reflector block: 4 x 4 T (column-major) then 4 tau
-    unsigned int* flags;    // one per reflector block
+    float2* taug;           // tau_t
     unsigned int* status;
 };
 
-__device__ __forceinline__ void fail_status(unsigned int* status) {
-    atomicCAS(status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+// VF and taug start filled with this signalling NaN (as the high word of
+// each pair): no arithmetic produces it (results are quiet NaNs), so an
+// entry that differs from it has been written.
+constexpr uint32_t UNSET = 0x7FBADBADu;
+
+__device__ __forceinline__ float2 ld_relaxed_f2(const float2* p) {
+    float2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p) : "memory");
+    return v;
+}
+
+// Bounded spin until *p has been written; false (status set) on timeout or
+// when another CTA has failed.
+__device__ __forceinline__ bool ld_written(const Args& a, const float2* p, float2& v) {
+    v = ld_relaxed_f2(p);
+    if (__float_as_uint(v.x) != UNSET) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned int spins = 0;
+    while (true) {
+        v = ld_relaxed_f2(p);
+        if (__float_as_uint(v.x) != UNSET) return true;
+        if ((++spins & 31u) == 0u) {
+            if (*((volatile unsigned int*)a.status) != 0u) return false;
+            if (globaltimer_ns() - t0 > MBAR_WAIT_NS) {
+                atomicCAS(a.status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+                return false;
+            }
+        }
+    }
 }
 
 // Block-wide float-float sums of NV unnormalised accumulators (h, l); the
@@ -100,137 +134,38 @@ __device__ __forceinline__ void block_sums(float (&h)[NV], float (&l)[NV], float
     __syncthreads();
 }
 
-// v_r[i] of a reflector stored in a column with its head at row t: 0 above
-// t, 1 at t, the stored value below.
-__device__ __forceinline__ float2 vval(const float2* col, int64_t i, int64_t t) {
-    return (i > t) ? col[i] : make_float2(i == t ? 1.f : 0.f, 0.f);
-}
-
-// Applies Q_b^T = I - V T^T V^T of reflector block b (V: the KB columns at
-// vb with stride vs, heads at rows b*KB + r; Tm: 4 x 4 column-major) to the
-// KB columns at c (stride m).  nr = reflectors in the block.  Both row
-// loops run on packed pairs: W = V^T C pairs reflectors (r, r+1), the
-// update pairs columns (q, q+1).
-__device__ void apply_block(const float2* vb, int64_t vs, const float2* Tm, int64_t b, int nr, float2* c,
-                            int64_t m, float2* red, float2* tot, float2* wsm) {
-    const int64_t t0 = b * KB;
-    f32x2 ah[KB][KB / 2], al[KB][KB / 2];     // [column q][reflector pair]
-#pragma unroll
-    for (int q = 0; q < KB; ++q)
-#pragma unroll
-        for (int k = 0; k < KB / 2; ++k) { ah[q][k] = 0ull; al[q][k] = 0ull; }
-    for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
-        float2 v[KB];
-#pragma unroll
-        for (int r = 0; r < KB; ++r) v[r] = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
-        f32x2 vh[KB / 2], vl[KB / 2];
-#pragma unroll
-        for (int k = 0; k < KB / 2; ++k) {
-            vh[k] = pk2(v[2 * k].x, v[2 * k + 1].x);
-            vl[k] = pk2(v[2 * k].y, v[2 * k + 1].y);
-        }
-#pragma unroll
-        for (int q = 0; q < KB; ++q) {
-            const float2 x = c[(size_t)q * m + i];
-            const f32x2 xh = pk2(x.x, x.x), nxh = pk2(-x.x, -x.x), xl = pk2(x.y, x.y);
-#pragma unroll
-            for (int k = 0; k < KB / 2; ++k) ff2_madd(vh[k], vl[k], xh, nxh, xl, ah[q][k], al[q][k]);
-        }
-    }
-    float h[KB * KB], l[KB * KB];        // [column q][reflector r]
-#pragma unroll
-    for (int q = 0; q < KB; ++q)
-#pragma unroll
-        for (int k = 0; k < KB / 2; ++k) {
-            const float2 H = upk2(ah[q][k]), L = upk2(al[q][k]);
-            h[q * KB + 2 * k] = H.x;
-            l[q * KB + 2 * k] = L.x;
-            h[q * KB + 2 * k + 1] = H.y;
-            l[q * KB + 2 * k + 1] = L.y;
-        }
-    block_sums<KB * KB>(h, l, red, tot);
-    // w'[q][s] = sum_r T[r][s] w[q][r]  (T^T w), one thread per (q, s)
-    if ((int)threadIdx.x < KB * KB) {
-        const int q = threadIdx.x / KB, s = threadIdx.x % KB;
-        float2 acc = make_float2(0.f, 0.f);
-        for (int r = 0; r <= s; ++r) acc = ff_add(acc, ff_mul(Tm[r + s * KB], tot[q * KB + r]));
-        wsm[q * KB + s] = acc;
-    }
-    __syncthreads();
-    // c_q -= sum_r v_r w'[q][r]: packed over column pairs (q, q+1)
-    f32x2 bh[KB / 2][KB], nbh[KB / 2][KB], bl[KB / 2][KB];
-#pragma unroll
-    for (int k = 0; k < KB / 2; ++k)
-#pragma unroll
-        for (int r = 0; r < KB; ++r) {
-            const float2 w0 = wsm[(2 * k) * KB + r], w1 = wsm[(2 * k + 1) * KB + r];
-            bh[k][r] = pk2(-w0.x, -w1.x);
-            nbh[k][r] = pk2(w0.x, w1.x);
-            bl[k][r] = pk2(-w0.y, -w1.y);
-        }
-    for (int64_t i = t0 + threadIdx.x; i < m; i += T) {
-        f32x2 vh[KB], vl[KB];
-#pragma unroll
-        for (int r = 0; r < KB; ++r) {
-            const float2 v = (r < nr) ? vval(vb + (size_t)r * vs, i, t0 + r) : make_float2(0.f, 0.f);
-            vh[r] = pk2(v.x, v.x);
-            vl[r] = pk2(v.y, v.y);
-        }
-#pragma unroll
-        for (int k = 0; k < KB / 2; ++k) {
-            const float2 x0 = c[(size_t)(2 * k) * m + i], x1 = c[(size_t)(2 * k + 1) * m + i];
-            f32x2 xh = pk2(x0.x, x1.x), xl = pk2(x0.y, x1.y);   // unnormalised accumulator
-#pragma unroll
-            for (int r = 0; r < KB; ++r) ff2_madd(vh[r], vl[r], bh[k][r], nbh[k][r], bl[k][r], xh, xl);
-            const float2 H = upk2(xh), L = upk2(xl);
-            c[(size_t)(2 * k) * m + i] = ff_norm(H.x, L.x);
-            c[(size_t)(2 * k + 1) * m + i] = ff_norm(H.y, L.y);
-        }
-    }
-    __syncthreads();
-}
-
 // Factors the block b held at c (KB columns, stride m; columns >= nc are
-// absent), writing each reflector to global memory as soon as it is formed;
-// then forms T and publishes T, tau and the flag.  One block reduction per
-// column t = b*KB + r gathers, over rows i > t, ||c_r||^2 and
-// S_q = sum c_q[i] c_r[i] for every other column q of the block: for q < r
-// (c_q holds v_q there) they give the Gram entries g_qr = v_q^T v_r that T
-// needs, g_qr = v_q[t] + scale * S_q; for q > r the reflector's dot
-// v_r^T c_q = c_q[t] + scale * S_q, so H_t is applied to the later columns
-// in the same row sweep that scales and publishes v_r.
-__device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, float2* tot, float2* tsm) {
+// absent), writing each reflector and its tau to global memory as soon as
+// it is formed.  Column step r (t = b*KB + r): the block reduction of
+// ||c_r[t+1:]||^2 and S_q = sum_{i>t} c_q[i] c_r[i] (q > r), the reflector
+// scalars, then one row sweep that scales v_r, publishes it, applies H_t to
+// the later columns (v_r^T c_q = c_q[t] + scale S_q) and accumulates the
+// next step's reduction on the updated rows.
+__device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, float2* tot) {
     const int64_t m = a.m, n = a.n, nc = a.nc;
     const int64_t t0 = b * KB;
     const int nr = (int)min((int64_t)KB, n - t0);
     const int ncol = (int)min((int64_t)KB, nc - t0);
-    float2* taus = tsm + KB * KB;
-    float2 g[KB][KB];                      // g[q][r], q < r (all threads hold the same values)
+    // slot 0: ||c_r[t+1:]||^2; slot q (q > r): sum_{i>t} c_q[i] c_r[i]
+    float h[KB], l[KB];
 #pragma unroll
-    for (int q = 0; q < KB; ++q)
+    for (int k = 0; k < KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
+    for (int64_t i = t0 + 1 + threadIdx.x; i < m; i += T) {
+        const float2 x = c[i];
+        ff_madd(x.x, x.y, x.x, x.y, h[0], l[0]);
 #pragma unroll
-        for (int r = 0; r < KB; ++r) g[q][r] = make_float2(0.f, 0.f);
+        for (int q = 1; q < KB; ++q)
+            if (q < ncol) {
+                const float2 y = c[(size_t)q * m + i];
+                ff_madd(y.x, y.y, x.x, x.y, h[q], l[q]);
+            }
+    }
 #pragma unroll
     for (int r = 0; r < KB; ++r) {
         if (r >= nr) break;
         const int64_t t = t0 + r;
         float2* col = c + (size_t)r * m;
-        // slot 0: ||c_r[t+1:]||^2; slot 1 + q: sum_{i>t} c_q[i] c_r[i] (q != r, q < ncol)
-        constexpr int NV = 8;
-        float h[NV], l[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k) { h[k] = 0.f; l[k] = 0.f; }
-        for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
-            const float2 x = col[i];
-            ff_madd(x.x, x.y, x.x, x.y, h[0], l[0]);
-#pragma unroll
-            for (int q = 0; q < KB; ++q)
-                if (q != r && q < ncol) {
-                    const float2 y = c[(size_t)q * m + i];
-                    ff_madd(y.x, y.y, x.x, x.y, h[1 + q], l[1 + q]);
-                }
-        }
-        block_sums<NV>(h, l, red, tot);
+        block_sums<KB>(h, l, red, tot);
         const float2 xn2 = tot[0];
         const float2 alpha = col[t];
         float2 tau = make_float2(0.f, 0.f), beta = alpha, scale = make_float2(0.f, 0.f);
@@ -240,79 +175,154 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
             scale = ff_div(make_float2(1.f, 0.f), ff_add(alpha, ff_neg(beta)));
             tau = ff_div(ff_add(beta, ff_neg(alpha)), beta);
         }
-        // g[q][r] (q < r) and the update coefficients f_q = -tau v_r^T c_q (q > r)
+        // update coefficients f_q = -tau v_r^T c_q (q > r)
         float2 f[KB];
 #pragma unroll
         for (int q = 0; q < KB; ++q) {
             f[q] = make_float2(0.f, 0.f);
-            if (q < r) g[q][r] = ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[1 + q]));
             if (q > r && q < ncol && tau.x != 0.f)
-                f[q] = ff_neg(ff_mul(tau, ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[1 + q]))));
+                f[q] = ff_neg(ff_mul(tau, ff_add(c[(size_t)q * m + t], ff_mul(scale, tot[q]))));
         }
-        // one row sweep: scale v_r, publish it, apply H_t to the later columns
+        // one row sweep: scale v_r, publish it, apply H_t to the later
+        // columns, accumulate the next step's reduction (rows > t + 1)
         const bool scl = xn2.x != 0.f;
+        const int rn = r + 1;                    // next column
+        const bool nxt = rn < nr;
+#pragma unroll
+        for (int k = 0; k < KB; ++k) { h[k] = 0.f; l[k] = 0.f; }
         for (int64_t i = t + 1 + threadIdx.x; i < m; i += T) {
             const float2 v = scl ? ff_mul(col[i], scale) : col[i];
             col[i] = v;
             a.VF[i + t * a.ldv] = v;
+            float2 y[KB];
 #pragma unroll
-            for (int q = 0; q < KB; ++q)
+            for (int q = 0; q < KB; ++q) {
+                y[q] = make_float2(0.f, 0.f);
                 if (q > r && q < ncol) {
                     const float2 x = c[(size_t)q * m + i];
                     float xh = x.x, xl = x.y;
                     ff_madd(f[q].x, f[q].y, v.x, v.y, xh, xl);
-                    c[(size_t)q * m + i] = ff_norm(xh, xl);
+                    y[q] = ff_norm(xh, xl);
+                    c[(size_t)q * m + i] = y[q];
                 }
+            }
+            if (nxt && i > t + 1) {
+                const float2 x = y[rn < KB ? rn : 0];
+                ff_madd(x.x, x.y, x.x, x.y, h[0], l[0]);
+#pragma unroll
+                for (int q = 0; q < KB; ++q)
+                    if (q > rn && q < ncol) ff_madd(y[q].x, y[q].y, x.x, x.y, h[q], l[q]);
+            }
         }
-        // row t after every thread has read it (the next column reads rows > t)
+        // row t after every thread has read it (the next step reads rows > t)
         __syncthreads();
         if (threadIdx.x == 0) {
             col[t] = beta;
-            taus[r] = tau;
 #pragma unroll
             for (int q = 0; q < KB; ++q)
                 if (q > r && q < ncol) c[(size_t)q * m + t] = ff_add(c[(size_t)q * m + t], f[q]);
+            a.taug[t] = tau;
         }
-    }
-    // T (dlarft, forward, columnwise): T[s][s] = tau_s,
-    // T[0:s, s] = -tau_s T[0:s, 0:s] (g[0:s][s]); unrolled, in registers.
-    if (threadIdx.x == 0) {
-        float2 Tm[KB][KB];
-#pragma unroll
-        for (int r = 0; r < KB; ++r)
-#pragma unroll
-            for (int s2 = 0; s2 < KB; ++s2) Tm[r][s2] = make_float2(0.f, 0.f);
-#pragma unroll
-        for (int s2 = 0; s2 < KB; ++s2) {
-            if (s2 < nr) {
-                const float2 ts = taus[s2];
-                Tm[s2][s2] = ts;
-#pragma unroll
-                for (int r = 0; r < KB; ++r)
-                    if (r < s2) {
-                        float2 acc = make_float2(0.f, 0.f);
-#pragma unroll
-                        for (int k = 0; k < KB; ++k)
-                            if (k >= r && k < s2) acc = ff_add(acc, ff_mul(Tm[r][k], g[k][s2]));
-                        Tm[r][s2] = ff_neg(ff_mul(ts, acc));
-                    }
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < KB; ++r)
-#pragma unroll
-            for (int s2 = 0; s2 < KB; ++s2) {
-                tsm[r + s2 * KB] = Tm[r][s2];
-                a.TF[b * (KB * KB + KB) + r + s2 * KB] = Tm[r][s2];
-            }
-#pragma unroll
-        for (int r = 0; r < KB; ++r) a.TF[b * (KB * KB + KB) + KB * KB + r] = taus[r];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicExch(&a.flags[b], 1u);
+}
+
+// H_t = I - tau_t v_t v_t^T on the ncol columns at c (stride m), v_t read
+// from VF through L2 as it is written (each thread waits for its own
+// entries) into vtmp (shared, m entries).  One block reduction of the ncol
+// dots v_t^T c_q, one update sweep.  False if a wait failed (all threads
+// agree through *ok).
+template <int NC>
+__device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, int ncol, float2* red,
+                                float2* tot, float2* vtmp, int* ok) {
+    constexpr int NP = NC / 2;               // column pairs (packed f32x2 arithmetic)
+    float2 ct[NC];
+#pragma unroll
+    for (int q = 0; q < NC; ++q)
+        ct[q] = (q < ncol) ? c[(size_t)q * m + t] : make_float2(0.f, 0.f);   // read before the reduction's barrier
+    if (threadIdx.x == 0) *ok = 1;
+    __syncthreads();
+    bool good = true;
+    const int np = (ncol + 1) >> 1;
+    f32x2 ah[NP], al[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) { ah[k] = 0ull; al[k] = 0ull; }
+    const float2* vg = a.VF + t * a.ldv;
+    // RB rows per thread per round: their L2 loads are all in flight before
+    // any is checked, so a round costs one L2 round trip
+    constexpr int RB = (NC <= 8) ? 4 : 2;
+    for (int64_t i0 = t + 1 + threadIdx.x; i0 < m; i0 += (int64_t)RB * T) {
+        float2 vr[RB];
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int64_t i = i0 + (int64_t)u * T;
+            vr[u] = (i < m) ? ld_relaxed_f2(vg + i) : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const int64_t i = i0 + (int64_t)u * T;
+            if (i >= m) break;
+            float2 v = vr[u];
+            if (__float_as_uint(v.x) == UNSET && !ld_written(a, vg + i, v)) { good = false; v = make_float2(0.f, 0.f); }
+            vtmp[i] = v;
+            const f32x2 vh = pk2(v.x, v.x), nvh = pk2(-v.x, -v.x), vl = pk2(v.y, v.y);
+#pragma unroll
+            for (int k = 0; k < NP; ++k)
+                if (k < np) {
+                    const float2 x0 = c[(size_t)(2 * k) * m + i], x1 = c[(size_t)(2 * k + 1) * m + i];
+                    ff2_madd(pk2(x0.x, x1.x), pk2(x0.y, x1.y), vh, nvh, vl, ah[k], al[k]);
+                }
+        }
     }
+    float2 tau;
+    if (!ld_written(a, a.taug + t, tau)) good = false;
+    if (!good) *ok = 0;
+    float h[NC], l[NC];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const float2 H = upk2(ah[k]), L = upk2(al[k]);
+        h[2 * k] = H.x; l[2 * k] = L.x;
+        h[2 * k + 1] = H.y; l[2 * k + 1] = L.y;
+    }
+    block_sums<NC>(h, l, red, tot);
+    if (!*ok) return false;
+    // c_q += f_q v over column pairs: b = (f_q, f_q+1)
+    f32x2 bh[NP], nbh[NP], bl[NP];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
+        if (tau.x != 0.f) {
+            if (2 * k < ncol) f0 = ff_neg(ff_mul(tau, ff_add(ct[2 * k], tot[2 * k])));
+            if (2 * k + 1 < ncol) f1 = ff_neg(ff_mul(tau, ff_add(ct[2 * k + 1], tot[2 * k + 1])));
+        }
+        bh[k] = pk2(f0.x, f1.x);
+        nbh[k] = pk2(-f0.x, -f1.x);
+        bl[k] = pk2(f0.y, f1.y);
+    }
+    for (int64_t i = t + threadIdx.x; i < m; i += T) {
+        const float2 v = (i == t) ? make_float2(1.f, 0.f) : vtmp[i];
+        const f32x2 vh = pk2(v.x, v.x), vl = pk2(v.y, v.y);
+#pragma unroll
+        for (int k = 0; k < NP; ++k)
+            if (k < np) {
+                float2* p0 = c + (size_t)(2 * k) * m + i;
+                float2* p1 = c + (size_t)(2 * k + 1) * m + i;
+                const float2 x0 = *p0, x1 = *p1;
+                f32x2 xh = pk2(x0.x, x1.x), xl = pk2(x0.y, x1.y);
+                ff2_madd(vh, vl, bh[k], nbh[k], bl[k], xh, xl);
+                const float2 H = upk2(xh), L = upk2(xl);
+                *p0 = ff_norm(H.x, L.x);
+                if (2 * k + 1 < ncol) *p1 = ff_norm(H.y, L.y);
+            }
+    }
+    __syncthreads();
+    return true;
+}
+
+// VF and taug <- UNSET
+__global__ void unset_kernel(float2* __restrict__ p, int64_t count) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        reinterpret_cast<uint2*>(p)[i] = make_uint2(UNSET, 0u);
 }
 
 template <int OWNB>
@@ -320,84 +330,39 @@ __global__ void __launch_bounds__(T, 1) qr_ff_kernel(Args a) {
     extern __shared__ __align__(16) float2 sm[];
     __shared__ float2 red[W * 16];
     __shared__ float2 tot[16];
-    __shared__ float2 wsm[KB * KB];
-    __shared__ __align__(16) float2 tsm[KB * KB + KB];      // own T and taus while factoring
-    __shared__ __align__(16) float2 tin[KB * KB + KB];      // received T and taus
-    __shared__ __align__(8) uint64_t vbar;
     __shared__ int ok_s;
+    constexpr int NC = (OWNB * KB <= 4) ? 4 : (OWNB * KB <= 8) ? 8 : 16;   // columns one reflector updates
     const int64_t m = a.m, n = a.n, nc = a.nc, G = gridDim.x;
     float2* cols = sm;                                  // OWNB * KB columns of m
-    float2* vb = sm + (size_t)OWNB * KB * m;            // received reflector block, KB x ldv
-    const int64_t nblk = (nc + KB - 1) / KB, nref = (n + KB - 1) / KB;
+    float2* vtmp = sm + (size_t)OWNB * KB * m;          // one reflector (m)
+    const int64_t nblk = (nc + KB - 1) / KB;
     int64_t blk[OWNB];
-    int64_t last = -1;
+    int nown = 0;
 #pragma unroll
     for (int q = 0; q < OWNB; ++q) {
         blk[q] = (int64_t)blockIdx.x + q * G;
-        if (blk[q] < nblk) last = blk[q];
+        if (blk[q] < nblk) nown = q + 1;
     }
 #pragma unroll
     for (int q = 0; q < OWNB; ++q)
         for (int r = 0; r < KB; ++r) {
             const int64_t j = blk[q] * KB + r;
-            if (blk[q] < nblk)
-                for (int64_t i = threadIdx.x; i < m; i += T)
-                    cols[(size_t)(q * KB + r) * m + i] = (j < nc) ? ff_split(a.X[i + j * a.ld]) : make_float2(0.f, 0.f);
+            for (int64_t i = threadIdx.x; i < m; i += T)
+                cols[(size_t)(q * KB + r) * m + i] =
+                    (blk[q] < nblk && j < nc) ? ff_split(a.X[i + j * a.ld]) : make_float2(0.f, 0.f);
         }
-    if (threadIdx.x == 0) {
-        mbar_init(&vbar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
     __syncthreads();
-    volatile int quiet = 0;
-    if (blk[0] == 0 && nref > 0) factor_block(a, cols, 0, red, tot, tsm);
-    for (int64_t rb = 0; rb < nref && rb < last; ++rb) {
-        const int nr = (int)min((int64_t)KB, n - rb * KB);
-        // flag, then one bulk copy per reflector column (rows from the block head) and T
-        if (threadIdx.x == 0) {
-            ok_s = 1;
-            const volatile unsigned int* vf = a.flags + rb;
-            if (*vf == 0u) {
-                const unsigned long long t0 = globaltimer_ns();
-                unsigned int spins = 0;
-                while (*vf == 0u) {
-                    if (*((volatile unsigned int*)a.status) != 0u) { ok_s = 0; break; }
-                    if ((++spins & 255u) == 0u && globaltimer_ns() - t0 > MBAR_WAIT_NS) {
-                        fail_status(a.status);
-                        ok_s = 0;
-                        break;
-                    }
-                }
-            }
-            __threadfence();
-            if (ok_s) {
-                const int64_t r0 = (rb * KB) & ~1LL;                 // even row: 16-byte aligned
-                const uint32_t bytes = (uint32_t)((a.ldv - r0) * sizeof(float2));
-                mbar_expect_tx(&vbar, (uint32_t)nr * bytes + (uint32_t)sizeof(tin));
-                for (int r = 0; r < nr; ++r)
-                    bulk_g2s(vb + (size_t)r * a.ldv + r0, a.VF + (rb * KB + r) * a.ldv + r0, bytes, &vbar);
-                bulk_g2s(tin, a.TF + rb * (KB * KB + KB), (uint32_t)sizeof(tin), &vbar);
-                if (!mbar_wait(&vbar, (uint32_t)(rb & 1), &quiet)) {
-                    fail_status(a.status);
-                    ok_s = 0;
-                }
-            }
-        }
-        __syncthreads();
-        if (!ok_s) return;
-        int la = -1;
-#pragma unroll
-        for (int q = 0; q < OWNB; ++q)
-            if (blk[q] == rb + 1) la = q;
-        if (la >= 0) {
-            apply_block(vb, a.ldv, tin, rb, nr, cols + (size_t)la * KB * m, m, red, tot, wsm);
-            if (rb + 1 < nref) factor_block(a, cols + (size_t)la * KB * m, rb + 1, red, tot, tsm);
-        }
-#pragma unroll
-        for (int q = 0; q < OWNB; ++q)
-            if (q != la && blk[q] > rb && blk[q] < nblk)
-                apply_block(vb, a.ldv, tin, rb, nr, cols + (size_t)q * KB * m, m, red, tot, wsm);
-        __syncthreads();
+    // reflectors in order: each one to every block still held, the own
+    // block factored as soon as every earlier reflector is applied
+    int64_t t = 0;
+    for (int q = 0; q < nown; ++q) {
+        const int64_t t0 = blk[q] * KB;
+        const int64_t tend = min(t0, n);
+        float2* c = cols + (size_t)q * KB * m;
+        const int ncol = (nown - q) * KB;
+        for (; t < tend; ++t)
+            if (!apply_reflector<NC>(a, t, c, m, ncol, red, tot, vtmp, &ok_s)) return;
+        if (t0 < n) factor_block(a, c, blk[q], red, tot);
     }
 #pragma unroll
     for (int q = 0; q < OWNB; ++q)
@@ -483,12 +448,11 @@ static const void* qr_kernel() { return (const void*)qr_ff_kernel<OWNB>; }
 // Dynamic shared memory of the QR kernel: the owned blocks (stride m) and
 // one received reflector block (stride m rounded up to even).
 static size_t qr_ff_smem(int64_t ownb, int64_t m) {
-    return ((size_t)ownb * qrff::KB * m + (size_t)qrff::KB * ((m + 1) & ~1LL)) * sizeof(float2);
+    return ((size_t)ownb * qrff::KB * m + (size_t)m) * sizeof(float2);
 }
 
 // Owned column blocks per CTA for the float-float QR (0: does not fit): the
-// owned blocks and one received reflector block in shared memory, one CTA
-// per SM.
+// owned blocks and one reflector in shared memory, one CTA per SM.
 static int qr_ff_ownb(const Ctx& ctx, int64_t m, int64_t nc) {
     const int64_t nblk = (nc + qrff::KB - 1) / qrff::KB;
     const int64_t G = nblk < ctx.sm_count ? nblk : ctx.sm_count;
@@ -516,13 +480,19 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, T, smem));
     if ((int64_t)nb * ctx.sm_count < G) fail(RNLA_ERR_UNSUPPORTED, "float-float QR: grid not co-resident");
     cudaStream_t s = ctx.stream;
-    const int64_t nref = (n + KB - 1) / KB;
     const int64_t ldv = (m + 1) & ~1LL;
-    DevBuf<float2> VF((size_t)ldv * n, s), TF((size_t)nref * (KB * KB + KB), s);
-    DevBuf<unsigned int> flags(nref, s);
-    RNLA_CUDA(cudaMemsetAsync(flags.get(), 0, nref * sizeof(unsigned int), s));
+    DevBuf<float2> VF((size_t)ldv * n, s), taug(n, s);
+    {
+        const int64_t cnt = (int64_t)ldv * n;
+        int g = (int)div_up(cnt, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        unset_kernel<<<g, 256, 0, s>>>(VF, cnt);
+        RNLA_LAUNCH_CHECK();
+        unset_kernel<<<(unsigned)div_up(n, 256), 256, 0, s>>>(taug, n);
+        RNLA_LAUNCH_CHECK();
+    }
     ctx.clear_status();
-    Args a{X, m, n, nc, ld, ldv, VF.get(), TF.get(), flags.get(), ctx.status};
+    Args a{X, m, n, nc, ld, ldv, VF.get(), taug.get(), ctx.status};
     void* args[] = {&a};
     RNLA_CUDA(cudaLaunchCooperativeKernel(k, dim3((unsigned)G), dim3(T), args, smem, s));
     count_launch();
