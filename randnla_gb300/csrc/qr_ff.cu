@@ -231,17 +231,40 @@ __device__ void factor_block(const Args& a, float2* c, int64_t b, float2* red, f
 // from VF through L2 as it is written (each thread waits for its own
 // entries) into vtmp (shared, m entries).  One block reduction of the ncol
 // dots v_t^T c_q, one update sweep.  False if a wait failed (all threads
-// agree through *ok).
+// agree through ok[0..1], shared).
+// eager: this CTA owns the block right after the reflector's (critical
+// path): every thread loads as soon as it can.  Otherwise thread 0 first
+// waits, with back-off, for tau_t, so the CTAs with slack do not crowd the
+// L2 lines the critical CTA is reading.
 template <int NC>
 __device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, int ncol, float2* red,
-                                float2* tot, float2* vtmp, int* ok) {
+                                float2* tot, float2* vtmp, int* ok, bool eager) {
     constexpr int NP = NC / 2;               // column pairs (packed f32x2 arithmetic)
     float2 ct[NC];
 #pragma unroll
     for (int q = 0; q < NC; ++q)
         ct[q] = (q < ncol) ? c[(size_t)q * m + t] : make_float2(0.f, 0.f);   // read before the reduction's barrier
-    if (threadIdx.x == 0) *ok = 1;
+    if (threadIdx.x == 0) {
+        int okv = 1;
+        if (!eager) {
+            float2 tv = ld_relaxed_f2(a.taug + t);
+            const unsigned long long t0 = globaltimer_ns();
+            while (__float_as_uint(tv.x) == UNSET) {
+                __nanosleep(256);
+                if (*((volatile unsigned int*)a.status) != 0u) { okv = 0; break; }
+                if (globaltimer_ns() - t0 > MBAR_WAIT_NS) {
+                    atomicCAS(a.status, 0u, (unsigned int)KSTATUS_BARRIER_TIMEOUT);
+                    okv = 0;
+                    break;
+                }
+                tv = ld_relaxed_f2(a.taug + t);
+            }
+        }
+        ok[0] = okv;       // the wait above; read after the barrier below
+        ok[1] = 1;         // the loads below; cleared by any thread whose wait fails
+    }
     __syncthreads();
+    if (!ok[0]) return false;
     bool good = true;
     const int np = (ncol + 1) >> 1;
     f32x2 ah[NP], al[NP];
@@ -276,7 +299,7 @@ __device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, 
     }
     float2 tau;
     if (!ld_written(a, a.taug + t, tau)) good = false;
-    if (!good) *ok = 0;
+    if (!good) ok[1] = 0;
     float h[NC], l[NC];
 #pragma unroll
     for (int k = 0; k < NP; ++k) {
@@ -285,7 +308,7 @@ __device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, 
         h[2 * k + 1] = H.y; l[2 * k + 1] = L.y;
     }
     block_sums<NC>(h, l, red, tot);
-    if (!*ok) return false;
+    if (!ok[1]) return false;
     // c_q += f_q v over column pairs: b = (f_q, f_q+1)
     f32x2 bh[NP], nbh[NP], bl[NP];
 #pragma unroll
@@ -330,7 +353,7 @@ __global__ void __launch_bounds__(T, 1) qr_ff_kernel(Args a) {
     extern __shared__ __align__(16) float2 sm[];
     __shared__ float2 red[W * 16];
     __shared__ float2 tot[16];
-    __shared__ int ok_s;
+    __shared__ int ok_s[2];
     constexpr int NC = (OWNB * KB <= 4) ? 4 : (OWNB * KB <= 8) ? 8 : 16;   // columns one reflector updates
     const int64_t m = a.m, n = a.n, nc = a.nc, G = gridDim.x;
     float2* cols = sm;                                  // OWNB * KB columns of m
@@ -361,7 +384,7 @@ __global__ void __launch_bounds__(T, 1) qr_ff_kernel(Args a) {
         float2* c = cols + (size_t)q * KB * m;
         const int ncol = (nown - q) * KB;
         for (; t < tend; ++t)
-            if (!apply_reflector<NC>(a, t, c, m, ncol, red, tot, vtmp, &ok_s)) return;
+            if (!apply_reflector<NC>(a, t, c, m, ncol, red, tot, vtmp, ok_s, t >= t0 - KB)) return;
         if (t0 < n) factor_block(a, c, blk[q], red, tot);
     }
 #pragma unroll
