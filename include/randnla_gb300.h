@@ -296,6 +296,21 @@ RNLA_API int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_
                                        int64_t l, double sampling_factor, const rnla_options* opt,
                                        double* x_dev, rnla_stats* stats, void* stream);
 
+/* sketch_and_solve.rs:24-33 (qr) and :53-65 (svd): x (n) from the
+ * Gaussian sketch S (m/4 x m; generator and key of opt, Philox key 0 by
+ * default) of [a b]: thin QR of S a and x = R^-1 (Q^T S b), or the SVD
+ * S a = U Sigma V^T and x = V Sigma^+ U^T S b; an exactly zero pivot or
+ * singular value gives a zero component (solvers.rs:22-41, 56-70).
+ * opt->precision selects the FP64 data flow or the tensor-core sketch.
+ * RNLA_ERR_INVALID_DIMENSIONS when m/4 < n. */
+RNLA_API int rnla_sketched_least_squares_qr(const double* a, int64_t m, int64_t n, int64_t lda,
+                                            const double* b, const rnla_options* opt, double* x);
+RNLA_API int rnla_sketched_least_squares_svd(const double* a, int64_t m, int64_t n, int64_t lda,
+                                             const double* b, const rnla_options* opt, double* x);
+RNLA_API int rnla_sketched_least_squares_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n,
+                                             int64_t lda, const double* b_dev, int32_t use_svd,
+                                             const rnla_options* opt, double* x_dev, void* stream);
+
 /* ---- building blocks exposed for parity tests (device pointers) ---- */
 
 /* Y (ldy) = S X: the sketch S (d x m, Gaussian, generator rng) applied to

@@ -447,6 +447,39 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_
     return (x, iters) if return_iters else x
 
 
+def sketched_least_squares_qr(a, b, S=None):
+    """sketch_and_solve.rs:24-33: Gaussian sketch S (m/4 x m, Philox key 0
+    by default), thin QR of S a, x = R^-1 Q^T S b with the zero-pivot rule
+    of solvers.rs:22-41.  Returns x (n)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    m, n = a.shape
+    d = m // 4
+    if d < n:
+        raise ValueError("InvalidDimensions")
+    if S is None:
+        S = sketch(DIST_GAUSSIAN, d, m)
+    q, r = np.linalg.qr(S @ a, mode="reduced")
+    return solve_upper_triangular_system(r, q.T @ (S @ b))
+
+
+def sketched_least_squares_svd(a, b, S=None):
+    """sketch_and_solve.rs:53-65: SVD of S a, x = V Sigma^+ U^T S b, a zero
+    singular value giving a zero component (solvers.rs:56-70).  Returns x (n)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    m, n = a.shape
+    d = m // 4
+    if d < n:
+        raise ValueError("InvalidDimensions")
+    if S is None:
+        S = sketch(DIST_GAUSSIAN, d, m)
+    u, sig, vt = np.linalg.svd(S @ a, full_matrices=False)
+    y = u.T @ (S @ b)
+    y = np.where(sig != 0.0, y / np.where(sig != 0.0, sig, 1.0), 0.0)
+    return vt.T @ y
+
+
 def _upper_inverse(r):
     """R^-1 of an upper-triangular R column by column (solve R X = I),
     as sketch_and_precondition.rs:55 does with solve_upper_triangular."""

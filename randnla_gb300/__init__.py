@@ -30,8 +30,8 @@ from ._lib import Options, Rng, Stats, LsqrResult
 __all__ = [
     "DistributionType", "Precision", "Mode", "InnerSolver", "Generator", "RandNLAError",
     "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd",
-    "blendenpik_overdetermined", "cgls", "lsqr", "solve_upper_triangular_system", "options",
-    "lib",
+    "blendenpik_overdetermined", "sketched_least_squares_qr", "sketched_least_squares_svd", "cgls",
+    "lsqr", "solve_upper_triangular_system", "options", "lib",
 ]
 
 
@@ -289,6 +289,29 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, opts=None, retu
 
 
 # ---------------------------------------------------------------------------
+# sketch_and_solve.rs
+# ---------------------------------------------------------------------------
+def _sketched_ls(entry, a, b, opts):
+    a = _f64(a)
+    m, n = a.shape
+    b = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(-1))
+    x = np.zeros(n)
+    o = opts if opts is not None else options()
+    _check(entry(_ptr(a), m, n, max(m, 1), _ptr(b), ctypes.byref(o), _ptr(x)))
+    return x.reshape(-1, 1)
+
+
+def sketched_least_squares_qr(a, b, opts=None):
+    """src/sketch_and_solve.rs:24-33: QR of the m/4-row Gaussian sketch.  Returns x (n x 1)."""
+    return _sketched_ls(lib().rnla_sketched_least_squares_qr, a, b, opts)
+
+
+def sketched_least_squares_svd(a, b, opts=None):
+    """src/sketch_and_solve.rs:53-65: SVD of the m/4-row Gaussian sketch.  Returns x (n x 1)."""
+    return _sketched_ls(lib().rnla_sketched_least_squares_svd, a, b, opts)
+
+
+# ---------------------------------------------------------------------------
 # Device-pointer forms (torch CUDA tensors, current torch stream)
 # ---------------------------------------------------------------------------
 def _stream():
@@ -319,6 +342,17 @@ def blendenpik_dev(a, b, x, epsilon, l, sampling_factor, opts=None):
         _dptr(a), int(a.dtype == torch.float32), m, n, _ld(a), _dptr(b), epsilon, l, sampling_factor,
         ctypes.byref(o), _dptr(x), ctypes.byref(st), _stream()))
     return st.as_dict()
+
+
+def sketched_least_squares_dev(a, b, x, use_svd=False, opts=None):
+    """rnla_sketched_least_squares_dev on torch CUDA tensors (a: m x n
+    float64/float32 column-major, b: m float64, x: n float64 output)."""
+    import torch
+    o = opts if opts is not None else options()
+    m, n = a.shape
+    _check(lib().rnla_sketched_least_squares_dev(_dptr(a), int(a.dtype == torch.float32), m, n, _ld(a),
+                                                 _dptr(b), int(bool(use_svd)), ctypes.byref(o), _dptr(x),
+                                                 _stream()))
 
 
 def rand_svd_dev(a, k, epsilon, s, U, sigma, Vt, opts=None):

@@ -421,6 +421,82 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     }
 }
 
+// zero the strict lower triangle of an n x n matrix
+__global__ void zero_lower_kernel(double* __restrict__ a, int64_t n, int64_t ld) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < n * n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % n, j = idx / n;
+        if (i > j) a[i + j * ld] = 0.0;
+    }
+}
+
+// y_i <- y_i / sigma_i, 0 where sigma_i == 0 (solvers.rs:56-70)
+__global__ void divide_sigma_kernel(double* __restrict__ y, const double* __restrict__ sigma, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y[i] = (sigma[i] != 0.0) ? y[i] / sigma[i] : 0.0;
+}
+
+// sketch_and_solve.rs:24-33 / 53-65.  [S a, S b] in one d x (n+1) block
+// (d = m / 4); its Householder QR gives R and Q^T S b in column n.  The SVD
+// variant factors R = U_R Sigma V^T: the SVD of S a is (Q U_R) Sigma V^T,
+// so U^T S b = U_R^T (Q^T S b).
+static void sketch_solve_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
+                              const double* b, bool use_svd, const rnla_options& o, double* x,
+                              const ColumnFeed* feed) {
+    if (m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    const int64_t d = m / 4;
+    if (d < n) fail(RNLA_ERR_INVALID_DIMENSIONS, "the sketch has m / 4 rows; it needs at least n");
+    const RngKey key = key_of(&o.rng);
+    const int64_t nc = n + 1;
+    DevBuf<double> SK((size_t)d * nc, ctx.stream);
+    if (o.precision == RNLA_PREC_FP64) {
+        if (feed) feed->wait_all(ctx.stream);
+        DevBuf<double> S((size_t)d * m, ctx.stream);
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key, d, m, S, d);
+        DevBuf<double> Aw;
+        const double* A = static_cast<const double*>(Av);
+        int64_t ld = lda;
+        if (a_f32) {
+            Aw.alloc((size_t)m * n, ctx.stream);
+            copy_matrix_f32_to_f64(ctx, m, n, static_cast<const float*>(Av), lda, Aw, m);
+            A = Aw.get();
+            ld = m;
+        }
+        gemm_f64(ctx, 'N', 'N', d, n, m, 1.0, S, d, A, ld, 0.0, SK, d);
+        gemm_f64(ctx, 'N', 'N', d, 1, m, 1.0, S, d, b, m, 0.0, SK.get() + n * d, d);
+    } else {
+        if (!tc_available(ctx))
+            fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed);
+        if (feed) feed->wait_all(ctx.stream);
+    }
+    if (o.precision != RNLA_PREC_FP64 && qr_ff_supported(ctx, d, n, nc)) {
+        householder_qr_ff(ctx, SK, d, n, nc, d);
+    } else {
+        DevBuf<double> tau(n, ctx.stream);
+        householder_qr(ctx, SK, d, n, nc, d, tau);
+    }
+    const double* z = SK.get() + n * d;          // (Q^T S b)[:n]
+    if (!use_svd) {
+        upper_solve_skip_zero(ctx, SK, n, d, z, x);
+        return;
+    }
+    DevBuf<double> R((size_t)n * n, ctx.stream), U((size_t)n * n, ctx.stream), V((size_t)n * n, ctx.stream),
+        sig(n, ctx.stream), y(n, ctx.stream);
+    copy_matrix(ctx, n, n, SK, d, R, n);
+    {
+        int g = (int)div_up(n * n, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        zero_lower_kernel<<<g, 256, 0, ctx.stream>>>(R, n, n);
+        RNLA_LAUNCH_CHECK();
+    }
+    small_svd(ctx, R, n, n, n, U, n, sig, V, n);
+    gemm_f64(ctx, 'T', 'N', n, 1, n, 1.0, U, n, z, d, 0.0, y, n);
+    divide_sigma_kernel<<<(unsigned)div_up(n, 256), 256, 0, ctx.stream>>>(y, sig, n);
+    RNLA_LAUNCH_CHECK();
+    gemm_f64(ctx, 'N', 'N', n, 1, n, 1.0, V, n, y, n, 0.0, x, n);
+}
+
 }  // namespace rnla
 
 using namespace rnla;
@@ -733,6 +809,46 @@ int rnla_blendenpik_overdetermined(const double* a, int64_t m, int64_t n, int64_
                                    double epsilon, int64_t l, double sampling_factor, double* x) {
     return rnla_blendenpik_overdetermined_ex(a, m, n, lda, b, epsilon, l, sampling_factor, nullptr, x,
                                              nullptr);
+}
+
+int rnla_sketched_least_squares_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n, int64_t lda,
+                                    const double* b_dev, int32_t use_svd, const rnla_options* opt,
+                                    double* x_dev, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    Ctx ctx((cudaStream_t)stream);
+    const rnla_options o = opts_or_default(opt);
+    sketch_solve_impl(ctx, a_dev, a_is_f32 != 0, m, n, lda, b_dev, use_svd != 0, o, x_dev, nullptr);
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_API_END
+}
+
+static int sketched_ls_host(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, bool use_svd,
+                            const rnla_options* opt, double* x) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    if (m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
+    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    ColumnFeed feed;
+    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
+    Ctx ctx(s);
+    const rnla_options o = opts_or_default(opt);
+    sketch_solve_impl(ctx, A.get(), false, m, n, m, B, use_svd, o, X, &feed);
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_sketched_least_squares_qr(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                                   const rnla_options* opt, double* x) {
+    return sketched_ls_host(a, m, n, lda, b, false, opt, x);
+}
+
+int rnla_sketched_least_squares_svd(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                                    const rnla_options* opt, double* x) {
+    return sketched_ls_host(a, m, n, lda, b, true, opt, x);
 }
 
 // ---- building blocks ----

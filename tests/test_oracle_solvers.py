@@ -126,3 +126,20 @@ def test_sketch_rows_rule():
     assert O.sketch_rows(100, 10, 1.5) == 15
     assert O.sketch_rows(100, 80, 1.5) == 100
     assert O.sketch_rows(100000, 500, 4.0) == 2000
+
+
+def test_sketched_least_squares_restatements_agree():
+    """sketch_and_solve.rs:24-33 and :53-65 solve the same sketched problem:
+    with the same sketch, QR and SVD give the same x; both come close to the
+    full least-squares residual (d = m/4 = 250 rows for n = 20)."""
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((1000, 20))
+    y = A @ rng.uniform(-100, 100, 20)
+    A = A + 0.01 * rng.standard_normal(A.shape)
+    xq = O.sketched_least_squares_qr(A, y)
+    xs = O.sketched_least_squares_svd(A, y)
+    assert np.linalg.norm(xq - xs) <= 1e-9 * np.linalg.norm(xq)
+    xl = np.linalg.lstsq(A, y, rcond=None)[0]
+    assert np.linalg.norm(A @ xq - y) <= 1.6 * np.linalg.norm(A @ xl - y)
+    with pytest.raises(ValueError):
+        O.sketched_least_squares_qr(A[:40], y[:40])
