@@ -296,6 +296,24 @@ RNLA_API int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_
                                        int64_t l, double sampling_factor, const rnla_options* opt,
                                        double* x_dev, rnla_stats* stats, void* stream);
 
+/* sketch_and_precondition.rs:82-119 (lsrn): the same sketch as blendenpik,
+ * preconditioner N = V Sigma^-1 from the SVD of S a, CGLS on A N from 0,
+ * x = N y.  Built on the QR of S a: with R = U_R Sigma V^T, N = R^-1 U_R, and
+ * CGLS on A R^-1 U_R from 0 is CGLS on A R^-1 from 0 rotated by U_R^T, so
+ * x = R^-1 z with z from CGLS (or LSQR, opt->inner_solver) on A R^-1
+ * started at 0.  An exactly singular sketch returns RNLA_ERR_SINGULAR_MATRIX
+ * (the reference would drop the zero singular directions). */
+RNLA_API int rnla_lsrn_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                                      double epsilon, int64_t l, double sampling_factor, double* x);
+RNLA_API int rnla_lsrn_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda,
+                                         const double* b, double epsilon, int64_t l,
+                                         double sampling_factor, const rnla_options* opt, double* x,
+                                         rnla_stats* stats);
+RNLA_API int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n,
+                                          int64_t lda, const double* b_dev, double epsilon, int64_t l,
+                                          double sampling_factor, const rnla_options* opt, double* x_dev,
+                                          rnla_stats* stats, void* stream);
+
 /* sketch_and_solve.rs:24-33 (qr) and :53-65 (svd): x (n) from the
  * Gaussian sketch S (m/4 x m; generator and key of opt, Philox key 0 by
  * default) of [a b]: thin QR of S a and x = R^-1 (Q^T S b), or the SVD

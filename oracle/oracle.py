@@ -447,6 +447,28 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_
     return (x, iters) if return_iters else x
 
 
+def lsrn_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_iters=False):
+    """sketch_and_precondition.rs:82-119: the blendenpik sketch, N = V Sigma^+
+    from the SVD of S a (zero singular values give zero), CGLS on the
+    explicit A N from y = 0, x = N y."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    m, n = a.shape
+    if m < n:
+        raise ValueError("NotOverdetermined")
+    if sampling_factor < 1.0 or not epsilon > 0.0 or l == 0:
+        raise InvalidParameters("invalid lsrn parameters")
+    d = sketch_rows(m, n, sampling_factor)
+    if S is None:
+        S = sketch(DIST_GAUSSIAN, d, m)
+    _, sig, vt = np.linalg.svd(S @ a, full_matrices=False)
+    sinv = np.where(sig != 0.0, 1.0 / np.where(sig != 0.0, sig, 1.0), 0.0)
+    N = vt.T * sinv
+    y, iters = cgls(a @ N, b, epsilon, l, np.zeros(N.shape[1]), return_iters=True)
+    x = N @ y
+    return (x, iters) if return_iters else x
+
+
 def sketched_least_squares_qr(a, b, S=None):
     """sketch_and_solve.rs:24-33: Gaussian sketch S (m/4 x m, Philox key 0
     by default), thin QR of S a, x = R^-1 Q^T S b with the zero-pivot rule

@@ -30,7 +30,8 @@ from ._lib import Options, Rng, Stats, LsqrResult
 __all__ = [
     "DistributionType", "Precision", "Mode", "InnerSolver", "Generator", "RandNLAError",
     "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd",
-    "blendenpik_overdetermined", "sketched_least_squares_qr", "sketched_least_squares_svd", "cgls",
+    "blendenpik_overdetermined", "lsrn_overdetermined", "sketched_least_squares_qr",
+    "sketched_least_squares_svd", "cgls",
     "lsqr", "solve_upper_triangular_system", "options", "lib",
 ]
 
@@ -285,6 +286,19 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, opts=None, retu
     _check(lib().rnla_blendenpik_overdetermined_ex(_ptr(a), m, n, max(m, 1), _ptr(b), epsilon, l,
                                                    sampling_factor, ctypes.byref(o), _ptr(x),
                                                    ctypes.byref(st)))
+    return (x.reshape(-1, 1), st.as_dict()) if return_stats else x.reshape(-1, 1)
+
+
+def lsrn_overdetermined(a, b, epsilon, l, sampling_factor, opts=None, return_stats=False):
+    """src/sketch_and_precondition.rs:82-119.  Returns x (n x 1)."""
+    a = _f64(a)
+    m, n = a.shape
+    b = np.ascontiguousarray(np.asarray(b, dtype=np.float64).reshape(-1))
+    x = np.zeros(n)
+    o = opts if opts is not None else options()
+    st = Stats()
+    _check(lib().rnla_lsrn_overdetermined_ex(_ptr(a), m, n, max(m, 1), _ptr(b), epsilon, l,
+                                             sampling_factor, ctypes.byref(o), _ptr(x), ctypes.byref(st)))
     return (x.reshape(-1, 1), st.as_dict()) if return_stats else x.reshape(-1, 1)
 
 

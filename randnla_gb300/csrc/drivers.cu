@@ -316,10 +316,13 @@ static void blendenpik_validate(int64_t m, int64_t n, double epsilon, int64_t l,
 // With a feed, A is still arriving from the host in column chunks: the
 // tensor-core sketch consumes each column tile as it lands; every other
 // path waits for the whole matrix first.
+// lsrn (sketch_and_precondition.rs:82-119) is the same pipeline started
+// from z0 = 0: its preconditioner V Sigma^-1 is R^-1 U_R, and the Krylov
+// solvers are invariant under the orthogonal U_R.
 static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
                             const double* b, double epsilon, int64_t l, double sf,
                             const rnla_options& o, double* x, rnla_stats* st,
-                            const ColumnFeed* feed = nullptr) {
+                            const ColumnFeed* feed = nullptr, bool lsrn = false) {
     blendenpik_validate(m, n, epsilon, l, sf);
     const int64_t d = sketch_rows(m, n, sf);
     if (d < n) fail(RNLA_ERR_SINGULAR_MATRIX, "sketch has fewer rows than columns");
@@ -373,7 +376,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     }
     if (!inv_ok) fail(RNLA_ERR_SINGULAR_MATRIX, "the R factor of the sketch is singular");
     tm.mark();
-    const double* z0 = SK.get() + n * d;
+    const double* z0 = lsrn ? nullptr : SK.get() + n * d;
     DevBuf<double> z(n, ctx.stream);
     const double* a64 = a_f32 ? nullptr : static_cast<const double*>(Av);
     const float* a32 = a_f32 ? static_cast<const float*>(Av) : nullptr;
@@ -809,6 +812,45 @@ int rnla_blendenpik_overdetermined(const double* a, int64_t m, int64_t n, int64_
                                    double epsilon, int64_t l, double sampling_factor, double* x) {
     return rnla_blendenpik_overdetermined_ex(a, m, n, lda, b, epsilon, l, sampling_factor, nullptr, x,
                                              nullptr);
+}
+
+int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n, int64_t lda,
+                                 const double* b_dev, double epsilon, int64_t l, double sampling_factor,
+                                 const rnla_options* opt, double* x_dev, rnla_stats* stats, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    Ctx ctx((cudaStream_t)stream);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    blendenpik_impl(ctx, a_dev, a_is_f32 != 0, m, n, lda, b_dev, epsilon, l, sampling_factor, o, x_dev,
+                    stats, nullptr, true);
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_API_END
+}
+
+int rnla_lsrn_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                                double epsilon, int64_t l, double sampling_factor, const rnla_options* opt,
+                                double* x, rnla_stats* stats) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    blendenpik_validate(m, n, epsilon, l, sampling_factor);
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
+    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
+    ColumnFeed feed;
+    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
+    Ctx ctx(s);
+    const rnla_options o = opts_or_default(opt);
+    if (stats) memset(stats, 0, sizeof *stats);
+    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed, true);
+    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
+int rnla_lsrn_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
+                             double epsilon, int64_t l, double sampling_factor, double* x) {
+    return rnla_lsrn_overdetermined_ex(a, m, n, lda, b, epsilon, l, sampling_factor, nullptr, x, nullptr);
 }
 
 int rnla_sketched_least_squares_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n, int64_t lda,

@@ -143,3 +143,17 @@ def test_sketched_least_squares_restatements_agree():
     assert np.linalg.norm(A @ xq - y) <= 1.6 * np.linalg.norm(A @ xl - y)
     with pytest.raises(ValueError):
         O.sketched_least_squares_qr(A[:40], y[:40])
+
+
+def test_lsrn_restatement_converges():
+    """sketch_and_precondition.rs:82-119 restated: on a well-posed problem the
+    V Sigma^+ preconditioned CGLS reaches the least-squares residual."""
+    rng = np.random.default_rng(9)
+    A = O.make_lowrank_test_matrix(1500, 30, np.logspace(0, -6, 30), 1, 2)
+    b = A @ rng.standard_normal(30) + 1e-6 * rng.standard_normal(1500)
+    x, it = O.lsrn_overdetermined(A, b, 1e-12, 500, 4.0, return_iters=True)
+    xl = np.linalg.lstsq(A, b, rcond=None)[0]
+    r = np.linalg.norm(A @ x - b) / np.linalg.norm(b)
+    rl = np.linalg.norm(A @ xl - b) / np.linalg.norm(b)
+    assert abs(r - rl) < 1e-10
+    assert it < 100
