@@ -314,6 +314,21 @@ RNLA_API int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, i
                                           double sampling_factor, const rnla_options* opt, double* x_dev,
                                           rnla_stats* stats, void* stream);
 
+/* cqrrpt.rs:27-58 (sap_chol_qrcp): Gaussian sketch S (d x m, n <= d <= m) of
+ * a, column-pivoted Householder QR of S a (pivot_decompositions.rs:106-174:
+ * largest remaining column norm, first index on ties), then CholeskyQR of
+ * a[:, jpvt] R_sk^-1:  a[:, jpvt] = Q R with Q m x n (orthonormal columns),
+ * R n x n upper triangular, jpvt the column order (n entries).  Errors:
+ * RNLA_ERR_INVALID_PARAMETERS unless n <= d <= m; RNLA_ERR_SINGULAR_MATRIX
+ * when the sketch's numerical rank (|R_ii| > 1e-10) is below n;
+ * RNLA_ERR_MATRIX_DECOMPOSITION when the Cholesky factorization fails. */
+RNLA_API int rnla_sap_chol_qrcp(const double* a, int64_t m, int64_t n, int64_t lda, int64_t d,
+                                const rnla_options* opt, double* q, int64_t ldq, double* r, int64_t ldr,
+                                int64_t* jpvt);
+RNLA_API int rnla_sap_chol_qrcp_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda, int64_t d,
+                                    const rnla_options* opt, double* q_dev, int64_t ldq, double* r_dev,
+                                    int64_t ldr, int64_t* jpvt_dev, void* stream);
+
 /* sketch_and_solve.rs:24-33 (qr) and :53-65 (svd): x (n) from the
  * Gaussian sketch S (m/4 x m; generator and key of opt, Philox key 0 by
  * default) of [a b]: thin QR of S a and x = R^-1 (Q^T S b), or the SVD

@@ -469,6 +469,59 @@ def lsrn_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_iters=
     return (x, iters) if return_iters else x
 
 
+def qrcp(a):
+    """pivot_decompositions.rs:106-174 restated: greedy column pivoting by the
+    largest remaining norm (strictly larger moves; the first index keeps ties),
+    Householder v = x + sign(x_0) ||x|| e_0 normalised, c -= 2 v (v^T c) on the
+    columns from k on, norms of the later columns recomputed below row k.
+    Returns (r, p): r the reflected matrix (R in its upper triangle), p the
+    column order."""
+    r = np.array(a, dtype=np.float64, copy=True)
+    m, n = r.shape
+    p = list(range(n))
+    norms = [float(np.linalg.norm(r[:, j])) for j in range(n)]
+    for k in range(min(m, n)):
+        best, bi = norms[k], k
+        for j in range(k + 1, n):
+            if norms[j] > best:
+                best, bi = norms[j], j
+        if bi != k:
+            r[:, [k, bi]] = r[:, [bi, k]]
+            p[k], p[bi] = p[bi], p[k]
+            norms[k], norms[bi] = norms[bi], norms[k]
+        x = r[k:, k].copy()
+        nx = float(np.linalg.norm(x))
+        if nx != 0.0:
+            v = x
+            v[0] += nx if v[0] >= 0.0 else -nx
+            v /= np.linalg.norm(v)
+            r[k:, k:] -= 2.0 * np.outer(v, v @ r[k:, k:])
+            for j in range(k + 1, n):
+                norms[j] = float(np.linalg.norm(r[k + 1:, j]))
+    return r, p
+
+
+def sap_chol_qrcp(a, d, S=None):
+    """cqrrpt.rs:27-58 restated: QRCP of the d x m Gaussian sketch of a, then
+    CholeskyQR of a[:, p] R_sk^-1.  Returns (q, r, p) with a[:, p] = q r
+    (r upper triangular, the sketch's R taken from its upper triangle)."""
+    a = np.asarray(a, dtype=np.float64)
+    m, n = a.shape
+    if not (n <= d <= m):
+        raise InvalidParameters("d must satisfy n <= d << m")
+    if S is None:
+        S = sketch(DIST_GAUSSIAN, d, m)
+    r_sk, p = qrcp(S @ a)
+    k = sum(1 for i in range(min(d, n)) if abs(r_sk[i, i]) > 1e-10)
+    if k < n:
+        raise ValueError("SingularMatrix")
+    rk = np.triu(r_sk[:n, :n])
+    a_pre = a[:, p] @ _upper_inverse(rk)
+    r_pre = np.linalg.cholesky(a_pre.T @ a_pre).T
+    q = a_pre @ _upper_inverse(r_pre)
+    return q, r_pre @ rk, p
+
+
 def sketched_least_squares_qr(a, b, S=None):
     """sketch_and_solve.rs:24-33: Gaussian sketch S (m/4 x m, Philox key 0
     by default), thin QR of S a, x = R^-1 Q^T S b with the zero-pivot rule

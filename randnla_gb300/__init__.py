@@ -30,7 +30,7 @@ from ._lib import Options, Rng, Stats, LsqrResult
 __all__ = [
     "DistributionType", "Precision", "Mode", "InnerSolver", "Generator", "RandNLAError",
     "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd",
-    "blendenpik_overdetermined", "lsrn_overdetermined", "sketched_least_squares_qr",
+    "blendenpik_overdetermined", "lsrn_overdetermined", "sap_chol_qrcp", "sketched_least_squares_qr",
     "sketched_least_squares_svd", "cgls",
     "lsqr", "solve_upper_triangular_system", "options", "lib",
 ]
@@ -300,6 +300,22 @@ def lsrn_overdetermined(a, b, epsilon, l, sampling_factor, opts=None, return_sta
     _check(lib().rnla_lsrn_overdetermined_ex(_ptr(a), m, n, max(m, 1), _ptr(b), epsilon, l,
                                              sampling_factor, ctypes.byref(o), _ptr(x), ctypes.byref(st)))
     return (x.reshape(-1, 1), st.as_dict()) if return_stats else x.reshape(-1, 1)
+
+
+# ---------------------------------------------------------------------------
+# cqrrpt.rs
+# ---------------------------------------------------------------------------
+def sap_chol_qrcp(a, d, opts=None):
+    """src/cqrrpt.rs:27-58.  Returns (q m x n, r n x n, j) with a[:, j] = q r."""
+    a = _f64(a)
+    m, n = a.shape
+    q = np.zeros((m, n), order="F")
+    r = np.zeros((n, n), order="F")
+    j = np.zeros(n, dtype=np.int64)
+    o = opts if opts is not None else options()
+    _check(lib().rnla_sap_chol_qrcp(_ptr(a), m, n, max(m, 1), d, ctypes.byref(o), _ptr(q), max(m, 1),
+                                    _ptr(r), max(n, 1), _ptr(j)))
+    return q, r, [int(v) for v in j]
 
 
 # ---------------------------------------------------------------------------

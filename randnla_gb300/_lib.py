@@ -102,6 +102,10 @@ SIGNATURES = [
     ("rnla_lsrn_overdetermined_dev", ctypes.c_int,
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
       ctypes.POINTER(Stats), c_vp]),
+    ("rnla_sap_chol_qrcp", ctypes.c_int,
+     [c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.POINTER(Options), c_vp, c_i64, c_vp, c_i64, c_vp]),
+    ("rnla_sap_chol_qrcp_dev", ctypes.c_int,
+     [c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.POINTER(Options), c_vp, c_i64, c_vp, c_i64, c_vp, c_vp]),
     ("rnla_sketched_least_squares_qr", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_vp, ctypes.POINTER(Options), c_vp]),
     ("rnla_sketched_least_squares_svd", ctypes.c_int,

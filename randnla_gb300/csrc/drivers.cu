@@ -865,6 +865,41 @@ int rnla_sketched_least_squares_dev(const void* a_dev, int32_t a_is_f32, int64_t
     RNLA_API_END
 }
 
+int rnla_sap_chol_qrcp_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda, int64_t d,
+                           const rnla_options* opt, double* q_dev, int64_t ldq, double* r_dev, int64_t ldr,
+                           int64_t* jpvt_dev, void* stream) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    check_mat(m, n, ldq);
+    check_mat(n, n, ldr);
+    Ctx ctx((cudaStream_t)stream);
+    const rnla_options o = opts_or_default(opt);
+    sap_chol_qrcp(ctx, key_of(&o.rng), o.precision, o.digits_a, a_dev, m, n, lda, d, q_dev, ldq, r_dev, ldr,
+                  jpvt_dev);
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    RNLA_API_END
+}
+
+int rnla_sap_chol_qrcp(const double* a, int64_t m, int64_t n, int64_t lda, int64_t d, const rnla_options* opt,
+                       double* q, int64_t ldq, double* r, int64_t ldr, int64_t* jpvt) {
+    RNLA_API_BEGIN
+    check_mat(m, n, lda);
+    check_mat(m, n, ldq);
+    check_mat(n, n, ldr);
+    cudaStream_t s = host_stream();
+    DevBuf<double> A((size_t)m * n, s), Q((size_t)m * n, s), R((size_t)n * n, s);
+    DevBuf<int64_t> J(n, s);
+    h2d_matrix(A, m, a, lda, m, n, s);
+    Ctx ctx(s);
+    const rnla_options o = opts_or_default(opt);
+    sap_chol_qrcp(ctx, key_of(&o.rng), o.precision, o.digits_a, A, m, n, m, d, Q, m, R, n, J);
+    d2h_matrix(q, ldq, Q, m, m, n, s);
+    d2h_matrix(r, ldr, R, n, n, n, s);
+    RNLA_CUDA(cudaMemcpyAsync(jpvt, J.get(), n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    RNLA_CUDA(cudaStreamSynchronize(s));
+    RNLA_API_END
+}
+
 static int sketched_ls_host(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, bool use_svd,
                             const rnla_options* opt, double* x) {
     RNLA_API_BEGIN

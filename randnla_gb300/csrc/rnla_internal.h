@@ -69,6 +69,15 @@ void full_piv_lu_l(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx,
 void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U,
                int64_t ldu, double* sigma, double* V, int64_t ldv);
 
+// ---- pivoted QR and CQRRPT (cqrrpt.cu) ----
+// Column-pivoted Householder QR of R (d x n, in place), the reference's
+// greedy largest-remaining-norm rule; jpvt (device, n) receives the order.
+void qrcp(Ctx& ctx, double* R, int64_t d, int64_t n, int64_t ld, int64_t* jpvt);
+// cqrrpt.rs:27-58 on device data: Q (m x n), R (n x n), jpvt (device, n).
+void sap_chol_qrcp(Ctx& ctx, const RngKey& key, int precision, int digits, const double* A, int64_t m,
+                   int64_t n, int64_t lda, int64_t d, double* Q, int64_t ldq, double* R, int64_t ldr,
+                   int64_t* jpvt_dev);
+
 // ---- iterative solvers (iterative.cu) ----
 struct LsqrParams {
     double damp = 0.0, atol = 1e-8, btol = 1e-8, conlim = 1e8;

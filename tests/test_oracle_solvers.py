@@ -157,3 +157,23 @@ def test_lsrn_restatement_converges():
     rl = np.linalg.norm(A @ xl - b) / np.linalg.norm(b)
     assert abs(r - rl) < 1e-10
     assert it < 100
+
+
+def test_qrcp_and_cqrrpt_restatements():
+    """pivot_decompositions.rs:106-174 and cqrrpt.rs:27-58 restated: the
+    pivoted R has non-increasing |R_kk| and R^T R = (a P)^T (a P); CQRRPT
+    gives orthonormal q with a[:, p] = q r."""
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal((300, 12)) * np.logspace(0, -3, 12)
+    r, p = O.qrcp(a)
+    R = np.triu(r[:12, :12])
+    assert sorted(p) == list(range(12))
+    assert np.all(np.diff(np.abs(np.diag(R))) <= 1e-12)
+    ap = a[:, p]
+    np.testing.assert_allclose(R.T @ R, ap.T @ ap, rtol=0, atol=1e-10)
+    q, rr, pp = O.sap_chol_qrcp(a, 60)
+    np.testing.assert_allclose(q.T @ q, np.eye(12), atol=1e-10)
+    np.testing.assert_allclose(q @ rr, a[:, pp], atol=1e-10)
+    assert np.allclose(np.tril(rr, -1), 0.0)
+    with pytest.raises(O.InvalidParameters):
+        O.sap_chol_qrcp(a, 5)
