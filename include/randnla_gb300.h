@@ -252,6 +252,22 @@ RNLA_API int rnla_qb1(const double* a, int64_t m, int64_t n, int64_t lda, int64_
  * mode (lora_drivers.rs:51 with the shapes of lora_helpers.rs:58-105). */
 RNLA_API int64_t rnla_rand_svd_rank(int64_t m, int64_t n, int64_t k, int64_t s, int32_t mode);
 
+/* lora_drivers.rs:84-140 (rand_evd1): a (n x n, symmetric) ~ V diag(lambda)
+ * V^T from QB1(a, k + s) and the eigenpairs of C = B Q, ordered by
+ * decreasing |lambda|; r = min(k, columns of Q) pairs.  v: n x k (ldv),
+ * lambda: k.  Errors: InvalidParameters (k, epsilon, s), NotHermitian (a
+ * differs from its transpose). */
+RNLA_API int rnla_rand_evd1(const double* a, int64_t n, int64_t lda, int64_t k, double epsilon, int64_t s,
+                            double* v, int64_t ldv, double* lambda, int64_t* r_out);
+/* lora_drivers.rs:153-213 (rand_evd2): Nystrom approximation of a PSD a
+ * with the shift nu = sqrt(n) eps ||a S||_F, S = tsog1(a, k + s, 3, 1);
+ * lambda = sigma^2 - nu of the singular values of (a S + nu S) R^-1 above the
+ * shift, r <= k of them.  Errors: InvalidParameters (k),
+ * NotPositiveSemiDefinite (an eigenvalue of a below 0),
+ * MatrixDecompositionError (the Cholesky factorization fails). */
+RNLA_API int rnla_rand_evd2(const double* a, int64_t n, int64_t lda, int64_t k, int64_t s, double* v,
+                            int64_t ldv, double* lambda, int64_t* r_out);
+
 /* lora_drivers::rand_svd (src/lora_drivers.rs:30-69): U (m x r), S (r x r,
  * diagonal, singular values descending), Vt (r x n).  Errors (checked in
  * this order, lora_drivers.rs:31-45): k == 0, epsilon <= 0, s == 0 ->

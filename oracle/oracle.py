@@ -417,6 +417,44 @@ def rand_svd(A, k, epsilon, s):
     return Q @ U[:, :r], np.diag(sig[:r]), Vt[:r, :]
 
 
+def rand_evd1(A, k, epsilon, s):
+    """lora_drivers.rs:84-140 restated: QB1(A, k + s), the eigenpairs of
+    C = B Q by decreasing |lambda|, V = Q U for the first min(k, cols) pairs."""
+    A = np.asarray(A, dtype=np.float64)
+    if k == 0 or not epsilon > 0.0 or s == 0:
+        raise InvalidParameters("invalid rand_evd1 parameters")
+    if not np.array_equal(A, A.T):
+        raise ValueError("NotHermitian")
+    Q, B = qb1(A, k + s, epsilon)
+    w, U = np.linalg.eigh(B @ Q)
+    order = np.argsort(-np.abs(w), kind="stable")
+    r = min(k, len(w))
+    return Q @ U[:, order[:r]], [float(w[i]) for i in order[:r]]
+
+
+def rand_evd2(A, k, s):
+    """lora_drivers.rs:153-213 restated: PSD check on every eigenvalue,
+    S = tsog1(A, k + s, 3, 1), the shifted Nystrom factor (A S + nu S) R^-1,
+    R^T R = S^T (A S + nu S), and lambda = sigma^2 - nu above the shift."""
+    A = np.asarray(A, dtype=np.float64)
+    if k == 0:
+        raise InvalidParameters("Rank k must be positive")
+    if np.any(np.linalg.eigvalsh(A) < 0.0):
+        raise ValueError("NotPositiveSemiDefinite")
+    n = A.shape[0]
+    # the odd-pass Gaussian: this library's Philox stream, key 0 (as the GPU draws it)
+    S = tsog1(A, k + s, 3, 1, gaussian=lambda r, c: sketch(DIST_GAUSSIAN, r, c))
+    Y = A @ S
+    nu = np.sqrt(n) * np.finfo(np.float64).eps * np.linalg.norm(Y)
+    Yn = Y + nu * S
+    R = np.linalg.cholesky(S.T @ Yn).T
+    B = Yn @ np.linalg.inv(R)
+    U, sig, _ = np.linalg.svd(B, full_matrices=False)
+    lam = [x * x for x in sig if x > 0.0]
+    r = min(k, sum(1 for x in lam if x > nu))
+    return U[:, :r], [x - nu for x in lam[:r]]
+
+
 def sketch_rows(m, n, sampling_factor):
     """sketch_and_precondition.rs:49: d = m if sf*n > m else floor(sf*n)."""
     return m if sampling_factor * n > m else int(np.floor(sampling_factor * n))

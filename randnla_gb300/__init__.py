@@ -29,7 +29,7 @@ from ._lib import Options, Rng, Stats, LsqrResult
 
 __all__ = [
     "DistributionType", "Precision", "Mode", "InnerSolver", "Generator", "RandNLAError",
-    "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd",
+    "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd", "rand_evd1", "rand_evd2",
     "blendenpik_overdetermined", "lsrn_overdetermined", "sap_chol_qrcp", "sketched_least_squares_qr",
     "sketched_least_squares_svd", "cgls",
     "lsqr", "solve_upper_triangular_system", "options", "lib",
@@ -270,6 +270,35 @@ def rand_svd(A, k, epsilon, s, opts=None, return_stats=False):
     rr = r.value
     out = (np.asfortranarray(U[:, :rr]), np.asfortranarray(S[:rr, :rr]), np.asfortranarray(Vt[:rr, :]))
     return out + (st.as_dict(),) if return_stats else out
+
+
+def rand_evd1(A, k, epsilon, s):
+    """src/lora_drivers.rs:84-140.  Returns (V n x r, lambda list of r)."""
+    A = _f64(A)
+    n = A.shape[0]
+    if A.shape[1] != n:
+        raise InvalidDimensions("A must be square")
+    kk = max(int(k), 1)
+    V = np.zeros((n, kk), order="F")
+    lam = np.zeros(kk)
+    r = ctypes.c_int64(0)
+    _check(lib().rnla_rand_evd1(_ptr(A), n, max(n, 1), k, epsilon, s, _ptr(V), max(n, 1), _ptr(lam),
+                                ctypes.byref(r)))
+    return np.asfortranarray(V[:, :r.value]), [float(x) for x in lam[:r.value]]
+
+
+def rand_evd2(A, k, s):
+    """src/lora_drivers.rs:153-213.  Returns (V n x r, lambda list of r)."""
+    A = _f64(A)
+    n = A.shape[0]
+    if A.shape[1] != n:
+        raise InvalidDimensions("A must be square")
+    kk = max(int(k), 1)
+    V = np.zeros((n, kk), order="F")
+    lam = np.zeros(kk)
+    r = ctypes.c_int64(0)
+    _check(lib().rnla_rand_evd2(_ptr(A), n, max(n, 1), k, s, _ptr(V), max(n, 1), _ptr(lam), ctypes.byref(r)))
+    return np.asfortranarray(V[:, :r.value]), [float(x) for x in lam[:r.value]]
 
 
 # ---------------------------------------------------------------------------

@@ -78,6 +78,8 @@ SIGNATURES = [
     ("rnla_qb1", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_i64, c_dbl, c_vp, c_i64, c_vp, c_i64, P_i64]),
     ("rnla_rand_svd_rank", c_i64, [c_i64, c_i64, c_i64, c_i64, c_i32]),
+    ("rnla_rand_evd1", ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_dbl, c_i64, c_vp, c_i64, c_vp, P_i64]),
+    ("rnla_rand_evd2", ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp, P_i64]),
     ("rnla_rand_svd", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_i64, c_dbl, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, P_i64]),
     ("rnla_rand_svd_ex", ctypes.c_int,

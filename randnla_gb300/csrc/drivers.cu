@@ -152,6 +152,140 @@ static DMat rf1_ref(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda
 }
 
 // ---------------------------------------------------------------------------
+// Symmetric eigenpairs and the eigenvalue drivers (lora_drivers.rs:84-213)
+// ---------------------------------------------------------------------------
+// lambda_i = sigma_i sign(u_i . v_i): for a symmetric matrix the SVD's
+// left and right singular vectors agree up to the eigenvalue's sign
+__global__ void eig_sign_kernel(const double* __restrict__ U, const double* __restrict__ V, int64_t p,
+                                int64_t c, const double* __restrict__ sigma, double* __restrict__ lambda) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t j = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < c; j += nw) {
+        double d = 0.0;
+        for (int64_t i = lane; i < p; i += 32) d = fma(U[i + j * p], V[i + j * p], d);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (lane == 0) lambda[j] = (d < 0.0) ? -sigma[j] : sigma[j];
+    }
+}
+
+// count of A[i][j] != A[j][i] (exact comparison, as lora_drivers.rs:103)
+__global__ void asym_count_kernel(const double* __restrict__ A, int64_t n, int64_t lda,
+                                  unsigned long long* __restrict__ cnt) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n * n;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % n, j = e / n;
+        if (i < j && !(A[i + j * lda] == A[j + i * lda])) atomicAdd(cnt, 1ull);
+    }
+}
+
+// y = y + nu x (n x c, same ld)
+__global__ void axpy_mat_kernel(double* __restrict__ Y, const double* __restrict__ X, int64_t count, double nu) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x)
+        Y[e] = fma(nu, X[e], Y[e]);
+}
+
+// symmetric eigenpairs of C (p x p): lambda ordered by decreasing |lambda|,
+// eigenvectors the right singular vectors
+static void sym_eig(Ctx& ctx, const double* C, int64_t p, double* lambda, double* W) {
+    DevBuf<double> U((size_t)p * p, ctx.stream), sg(p, ctx.stream);
+    small_svd(ctx, C, p, p, p, U, p, sg, W, p);
+    eig_sign_kernel<<<(unsigned)div_up(p, 8), 256, 0, ctx.stream>>>(U, W, p, p, sg, lambda);
+    RNLA_LAUNCH_CHECK();
+}
+
+static void rand_evd1_impl(Ctx& ctx, const double* A, int64_t n, int64_t lda, int64_t k, double eps, int64_t s,
+                           double* v, int64_t ldv, double* lambda_host, int64_t* r_out) {
+    if (k <= 0) fail(RNLA_ERR_INVALID_PARAMETERS, "Rank k must be positive");
+    if (!(eps > 0.0)) fail(RNLA_ERR_INVALID_PARAMETERS, "Epsilon must be positive");
+    if (s <= 0) fail(RNLA_ERR_INVALID_PARAMETERS, "Oversampling parameter s must be positive");
+    {
+        DevBuf<unsigned long long> cnt(1, ctx.stream);
+        RNLA_CUDA(cudaMemsetAsync(cnt.get(), 0, sizeof(unsigned long long), ctx.stream));
+        int g = (int)div_up(n * n, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        asym_count_kernel<<<g, 256, 0, ctx.stream>>>(A, n, lda, cnt);
+        RNLA_LAUNCH_CHECK();
+        unsigned long long h = 0;
+        RNLA_CUDA(cudaMemcpyAsync(&h, cnt.get(), sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+        RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+        if (h) fail(RNLA_ERR_NOT_HERMITIAN, "Input matrix is not Hermitian");
+    }
+    const bool finite = all_finite(ctx, n, n, A, lda);
+    DMat Q = rf1_ref(ctx, A, n, n, lda, k + s, finite);              // QB1: Q
+    const int64_t c = Q.cols;
+    DevBuf<double> B((size_t)c * n, ctx.stream), C((size_t)c * c, ctx.stream), W((size_t)c * c, ctx.stream),
+        lam(c, ctx.stream);
+    gemm_f64(ctx, 'T', 'N', c, n, n, 1.0, Q.p(), n, A, lda, 0.0, B, c);     // B = Q^T A
+    gemm_f64(ctx, 'N', 'N', c, c, n, 1.0, B, c, Q.p(), n, 0.0, C, c);       // C = B Q
+    sym_eig(ctx, C, c, lam, W);
+    const int64_t r = k < c ? k : c;
+    gemm_f64(ctx, 'N', 'N', n, r, c, 1.0, Q.p(), n, W, c, 0.0, v, ldv);      // V = Q U
+    RNLA_CUDA(cudaMemcpyAsync(lambda_host, lam.get(), r * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    *r_out = r;
+}
+
+static double frob_norm(Ctx& ctx, const double* X, int64_t count) {
+    DevBuf<double> out(1, ctx.stream);
+    gemm_f64(ctx, 'T', 'N', 1, 1, count, 1.0, X, count, X, count, 0.0, out, 1);
+    double h = 0.0;
+    RNLA_CUDA(cudaMemcpyAsync(&h, out.get(), sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    return sqrt(h);
+}
+
+static void rand_evd2_impl(Ctx& ctx, const double* A, int64_t n, int64_t lda, int64_t k, int64_t s, double* v,
+                           int64_t ldv, double* lambda_host, int64_t* r_out) {
+    if (k <= 0) fail(RNLA_ERR_INVALID_PARAMETERS, "Rank k must be positive");
+    // every eigenvalue of A must be >= 0 (lora_drivers.rs:166-172)
+    {
+        DevBuf<double> W((size_t)n * n, ctx.stream), lam(n, ctx.stream);
+        DevBuf<double> Ac((size_t)n * n, ctx.stream);
+        copy_matrix(ctx, n, n, A, lda, Ac, n);
+        sym_eig(ctx, Ac, n, lam, W);
+        std::vector<double> h(n);
+        RNLA_CUDA(cudaMemcpyAsync(h.data(), lam.get(), n * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+        RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+        for (double x : h)
+            if (x < 0.0) fail(RNLA_ERR_NOT_POSITIVE_SEMIDEFINITE, "Matrix is not positive semi-definite");
+    }
+    const bool finite = all_finite(ctx, n, n, A, lda);
+    DMat S = tsog1_ref(ctx, A, n, n, lda, k + s, 3, 1, finite);        // lines 174
+    const int64_t l = S.cols;
+    DevBuf<double> Y((size_t)n * l, ctx.stream), SY((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream),
+        B((size_t)n * l, ctx.stream), U((size_t)n * l, ctx.stream), sg(l, ctx.stream), Vs((size_t)l * l, ctx.stream);
+    gemm_f64(ctx, 'N', 'N', n, l, n, 1.0, A, lda, S.p(), n, 0.0, Y, n);     // Y = A S
+    const double nu = sqrt((double)n) * 2.220446049250313e-16 * frob_norm(ctx, Y, n * l);
+    {
+        int g = (int)div_up(n * l, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        axpy_mat_kernel<<<g, 256, 0, ctx.stream>>>(Y, S.p(), n * l, nu);     // Y_new = Y + nu S
+        RNLA_LAUNCH_CHECK();
+    }
+    gemm_f64(ctx, 'T', 'N', l, l, n, 1.0, S.p(), n, Y, n, 0.0, SY, l);      // S^T Y_new
+    if (!cholesky_upper(ctx, SY, l, l))
+        fail(RNLA_ERR_MATRIX_DECOMPOSITION, "Cholesky Decomposition Failed");
+    if (!upper_inverse(ctx, SY, l, l, Ri, l)) fail(RNLA_ERR_MATRIX_DECOMPOSITION, "Matrix Inverse Failed");
+    gemm_f64(ctx, 'N', 'N', n, l, l, 1.0, Y, n, Ri, l, 0.0, B, n);          // B = Y_new R^-1
+    small_svd(ctx, B, n, l, n, U, n, sg, Vs, l);
+    std::vector<double> sh(l);
+    RNLA_CUDA(cudaMemcpyAsync(sh.data(), sg.get(), l * sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    std::vector<double> lam;
+    for (double x : sh)
+        if (x > 0.0) lam.push_back(x * x);
+    int64_t above = 0;
+    for (double x : lam)
+        if (x > nu) ++above;
+    const int64_t r = k < above ? k : above;
+    for (int64_t i = 0; i < r; ++i) lambda_host[i] = lam[(size_t)i] - nu;
+    if (r > 0) copy_matrix(ctx, n, r, U, n, v, ldv);
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    *r_out = r;
+}
+
+// ---------------------------------------------------------------------------
 // Shared helpers for the randomized drivers
 // ---------------------------------------------------------------------------
 // C (MM x NN) = X^T Y with X (K x MM), Y (K x NN) in the requested precision.
@@ -710,6 +844,42 @@ int rnla_qb1(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, doub
 }
 
 // ---- lora_drivers.rs ----
+int rnla_rand_evd1(const double* a, int64_t n, int64_t lda, int64_t k, double epsilon, int64_t s, double* v,
+                   int64_t ldv, double* lambda, int64_t* r_out) {
+    RNLA_API_BEGIN
+    check_mat(n, n, lda);
+    if (n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty input");
+    cudaStream_t st = host_stream();
+    Ctx ctx(st);
+    const int64_t kk = k > 0 ? k : 1;
+    DevBuf<double> A((size_t)n * n, st), V((size_t)n * kk, st);
+    h2d_matrix(A, n, a, lda, n, n, st);
+    int64_t r = 0;
+    rand_evd1_impl(ctx, A, n, n, k, epsilon, s, V, n, lambda, &r);
+    d2h_matrix(v, ldv, V, n, n, r, st);
+    RNLA_CUDA(cudaStreamSynchronize(st));
+    if (r_out) *r_out = r;
+    RNLA_API_END
+}
+
+int rnla_rand_evd2(const double* a, int64_t n, int64_t lda, int64_t k, int64_t s, double* v, int64_t ldv,
+                   double* lambda, int64_t* r_out) {
+    RNLA_API_BEGIN
+    check_mat(n, n, lda);
+    if (n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty input");
+    cudaStream_t st = host_stream();
+    Ctx ctx(st);
+    const int64_t kk = k > 0 ? k : 1;
+    DevBuf<double> A((size_t)n * n, st), V((size_t)n * kk, st);
+    h2d_matrix(A, n, a, lda, n, n, st);
+    int64_t r = 0;
+    rand_evd2_impl(ctx, A, n, n, k, s, V, n, lambda, &r);
+    d2h_matrix(v, ldv, V, n, n, r, st);
+    RNLA_CUDA(cudaStreamSynchronize(st));
+    if (r_out) *r_out = r;
+    RNLA_API_END
+}
+
 int64_t rnla_rand_svd_rank(int64_t m, int64_t n, int64_t k, int64_t s, int32_t mode) {
     if (k <= 0 || s < 0 || m <= 0 || n <= 0) return 0;
     int64_t l = k + s;

@@ -177,3 +177,19 @@ def test_qrcp_and_cqrrpt_restatements():
     assert np.allclose(np.tril(rr, -1), 0.0)
     with pytest.raises(O.InvalidParameters):
         O.sap_chol_qrcp(a, 5)
+
+
+def test_rand_evd_restatements():
+    """lora_drivers.rs:84-213 restated: the dominant eigenpairs of a
+    symmetric matrix with a clear gap come out of both drivers."""
+    rng = np.random.default_rng(8)
+    Q, _ = np.linalg.qr(rng.standard_normal((80, 80)))
+    eigs = np.concatenate([[20.0, -10.0, 5.0], 1e-4 * np.ones(77)])
+    A = (Q * eigs) @ Q.T
+    A = (A + A.T) / 2
+    V, lam = O.rand_evd1(A, 3, 1e-6, 8)
+    np.testing.assert_allclose(lam, [20.0, -10.0, 5.0], atol=1e-3)
+    P = (Q * np.abs(eigs)) @ Q.T
+    P = (P + P.T) / 2
+    V2, lam2 = O.rand_evd2(P, 3, 8)
+    np.testing.assert_allclose(lam2, [20.0, 10.0, 5.0], rtol=1e-3)
