@@ -19,7 +19,7 @@ textbook algorithms or LAPACK calls through numpy:
   elimination, which reproduces Stabilizer(0) = I (lora_helpers.rs:359-366);
 * SVD             -> numpy.linalg.svd (LAPACK gesdd).
 
-Parity status (also stated in the design doc): the reference's generator values
+Parity status: the reference's generator values
 (rand_distr's normal sampler behind sketch.rs:114-117) are unpinned; results
 that are independent of the sketch (the reference rand_svd, which never uses
 its Gaussian — lora_helpers.rs:70-99 — and converged least-squares

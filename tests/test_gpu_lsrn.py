@@ -54,7 +54,7 @@ def test_errors(rnla):
 
 def test_singular_sketch_is_an_error(rnla):
     """A zero column makes the sketch exactly singular: the reference would
-    drop that singular direction; this build reports SingularMatrix."""
+    drop that singular direction; this library reports SingularMatrix."""
     A, b = _problem(800, 12, 1e3, 1e-4)
     A[:, 3] = 0.0
     with pytest.raises(rnla.SingularMatrix):
