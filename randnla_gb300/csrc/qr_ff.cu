@@ -271,6 +271,9 @@ __device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, 
 #pragma unroll
     for (int k = 0; k < NP; ++k) { ah[k] = 0ull; al[k] = 0ull; }
     const float2* vg = a.VF + t * a.ldv;
+    // tau_t is loaded with the first round of rows (it is written right after
+    // them), so it costs no separate L2 round trip
+    float2 tau = ld_relaxed_f2(a.taug + t);
     // RB rows per thread per round: their L2 loads are all in flight before
     // any is checked, so a round costs one L2 round trip
     constexpr int RB = (NC <= 8) ? 4 : 2;
@@ -297,8 +300,7 @@ __device__ bool apply_reflector(const Args& a, int64_t t, float2* c, int64_t m, 
                 }
         }
     }
-    float2 tau;
-    if (!ld_written(a, a.taug + t, tau)) good = false;
+    if (__float_as_uint(tau.x) == UNSET && !ld_written(a, a.taug + t, tau)) good = false;
     if (!good) ok[1] = 0;
     float h[NC], l[NC];
 #pragma unroll
