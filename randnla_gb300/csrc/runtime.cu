@@ -65,11 +65,10 @@ static int sm_count_of(int dev) {
     return c;
 }
 
-// A second, non-blocking stream per device for work that can overlap the
-// main stream (created once, never destroyed).
-cudaStream_t side_stream(int dev) {
-    static std::mutex mu;
-    static std::map<int, cudaStream_t> cache;
+// One lazily created, never destroyed, non-blocking stream per device and
+// purpose: `side` for work that overlaps the caller's stream (the sketch
+// generator, the solver's input copies), `copy` for host <-> device copies.
+static cudaStream_t device_stream(std::map<int, cudaStream_t>& cache, std::mutex& mu, int dev) {
     std::lock_guard<std::mutex> g(mu);
     auto it = cache.find(dev);
     if (it != cache.end()) return it->second;
@@ -79,17 +78,16 @@ cudaStream_t side_stream(int dev) {
     return st;
 }
 
-// A third stream per device for host <-> device copies that overlap compute.
+cudaStream_t side_stream(int dev) {
+    static std::mutex mu;
+    static std::map<int, cudaStream_t> cache;
+    return device_stream(cache, mu, dev);
+}
+
 cudaStream_t copy_stream(int dev) {
     static std::mutex mu;
     static std::map<int, cudaStream_t> cache;
-    std::lock_guard<std::mutex> g(mu);
-    auto it = cache.find(dev);
-    if (it != cache.end()) return it->second;
-    cudaStream_t st = nullptr;
-    RNLA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    cache[dev] = st;
-    return st;
+    return device_stream(cache, mu, dev);
 }
 
 void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64_t lda, int64_t chunk,
