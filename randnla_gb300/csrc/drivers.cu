@@ -955,27 +955,33 @@ int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int6
     RNLA_API_END
 }
 
-int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda,
-                                      const double* b, double epsilon, int64_t l,
-                                      double sampling_factor, const rnla_options* opt, double* x,
-                                      rnla_stats* stats) {
+// Host-pointer blendenpik / lsrn: A goes up in column tiles on the copy
+// stream and the solve starts on the first tile while the rest is in flight.
+static int blendenpik_host(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double epsilon,
+                           int64_t l, double sampling_factor, const rnla_options* opt, double* x,
+                           rnla_stats* stats, bool lsrn) {
     RNLA_API_BEGIN
     check_mat(m, n, lda);
     blendenpik_validate(m, n, epsilon, l, sampling_factor);
     cudaStream_t s = host_stream();
     DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
     RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
-    // A goes up in column tiles on the copy stream; the solve starts on the
-    // first tile while the rest is in flight
     ColumnFeed feed;
     h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
     Ctx ctx(s);
     const rnla_options o = opts_or_default(opt);
     if (stats) memset(stats, 0, sizeof *stats);
-    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed);
+    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed, lsrn);
     RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
     RNLA_CUDA(cudaStreamSynchronize(s));
     RNLA_API_END
+}
+
+int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda,
+                                      const double* b, double epsilon, int64_t l,
+                                      double sampling_factor, const rnla_options* opt, double* x,
+                                      rnla_stats* stats) {
+    return blendenpik_host(a, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, false);
 }
 
 int rnla_blendenpik_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
@@ -1001,21 +1007,7 @@ int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m,
 int rnla_lsrn_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
                                 double epsilon, int64_t l, double sampling_factor, const rnla_options* opt,
                                 double* x, rnla_stats* stats) {
-    RNLA_API_BEGIN
-    check_mat(m, n, lda);
-    blendenpik_validate(m, n, epsilon, l, sampling_factor);
-    cudaStream_t s = host_stream();
-    DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
-    RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
-    ColumnFeed feed;
-    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
-    Ctx ctx(s);
-    const rnla_options o = opts_or_default(opt);
-    if (stats) memset(stats, 0, sizeof *stats);
-    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed, true);
-    RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    RNLA_CUDA(cudaStreamSynchronize(s));
-    RNLA_API_END
+    return blendenpik_host(a, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, true);
 }
 
 int rnla_lsrn_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
