@@ -107,9 +107,10 @@ RNLA_API int rnla_sketching_operator_ex(int32_t dist, int64_t rows, int64_t cols
                                double* out, int64_t ld);
 RNLA_API int rnla_sketching_operator_dev(int32_t dist, int64_t rows, int64_t cols, const rnla_rng* rng,
                                 double* out_dev, int64_t ld, void* stream);
-/* float32 entries; `quantized` != 0 rounds Gaussian entries to the nearest
- * multiple of 1/8 clamped to +-63/8 — the operator the tensor-core sketch
- * applies (exactly representable in bf16). */
+/* float32 entries; `quantized` != 0 gives the operator the tensor-core
+ * sketch applies (exactly representable in bf16): the Gaussian as t / 8,
+ * t = round(8 g) clamped to +-63 (drawn through an alias table), the uniform
+ * as the bin midpoints (2 floor(u / 2^26) - 63) / 64, Rademacher unchanged. */
 RNLA_API int rnla_sketching_operator_f32_dev(int32_t dist, int64_t rows, int64_t cols, const rnla_rng* rng,
                                     int32_t quantized, float* out_dev, int64_t ld, void* stream);
 
@@ -370,6 +371,14 @@ RNLA_API int rnla_sketched_least_squares_dev(const void* a_dev, int32_t a_is_f32
 RNLA_API int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
                           int64_t d, const rnla_rng* rng, int32_t precision, int32_t digits,
                           double* y_dev, int64_t ldy, void* stream);
+/* The same with the distribution of S (dist: RNLA_GAUSSIAN, RNLA_UNIFORM,
+ * RNLA_RADEMACHER).  Under RNLA_PREC_BF16X S is the quantised form of the
+ * distribution (rnla_sketching_operator_f32_dev with quantized = 1): t / 8
+ * with t the alias-table Gaussian, (2 floor(u / 2^26) - 63) / 64 for the
+ * uniform, the exact +-1 for Rademacher. */
+RNLA_API int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
+                                      int64_t d, int32_t dist, const rnla_rng* rng, int32_t precision,
+                                      int32_t digits, double* y_dev, int64_t ldy, void* stream);
 
 /* C (ldc) = X^T Y for X (k x mm, ldx) and Y (k x nn, ldy), both double,
  * in the given precision (FP64 CUDA cores or bf16 digit-sliced tensor cores

@@ -64,6 +64,9 @@ def lib():
                                                    ctypes.c_uint64, ctypes.c_int64,
                                                    ctypes.c_int64, ctypes.c_void_p,
                                                    ctypes.c_int64]
+        L.oracle_sketch_fill_quantized_dist.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                                         ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                                         ctypes.c_void_p, ctypes.c_int64]
         _LIB = L
     return _LIB
 
@@ -117,8 +120,7 @@ def sketch(dist, rows, cols, gen=GEN_PHILOX4X32, key0=0, key1=0, quantized=False
         raise ValueError("Rows and columns must be greater than 0")
     out = np.empty((rows, cols), dtype=np.float32, order="F")
     if quantized:
-        assert dist == DIST_GAUSSIAN
-        lib().oracle_sketch_fill_quantized(gen, key0, key1, rows, cols, out.ctypes.data, rows)
+        lib().oracle_sketch_fill_quantized_dist(dist, gen, key0, key1, rows, cols, out.ctypes.data, rows)
     else:
         lib().oracle_sketch_fill(dist, gen, key0, key1, rows, cols, out.ctypes.data, rows)
     return out.astype(np.float64)

@@ -310,3 +310,23 @@ void oracle_sketch_fill_quantized(int gen, uint64_t key0, uint64_t key1,
             out[i + j * ld] = (float)oracle_qgauss_t(w[L & 3]) * 0.125f;
         }
 }
+
+/* The quantised uniform and Rademacher sketches (this library's own
+ * definitions, restated from the word): dist 1 gives (2 (u >> 26) - 63) / 64,
+ * dist 2 gives +-1 from the top bit; dist 0 is the Gaussian above. */
+void oracle_sketch_fill_quantized_dist(int dist, int gen, uint64_t key0, uint64_t key1,
+                                       int64_t rows, int64_t cols, float *out, int64_t ld) {
+    if (dist == 0) {
+        oracle_sketch_fill_quantized(gen, key0, key1, rows, cols, out, ld);
+        return;
+    }
+    int64_t rows4 = (rows + 3) & ~(int64_t)3;
+    for (int64_t j = 0; j < cols; ++j)
+        for (int64_t i = 0; i < rows; ++i) {
+            uint64_t L = (uint64_t)(i + j * rows4);
+            uint32_t w[4];
+            block_words(gen, key0, key1, L >> 2, w);
+            uint32_t u = w[L & 3];
+            out[i + j * ld] = (dist == 1) ? (float)(2 * (int)(u >> 26) - 63) / 64.0f : ((u >> 31) ? 1.0f : -1.0f);
+        }
+}

@@ -427,14 +427,15 @@ def rand_svd_dev(a, k, epsilon, s, U, sigma, Vt, opts=None):
 
 
 def sketch_apply_dev(x, d, y, precision=Precision.FP64, digits=0, generator=Generator.Philox4x32,
-                     seed=0):
-    """y (d x n, column-major float64) = S x for the Gaussian sketch S (d x m)."""
+                     seed=0, dist_type=DistributionType.Gaussian):
+    """y (d x n, column-major float64) = S x for the sketch S (d x m) of
+    `dist_type` (quantised under Precision.BF16X)."""
     import torch
     r = _rng(generator, seed)
     m, n = x.shape
-    _check(lib().rnla_sketch_apply_dev(_dptr(x), int(x.dtype == torch.float32), m, n, _ld(x), d,
-                                       ctypes.byref(r), int(precision), digits, _dptr(y), _ld(y),
-                                       _stream()))
+    _check(lib().rnla_sketch_apply_ex_dev(_dptr(x), int(x.dtype == torch.float32), m, n, _ld(x), d,
+                                          int(dist_type), ctypes.byref(r), int(precision), digits, _dptr(y),
+                                          _ld(y), _stream()))
 
 
 def sketching_operator_dev(out, dist_type=DistributionType.Gaussian, quantized=False,

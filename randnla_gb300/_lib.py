@@ -114,6 +114,8 @@ SIGNATURES = [
      [c_vp, c_i64, c_i64, c_i64, c_vp, ctypes.POINTER(Options), c_vp]),
     ("rnla_sketched_least_squares_dev", ctypes.c_int,
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_vp, c_i32, ctypes.POINTER(Options), c_vp, c_vp]),
+    ("rnla_sketch_apply_ex_dev", ctypes.c_int,
+     [c_vp, c_i32, c_i64, c_i64, c_i64, c_i64, c_i32, ctypes.POINTER(Rng), c_i32, c_i32, c_vp, c_i64, c_vp]),
     ("rnla_sketch_apply_dev", ctypes.c_int,
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_i64, ctypes.POINTER(Rng), c_i32, c_i32, c_vp, c_i64, c_vp]),
     ("rnla_gemm_tn_dev", ctypes.c_int,

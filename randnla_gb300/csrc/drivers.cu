@@ -1091,17 +1091,19 @@ int rnla_sketched_least_squares_svd(const double* a, int64_t m, int64_t n, int64
 }
 
 // ---- building blocks ----
-int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
-                          int64_t d, const rnla_rng* rng, int32_t precision, int32_t digits,
-                          double* y_dev, int64_t ldy, void* stream) {
+int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
+                             int64_t d, int32_t dist, const rnla_rng* rng, int32_t precision, int32_t digits,
+                             double* y_dev, int64_t ldy, void* stream) {
     RNLA_API_BEGIN
     check_mat(m, n, ldx);
     if (d <= 0 || m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty sketch product");
+    if (dist != RNLA_GAUSSIAN && dist != RNLA_UNIFORM && dist != RNLA_RADEMACHER)
+        fail(RNLA_ERR_INVALID_PARAMETERS, "unknown distribution");
     Ctx ctx((cudaStream_t)stream);
     const RngKey key = key_of(rng);
     if (precision == RNLA_PREC_FP64) {
         DevBuf<double> S((size_t)d * m, ctx.stream);
-        sketch_fill_f64(ctx, DIST_GAUSSIAN, key, d, m, S, d);
+        sketch_fill_f64(ctx, dist, key, d, m, S, d);
         DevBuf<double> Xw;
         const double* X = static_cast<const double*>(x_dev);
         int64_t ld = ldx;
@@ -1114,9 +1116,16 @@ int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_
         gemm_f64(ctx, 'N', 'N', d, n, m, 1.0, S, d, X, ld, 0.0, y_dev, ldy);
     } else {
         if (!tc_available(ctx)) fail(RNLA_ERR_UNSUPPORTED, "sm_103a tensor-core kernels unavailable");
-        tc_sketch_apply(ctx, key, x_dev, x_is_f32 != 0, m, n, ldx, nullptr, d, digits, y_dev, ldy);
+        tc_sketch_apply(ctx, key, x_dev, x_is_f32 != 0, m, n, ldx, nullptr, d, digits, y_dev, ldy, nullptr, dist);
     }
     RNLA_API_END
+}
+
+int rnla_sketch_apply_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int64_t n, int64_t ldx,
+                          int64_t d, const rnla_rng* rng, int32_t precision, int32_t digits,
+                          double* y_dev, int64_t ldy, void* stream) {
+    return rnla_sketch_apply_ex_dev(x_dev, x_is_f32, m, n, ldx, d, RNLA_GAUSSIAN, rng, precision, digits, y_dev,
+                                    ldy, stream);
 }
 
 int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, const double* y_dev,

@@ -199,7 +199,7 @@ bool tc_available(Ctx& ctx);
 // of the product is started as soon as its columns are on the device.
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed = nullptr);
+                     const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN);
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
 // C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.

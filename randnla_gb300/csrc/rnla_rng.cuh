@@ -144,6 +144,23 @@ __device__ __forceinline__ int qgauss_t(uint32_t u, const uint32_t* tab) {
     return (int)o - 63;
 }
 
+// Quantised entries of the tensor-core sketch for each distribution: an
+// integer t with |t| <= 63 (so t is exact in bf16 and the digit products stay
+// below 2^14) and the scale 2^-qshift(dist) that makes t 2^-qshift the entry.
+//   Gaussian    t = qgauss_t(u), entry t / 8
+//   Uniform     t = 2 (u >> 26) - 63 (odd, -63..63), entry t / 64: the midpoint
+//               of the 1/32-wide bin holding the unquantised U(-1, 1) value
+//               uniform_pm1(u) (both come from the top bits of u)
+//   Rademacher  t = +-1 from the top bit, entry t (already exact)
+__device__ __forceinline__ int quant_t(int dist, uint32_t u, const uint32_t* tab) {
+    if (dist == DIST_GAUSSIAN) return qgauss_t(u, tab);
+    if (dist == DIST_UNIFORM) return 2 * (int)(u >> 26) - 63;
+    return (u >> 31) ? 1 : -1;
+}
+__host__ __device__ constexpr int quant_shift(int dist) {
+    return dist == DIST_GAUSSIAN ? 3 : dist == DIST_UNIFORM ? 6 : 0;
+}
+
 // The four entries generated by block g for distribution `dist`.
 __device__ __forceinline__ void block_entries(const RngKey& k, int dist, uint64_t g, float v[4]) {
     uint32_t w[4];

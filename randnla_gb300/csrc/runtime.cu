@@ -193,7 +193,7 @@ __global__ void sketch_fill_kernel(RngKey key, int dist, int64_t rows, int64_t c
             uint32_t w[4];
             block_words(key, g, w);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) v[t] = __fmul_rn((float)qgauss_t(w[t], k_qgauss_table), 0.125f);
+            for (int t = 0; t < 4; ++t) v[t] = ldexpf((float)quant_t(dist, w[t], k_qgauss_table), -quant_shift(dist));
         } else {
             block_entries(key, dist, g, v);
         }
@@ -230,7 +230,7 @@ void sketch_fill_f32(Ctx& ctx, int dist, const RngKey& key, int64_t rows, int64_
     const uint64_t blocks = (uint64_t)((rows + 3) >> 2) * (uint64_t)cols;
     if (quantized)
         sketch_fill_kernel<float, true><<<grid_for(ctx, blocks, 256), 256, 0, ctx.stream>>>(
-            key, DIST_GAUSSIAN, rows, cols, out, ld);
+            key, dist, rows, cols, out, ld);
     else
         sketch_fill_kernel<float, false><<<grid_for(ctx, blocks, 256), 256, 0, ctx.stream>>>(
             key, dist, rows, cols, out, ld);
@@ -357,8 +357,6 @@ int rnla_sketching_operator_f32_dev(int32_t dist, int64_t rows, int64_t cols, co
                                     int32_t quantized, float* out_dev, int64_t ld, void* stream) {
     RNLA_API_BEGIN
     check_sketch_args(dist, rows, cols, ld);
-    if (quantized && dist != RNLA_GAUSSIAN)
-        fail(RNLA_ERR_INVALID_PARAMETERS, "quantized applies to the Gaussian distribution");
     Ctx ctx((cudaStream_t)stream);
     sketch_fill_f32(ctx, dist, key_of(rng), rows, cols, quantized != 0, out_dev, ld);
     RNLA_API_END

@@ -140,11 +140,12 @@ struct Params {
 };
 
 // The four quantised entries t (integers, |t| <= 63) of block g.
-__device__ __forceinline__ void sketch_block(const RngKey& key, uint64_t g, const uint32_t* tab, float v[4]) {
+__device__ __forceinline__ void sketch_block(const RngKey& key, int dist, uint64_t g, const uint32_t* tab,
+                                             float v[4]) {
     uint32_t w[4];
     block_words(key, g, w);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) v[t] = (float)qgauss_t(w[t], tab);
+    for (int t = 0; t < 4; ++t) v[t] = (float)quant_t(dist, w[t], tab);
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -156,7 +157,7 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // K) unit of a stage; a warp covers 4 rows x 64 K, i.e. four whole 128-byte
 // rows of the image, so stores are coalesced.  Entry (i, k) is word
 // i + k * round_up(M, 4) of the stream (block (i >> 2) + k * M4 / 4).
-__global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int64_t M, int64_t K, int Ks,
+__global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int dist, int64_t M, int64_t K, int Ks,
                                                          uint8_t* __restrict__ S) {
     __shared__ uint32_t qtab[128];
     if (threadIdx.x < 128) qtab[threadIdx.x] = k_qgauss_table[threadIdx.x];
@@ -171,8 +172,9 @@ __global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int64_t M, 
         const int64_t row0 = (int64_t)it * BM + 4 * ig;
         const int64_t k = s * BK + 2 * kp;
         float v0[4] = {0.f, 0.f, 0.f, 0.f}, v1[4] = {0.f, 0.f, 0.f, 0.f};
-        if (row0 < M && k < K) sketch_block(key, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, qtab, v0);
-        if (row0 < M && k + 1 < K) sketch_block(key, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, qtab, v1);
+        if (row0 < M && k < K) sketch_block(key, dist, (uint64_t)(row0 >> 2) + (uint64_t)k * gstride, qtab, v0);
+        if (row0 < M && k + 1 < K)
+            sketch_block(key, dist, (uint64_t)(row0 >> 2) + (uint64_t)(k + 1) * gstride, qtab, v1);
         uint8_t* tile = S + ((size_t)it * Ks + (size_t)s) * S_BYTES;
         const int kl = 2 * kp;
 #pragma unroll
@@ -544,8 +546,8 @@ static size_t smem_bytes() {
 }
 
 template <int P>
-static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t K, int64_t N0, int64_t ldy,
-                const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed) {
+static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32, int64_t K, int64_t N0,
+                int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
     const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
     const size_t smem = smem_bytes<P>();
@@ -591,7 +593,7 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
         int gx = div_up((int64_t)Ks * 1024, 256);
         const int cap = 16 * sm / (tiles_m < 16 ? tiles_m : 16) + 1;
         if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, M, K, Ks, sk);
+        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, sk);
         RNLA_LAUNCH_CHECK();
     }
     Params prm;
@@ -643,7 +645,7 @@ static void run(Ctx& ctx, const RngKey& key, const void* Y, bool y_f32, int64_t 
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
     const int exact_sum = (int64_t)wins + kc_count <= WIN_MAX ? 1 : 0;   // all windows together fit int64
-    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 8 * P + 3,
+    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 8 * P + quant_shift(dist),
                                                  exact_sum, C, ldc);
     RNLA_LAUNCH_CHECK();
     ctx.check_status("tensor-core sketch");
@@ -660,14 +662,14 @@ bool tc_available(Ctx& ctx) {
 
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed) {
+                     const ColumnFeed* feed, int dist) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
     if (digits <= 0) digits = 4;
     switch (digits) {
-        case 1: tc::run<1>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 2: tc::run<2>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 3: tc::run<3>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 4: tc::run<4>(ctx, key, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 3: tc::run<3>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 4: tc::run<4>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
         default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..4");
     }
 }

@@ -6,22 +6,25 @@ reduction and the ragged edge tiles."""
 import numpy as np
 import pytest
 
+from oracle import oracle as O
+
 pytestmark = pytest.mark.gpu
 
 
-def _quantized_sketch(d, m, seed):
+def _quantized_sketch(d, m, seed, dist=0):
     import torch
     import randnla_gb300 as R
     S = torch.empty((m, d), dtype=torch.float32, device="cuda").t()     # column-major d x m
-    R.sketching_operator_dev(S, quantized=True, seed=seed)
+    R.sketching_operator_dev(S, dist_type=R.DistributionType(dist), quantized=True, seed=seed)
     return S.double()
 
 
-def _tc(Y, d, seed, digits=0):
+def _tc(Y, d, seed, digits=0, dist=0):
     import torch
     import randnla_gb300 as R
     C = torch.empty((Y.shape[1], d), dtype=torch.float64, device="cuda").t()
-    R.sketch_apply_dev(Y, d, C, precision=R.Precision.BF16X, digits=digits, seed=seed)
+    R.sketch_apply_dev(Y, d, C, precision=R.Precision.BF16X, digits=digits, seed=seed,
+                       dist_type=R.DistributionType(dist))
     torch.cuda.synchronize()
     return C
 
@@ -34,6 +37,32 @@ def test_integer_data_bit_exact(rnla, d, m, n):
     C = _tc(Y, d, seed=11)
     ref = _quantized_sketch(d, m, 11) @ Y
     assert torch.equal(C, ref), (C - ref).abs().max().item()
+
+
+@pytest.mark.parametrize("dist", [1, 2])
+@pytest.mark.parametrize("d,m,n", [(200, 5000, 100), (37, 4099, 5)])
+def test_uniform_and_rademacher_bit_exact(rnla, dist, d, m, n):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(d + m + n + dist)
+    Y = torch.randint(-1000, 1001, (n, m), generator=g, device="cuda").double().t()
+    C = _tc(Y, d, seed=13, dist=dist)
+    S = _quantized_sketch(d, m, 13, dist)
+    assert torch.equal(C, S @ Y), (C - S @ Y).abs().max().item()
+    # the device quantised operator is the oracle's, word for word
+    ref = O.sketch(dist, d, 64, key0=13, quantized=True)
+    assert np.array_equal(S[:, :64].cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("dist", [1, 2])
+def test_uniform_and_rademacher_fp64_data(rnla, dist):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(17)
+    d, m, n = 160, 12000, 70
+    Y = torch.randn((n, m), generator=g, device="cuda", dtype=torch.float64).t()
+    C = _tc(Y, d, seed=5, dist=dist)
+    ref = _quantized_sketch(d, m, 5, dist) @ Y
+    err = (C - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-9, err
 
 
 def test_gaussian_fp64_data(rnla):

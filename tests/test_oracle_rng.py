@@ -119,6 +119,18 @@ def test_quantized_sketch_grid():
     assert np.array_equal(Q[:, 2], col)
 
 
+def test_quantized_uniform_and_rademacher_grid():
+    w = O.word_stream(O.GEN_PHILOX4X32, 3, 0, 0, 64 * 3).astype(np.int64)
+    U = O.sketch(O.DIST_UNIFORM, 64, 3, key0=3, quantized=True)
+    assert np.array_equal(U[:, 1], (2 * (w[64:128] >> 26) - 63) / 64)
+    assert np.abs(U).max() <= 63 / 64 and np.all(np.abs(U * 64 - np.rint(U * 64)) == 0)
+    Rm = O.sketch(O.DIST_RADEMACHER, 64, 3, key0=3, quantized=True)
+    assert np.array_equal(Rm[:, 2], np.where(w[128:192] >> 31, 1.0, -1.0))
+    big = O.sketch(O.DIST_UNIFORM, 64, 2000, key0=1, quantized=True)
+    # midpoints of 64 equal cells of [-1, 1): mean 0, variance 1/3 - 1/(3 * 64^2)
+    assert abs(big.mean()) < 0.01 and abs(big.var() - (1 / 3 - 1 / 12288)) < 0.01
+
+
 def test_sketch_shape_errors():
     with pytest.raises(ValueError):
         O.sketch(O.DIST_GAUSSIAN, 0, 5)
