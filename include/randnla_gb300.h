@@ -331,6 +331,32 @@ RNLA_API int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, i
                                           double sampling_factor, const rnla_options* opt, double* x_dev,
                                           rnla_stats* stats, void* stream);
 
+/* One least-squares problem of a batch: device pointers to column-major A
+ * (m x n, leading dimension lda; float when a_is_f32), b (m values) and
+ * the output x (n values). */
+typedef struct {
+    const void* a;
+    int32_t a_is_f32;
+    int32_t reserved;
+    int64_t m, n, lda;
+    const double* b;
+    double* x;
+} rnla_ls_problem;
+
+/* Many independent blendenpik_overdetermined solves
+ * (sketch_and_precondition.rs:26-59 per problem; the reference has no
+ * batched entry, callers loop) with shared epsilon, l, sampling_factor and
+ * options, queued on one stream.  Each problem's x is exactly what
+ * rnla_blendenpik_overdetermined_dev gives for it alone (same sketch seed,
+ * same kernels).  status_out (count entries, required) receives each
+ * problem's status, stats_out (nullable, count entries) its facts.  Returns
+ * RNLA_OK when every problem succeeded, else the first failing problem's
+ * status (its message in rnla_last_error_message); a CUDA error stops the
+ * batch and marks the problems not yet run RNLA_ERR_CUDA.  Synchronises. */
+RNLA_API int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsilon, int64_t l,
+                                double sampling_factor, const rnla_options* opt, int32_t* status_out,
+                                rnla_stats* stats_out, void* stream);
+
 /* cqrrpt.rs:27-58 (sap_chol_qrcp): Gaussian sketch S (d x m, n <= d <= m) of
  * a, column-pivoted Householder QR of S a (pivot_decompositions.rs:106-174:
  * largest remaining column norm, first index on ties), then CholeskyQR of

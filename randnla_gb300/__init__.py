@@ -25,12 +25,12 @@ import enum
 import numpy as np
 
 from . import _lib
-from ._lib import Options, Rng, Stats, LsqrResult
+from ._lib import Options, Rng, Stats, LsqrResult, LsProblem
 
 __all__ = [
     "DistributionType", "Precision", "Mode", "InnerSolver", "Generator", "RandNLAError",
     "sketching_operator", "tsog1", "RF1", "QB1", "Orth", "Stabilizer", "rand_svd", "rand_evd1", "rand_evd2",
-    "blendenpik_overdetermined", "lsrn_overdetermined", "sap_chol_qrcp", "sketched_least_squares_qr",
+    "blendenpik_overdetermined", "lsrn_overdetermined", "solve_batched_dev", "sap_chol_qrcp", "sketched_least_squares_qr",
     "sketched_least_squares_svd", "cgls",
     "lsqr", "solve_upper_triangular_system", "options", "lib",
 ]
@@ -401,6 +401,27 @@ def blendenpik_dev(a, b, x, epsilon, l, sampling_factor, opts=None):
         _dptr(a), int(a.dtype == torch.float32), m, n, _ld(a), _dptr(b), epsilon, l, sampling_factor,
         ctypes.byref(o), _dptr(x), ctypes.byref(st), _stream()))
     return st.as_dict()
+
+
+def solve_batched_dev(problems, epsilon, l, sampling_factor, opts=None):
+    """rnla_solve_batched: problems is a sequence of (a, b, x) torch CUDA
+    tensors as for blendenpik_dev.  Returns (statuses, stats): one status
+    code and one stats dict per problem; a failing problem does not stop
+    the others, and nothing is raised for it (a CUDA error is raised)."""
+    import torch
+    o = opts if opts is not None else options()
+    count = len(problems)
+    arr = (LsProblem * max(count, 1))()
+    for i, (a, b, x) in enumerate(problems):
+        m, n = a.shape
+        arr[i] = LsProblem(_dptr(a), int(a.dtype == torch.float32), 0, m, n, _ld(a), _dptr(b), _dptr(x))
+    status = (ctypes.c_int32 * max(count, 1))()
+    st = (Stats * max(count, 1))()
+    rc = lib().rnla_solve_batched(arr, count, epsilon, l, sampling_factor, ctypes.byref(o), status, st,
+                                  _stream())
+    if rc == CudaError.code:
+        _check(rc)
+    return [int(status[i]) for i in range(count)], [st[i].as_dict() for i in range(count)]
 
 
 def sketched_least_squares_dev(a, b, x, use_svd=False, opts=None):

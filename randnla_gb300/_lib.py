@@ -37,6 +37,11 @@ class Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class LsProblem(ctypes.Structure):
+    _fields_ = [("a", c_vp), ("a_is_f32", c_i32), ("reserved", c_i32), ("m", c_i64), ("n", c_i64),
+                ("lda", c_i64), ("b", c_vp), ("x", c_vp)]
+
+
 class LsqrResult(ctypes.Structure):
     _fields_ = [("istop", c_i64), ("itn", c_i64), ("r1norm", c_dbl), ("r2norm", c_dbl),
                 ("anorm", c_dbl), ("acond", c_dbl), ("xnorm", c_dbl)]
@@ -104,6 +109,9 @@ SIGNATURES = [
     ("rnla_lsrn_overdetermined_dev", ctypes.c_int,
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
       ctypes.POINTER(Stats), c_vp]),
+    ("rnla_solve_batched", ctypes.c_int,
+     [ctypes.POINTER(LsProblem), c_i64, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options),
+      ctypes.POINTER(c_i32), ctypes.POINTER(Stats), c_vp]),
     ("rnla_sap_chol_qrcp", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.POINTER(Options), c_vp, c_i64, c_vp, c_i64, c_vp]),
     ("rnla_sap_chol_qrcp_dev", ctypes.c_int,

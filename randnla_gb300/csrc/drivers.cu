@@ -3,6 +3,7 @@
 #include "rnla_abi.h"
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace rnla {
@@ -1002,6 +1003,54 @@ int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m,
                     stats, nullptr, true);
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
     RNLA_API_END
+}
+
+// Problems run one after another on the caller's stream, each through the
+// single-problem pipeline, so every x matches its own _dev call bit for bit.
+// A failing problem (bad shape, singular sketch, a device wait that gave
+// up) is recorded and the batch goes on; a CUDA error ends it.
+int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsilon, int64_t l,
+                       double sampling_factor, const rnla_options* opt, int32_t* status_out,
+                       rnla_stats* stats_out, void* stream) {
+    if (count < 0) return abi_error(RNLA_ERR_NEGATIVE_DIMENSIONS, "count must be non-negative");
+    if (count > 0 && (!probs || !status_out))
+        return abi_error(RNLA_ERR_INVALID_PARAMETERS, "probs and status_out are required");
+    if (count == 0) return abi_ok();
+    const rnla_options o = opts_or_default(opt);
+    int first = RNLA_OK;
+    std::string first_msg;
+    for (int64_t p = 0; p < count; ++p) {
+        const rnla_ls_problem& q = probs[p];
+        rnla_stats* st = stats_out ? stats_out + p : nullptr;
+        if (st) memset(st, 0, sizeof *st);
+        int rc = RNLA_OK;
+        std::string msg;
+        try {
+            check_mat(q.m, q.n, q.lda);
+            if (!q.a || !q.b || !q.x) fail(RNLA_ERR_INVALID_PARAMETERS, "problem with a null pointer");
+            Ctx ctx((cudaStream_t)stream);
+            blendenpik_impl(ctx, q.a, q.a_is_f32 != 0, q.m, q.n, q.lda, q.b, epsilon, l, sampling_factor, o,
+                            q.x, st);
+        } catch (const Error& e) {
+            rc = e.code;
+            msg = e.what();
+        } catch (const std::bad_alloc&) {
+            rc = RNLA_ERR_COMPUTATION;
+            msg = "host allocation failed";
+        }
+        status_out[p] = rc;
+        if (rc != RNLA_OK && first == RNLA_OK) {
+            first = rc;
+            first_msg = "problem " + std::to_string(p) + ": " + msg;
+        }
+        if (rc == RNLA_ERR_CUDA) {
+            for (int64_t r = p + 1; r < count; ++r) status_out[r] = RNLA_ERR_CUDA;
+            return abi_error(first, first_msg.c_str());
+        }
+    }
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return abi_error(RNLA_ERR_CUDA, cudaGetErrorString(e));
+    return first == RNLA_OK ? abi_ok() : abi_error(first, first_msg.c_str());
 }
 
 int rnla_lsrn_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,

@@ -58,6 +58,20 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.Rng) == 24
     assert ctypes.sizeof(_lib.Options) == 16 + 24 + 24 + 16
     assert ctypes.sizeof(_lib.LsqrResult) == 16 + 5 * 8
+    assert ctypes.sizeof(_lib.LsProblem) == 8 + 8 + 24 + 16
+
+
+def test_batched_argument_errors_need_no_device():
+    """rnla_solve_batched rejects a negative count or missing arrays before
+    touching the GPU; an empty batch is fine."""
+    import randnla_gb300 as R
+    lib = R.lib()
+    st = (ctypes.c_int32 * 1)()
+    assert lib.rnla_solve_batched(None, -1, 1e-8, 10, 4.0, None, st, None, None) == R.NegativeDimensions.code
+    assert lib.rnla_solve_batched(None, 2, 1e-8, 10, 4.0, None, st, None, None) == R.InvalidParameters.code
+    assert lib.rnla_solve_batched((R.LsProblem * 1)(), 1, 1e-8, 10, 4.0, None, None, None, None) \
+        == R.InvalidParameters.code
+    assert lib.rnla_solve_batched(None, 0, 1e-8, 10, 4.0, None, None, None, None) == 0
 
 
 def test_no_oracle_in_product():
