@@ -404,6 +404,31 @@ class InvalidParameters(ValueError):
     pass
 
 
+# the other RandNLAError variants (errors.rs:3-14) the restatements raise
+class InvalidDimensions(ValueError):
+    pass
+
+
+class NotOverdetermined(ValueError):
+    pass
+
+
+class SingularMatrix(ValueError):
+    pass
+
+
+class MatrixDecompositionError(ValueError):
+    pass
+
+
+class NotHermitian(ValueError):
+    pass
+
+
+class NotPositiveSemiDefinite(ValueError):
+    pass
+
+
 def rand_svd(A, k, epsilon, s):
     """lora_drivers.rs:30-69: validation, QB1(A, k+s), SVD of B, truncation
     to r = min(k, Q.ncols()), U = Q U_B.  Returns (U m x r, S r x r, Vt r x n)."""
@@ -426,7 +451,7 @@ def rand_evd1(A, k, epsilon, s):
     if k == 0 or not epsilon > 0.0 or s == 0:
         raise InvalidParameters("invalid rand_evd1 parameters")
     if not np.array_equal(A, A.T):
-        raise ValueError("NotHermitian")
+        raise NotHermitian("NotHermitian")
     Q, B = qb1(A, k + s, epsilon)
     w, U = np.linalg.eigh(B @ Q)
     order = np.argsort(-np.abs(w), kind="stable")
@@ -442,14 +467,17 @@ def rand_evd2(A, k, s):
     if k == 0:
         raise InvalidParameters("Rank k must be positive")
     if np.any(np.linalg.eigvalsh(A) < 0.0):
-        raise ValueError("NotPositiveSemiDefinite")
+        raise NotPositiveSemiDefinite("NotPositiveSemiDefinite")
     n = A.shape[0]
     # the odd-pass Gaussian: this library's Philox stream, key 0 (as the GPU draws it)
     S = tsog1(A, k + s, 3, 1, gaussian=lambda r, c: sketch(DIST_GAUSSIAN, r, c))
     Y = A @ S
     nu = np.sqrt(n) * np.finfo(np.float64).eps * np.linalg.norm(Y)
     Yn = Y + nu * S
-    R = np.linalg.cholesky(S.T @ Yn).T
+    try:
+        R = np.linalg.cholesky(S.T @ Yn).T
+    except np.linalg.LinAlgError:
+        raise MatrixDecompositionError("Cholesky Decomposition Failed") from None
     B = Yn @ np.linalg.inv(R)
     U, sig, _ = np.linalg.svd(B, full_matrices=False)
     lam = [x * x for x in sig if x > 0.0]
@@ -470,7 +498,7 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_
     b = np.asarray(b, dtype=np.float64).reshape(-1)
     m, n = a.shape
     if m < n:
-        raise ValueError("NotOverdetermined")
+        raise NotOverdetermined("NotOverdetermined")
     if sampling_factor < 1.0 or not epsilon > 0.0 or l == 0:
         raise InvalidParameters("invalid blendenpik parameters")
     d = sketch_rows(m, n, sampling_factor)
@@ -495,7 +523,7 @@ def lsrn_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_iters=
     b = np.asarray(b, dtype=np.float64).reshape(-1)
     m, n = a.shape
     if m < n:
-        raise ValueError("NotOverdetermined")
+        raise NotOverdetermined("NotOverdetermined")
     if sampling_factor < 1.0 or not epsilon > 0.0 or l == 0:
         raise InvalidParameters("invalid lsrn parameters")
     d = sketch_rows(m, n, sampling_factor)
@@ -554,7 +582,7 @@ def sap_chol_qrcp(a, d, S=None):
     r_sk, p = qrcp(S @ a)
     k = sum(1 for i in range(min(d, n)) if abs(r_sk[i, i]) > 1e-10)
     if k < n:
-        raise ValueError("SingularMatrix")
+        raise SingularMatrix("SingularMatrix")
     rk = np.triu(r_sk[:n, :n])
     a_pre = a[:, p] @ _upper_inverse(rk)
     r_pre = np.linalg.cholesky(a_pre.T @ a_pre).T
@@ -571,7 +599,7 @@ def sketched_least_squares_qr(a, b, S=None):
     m, n = a.shape
     d = m // 4
     if d < n:
-        raise ValueError("InvalidDimensions")
+        raise InvalidDimensions("InvalidDimensions")
     if S is None:
         S = sketch(DIST_GAUSSIAN, d, m)
     q, r = np.linalg.qr(S @ a, mode="reduced")
@@ -586,7 +614,7 @@ def sketched_least_squares_svd(a, b, S=None):
     m, n = a.shape
     d = m // 4
     if d < n:
-        raise ValueError("InvalidDimensions")
+        raise InvalidDimensions("InvalidDimensions")
     if S is None:
         S = sketch(DIST_GAUSSIAN, d, m)
     u, sig, vt = np.linalg.svd(S @ a, full_matrices=False)

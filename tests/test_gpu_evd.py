@@ -61,3 +61,44 @@ def test_errors(rnla):
     C = _sym(30, np.linspace(-1, 2, 30), 4)
     with pytest.raises(rnla.NotPositiveSemiDefinite):
         rnla.rand_evd2(C, 3, 2)
+
+
+def test_reference_known_answers(rnla):
+    """The reference's rand_evd tests with fixed answers
+    (lora_drivers.rs:506-514, 532-563, 702-710, 725-746, 748-776)."""
+    Z = np.zeros((5, 5))
+    V, lam = rnla.rand_evd1(Z, 3, 1e-6, 2)
+    np.testing.assert_allclose(V, np.eye(5)[:, :3], atol=1e-6)   # symmetric_eigen(0) vectors
+    assert all(x == 0.0 for x in lam)
+    with pytest.raises(rnla.MatrixDecompositionError):
+        rnla.rand_evd2(Z, 3, 2)                                   # Cholesky of S^T 0 fails
+    V, lam = rnla.rand_evd1(np.eye(5), 3, 1e-6, 2)
+    assert V.shape == (5, 3) and len(lam) == 3
+    V, lam = rnla.rand_evd2(np.eye(5), 3, 2)
+    assert V.shape == (5, 3) and len(lam) == 3
+    W = np.array([[1.0, 2.0, 3.0], [100.0, 200.0, 4.0], [3.0, 38.0, 1.0]])
+    with pytest.raises(rnla.NotHermitian):
+        rnla.rand_evd1(W, 3, 1e-6, 2)
+    with pytest.raises(rnla.RandNLAError):
+        rnla.rand_evd2(W, 3, 2)
+    # 5 x 5 PSD, k + s = n: the exact dominant eigenpairs
+    G = np.random.default_rng(3).standard_normal((5, 5))
+    P = G @ G.T
+    V, lam = rnla.rand_evd2(P, 3, 2)
+    w, U = np.linalg.eigh(P)
+    top = np.argsort(-np.abs(w))[:3]
+    np.testing.assert_allclose(lam, w[top], atol=1e-6)
+    np.testing.assert_allclose(V.T @ V, np.eye(3), atol=1e-6)
+    np.testing.assert_allclose(V @ V.T @ P, U[:, top] @ U[:, top].T @ P, atol=1e-6)
+
+
+def test_evd1_order_orthogonality_and_error(rnla):
+    """lora_drivers.rs:631-686: |lambda| non-increasing, V^T V = I, and the
+    relative Frobenius error of V diag(lambda) V^T within epsilon."""
+    G = np.random.default_rng(5).standard_normal((100, 100))
+    A = 0.5 * (G + G.T)
+    V, lam = rnla.rand_evd1(A, 3, 2.0, 2)
+    assert list(np.abs(lam)) == sorted(np.abs(lam), reverse=True)
+    np.testing.assert_allclose(V.T @ V, np.eye(3), atol=1e-6)
+    err = np.linalg.norm(A - (V * lam) @ V.T) / np.linalg.norm(A)
+    assert err <= 2.0

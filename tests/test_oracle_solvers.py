@@ -193,3 +193,30 @@ def test_rand_evd_restatements():
     P = (P + P.T) / 2
     V2, lam2 = O.rand_evd2(P, 3, 8)
     np.testing.assert_allclose(lam2, [20.0, 10.0, 5.0], rtol=1e-3)
+
+
+def test_rand_evd_reference_known_answers():
+    """The reference's rand_evd tests with fixed answers
+    (lora_drivers.rs:506-514, 532-563, 702-710, 725-746, 748-776)."""
+    Z = np.zeros((5, 5))
+    V, lam = O.rand_evd1(Z, 3, 1e-6, 2)
+    np.testing.assert_array_equal(V, np.eye(5)[:, :3])        # symmetric_eigen(0) vectors
+    assert all(x == 0.0 for x in lam)
+    with pytest.raises(O.MatrixDecompositionError):
+        O.rand_evd2(Z, 3, 2)                                   # Cholesky of S^T 0 fails
+    assert len(O.rand_evd1(np.eye(5), 3, 1e-6, 2)[1]) == 3
+    assert len(O.rand_evd2(np.eye(5), 3, 2)[1]) == 3
+    W = np.array([[1.0, 2.0, 3.0], [100.0, 200.0, 4.0], [3.0, 38.0, 1.0]])
+    with pytest.raises(O.NotHermitian):
+        O.rand_evd1(W, 3, 1e-6, 2)
+    with pytest.raises(ValueError):
+        O.rand_evd2(W, 3, 2)
+    # 5 x 5 PSD, k + s = n: the exact dominant eigenpairs
+    G = np.random.default_rng(3).standard_normal((5, 5))
+    P = G @ G.T
+    V, lam = O.rand_evd2(P, 3, 2)
+    w, U = np.linalg.eigh(P)
+    top = np.argsort(-np.abs(w))[:3]
+    np.testing.assert_allclose(lam, w[top], atol=1e-6)
+    np.testing.assert_allclose(V.T @ V, np.eye(3), atol=1e-6)
+    np.testing.assert_allclose(V @ V.T @ P, U[:, top] @ U[:, top].T @ P, atol=1e-6)
