@@ -482,6 +482,8 @@ def run_batched(args, rank, local, ws):
                    "l2": "inputs larger than L2", "parallelism": "replicas" if ws > 1 else "single"},
         "accuracy": {"max_abs_diff_rel_residual_vs_lapack_first4": worst},
         "mean_iterations": float(np.mean(its)),
+        "stages_mean_ms": {k: float(np.mean([s_[k] for s_ in stats]))
+                           for k in ("ms_sketch", "ms_factor", "ms_solve", "ms_total")},
         "fp64_path": {"value": fp64_value, "unit": "problems/s",
                       "sample": "loop of single-problem FP64 solves over the first %d problems" % len(sub)},
         "gpu_launches": int(launches),
