@@ -20,6 +20,8 @@ copied in, x copied out inside the timed region).
 `--workload batched` times many independent problems of mixed shape
 (m in [1000, 50000], n in [16, 256], m >= 8 n, kappa 1e6) through one
 rnla_solve_batched call per step, beside a loop of plain FP64 solves.
+Under torchrun each rank takes its own P problems of the sequence (no
+collective): value = all ranks' problems / the slowest rank's time.
 
 With N > 1 (torchrun) every rank solves its own replica (the path has no
 exchange step); value = all ranks' solves / max-over-ranks time.
@@ -366,26 +368,31 @@ def run_ours(args, rank, local, ws):
 # ---------------------------------------------------------------------------
 # batched workload: many independent problems of mixed shape
 # ---------------------------------------------------------------------------
-def batched_shapes(count, seed=12):
-    """m ~ U[1000, 50000], n ~ U[16, 256], redrawn until m >= 8 n."""
+def batched_shapes(count, seed=12, rank=0, world=1):
+    """Problem p of the seeded sequence: m ~ U[1000, 50000], n ~ U[16, 256],
+    redrawn until m >= 8 n.  Rank r of `world` takes problems
+    [r count, (r + 1) count) -- independent units, no exchange between
+    ranks, the same work per rank at every world size.  Returns
+    (global index, (m, n)) pairs."""
     import numpy as np
     rng = np.random.default_rng(seed)
     out = []
-    while len(out) < count:
+    while len(out) < count * (rank + 1):
         m, n = int(rng.integers(1000, 50001)), int(rng.integers(16, 257))
         if m >= 8 * n:
             out.append((m, n))
-    return out
+    return list(enumerate(out))[count * rank:]
 
 
 def make_batched(shapes, dev, kappa=1e6, noise=1e-6, seed=12):
     """A_p = U_p diag(sigma) V_p^T (orthonormal factors of seeded Gaussian
-    matrices, sigma log-spaced to kappa), b_p = A_p x* + noise, on the GPU."""
+    matrices, sigma log-spaced to kappa), b_p = A_p x* + noise, on the GPU;
+    problem p's data depends only on its global index."""
     import torch
     g = torch.Generator(device=dev)
-    g.manual_seed(seed)
     probs = []
-    for m, n in shapes:
+    for p, (m, n) in shapes:
+        g.manual_seed(seed * 1000003 + p)
         U = torch.linalg.qr(torch.randn(m, n, generator=g, device=dev, dtype=torch.float64))[0]
         V = torch.linalg.qr(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64))[0]
         sig = torch.logspace(0, -math.log10(kappa), n, device=dev, dtype=torch.float64)
@@ -405,8 +412,9 @@ def run_batched(args, rank, local, ws):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     lib = R.lib()
-    shapes = batched_shapes(args.problems)
-    probs = make_batched(shapes, dev)
+    indexed = batched_shapes(args.problems, rank=rank, world=ws)
+    probs = make_batched(indexed, dev)
+    shapes = [mn for _, mn in indexed]
     tol, sf = 1e-12, CFG["sampling_factor"]
     o = R.options(precision=R.Precision.BF16X, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol)
     o64 = R.options(precision=R.Precision.FP64, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol)
@@ -475,11 +483,12 @@ def run_batched(args, rank, local, ws):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 digit-sliced sketch + float-float (fp32 pairs) QR/LSQR",
         "data": "synthetic (seeded torch CUDA generator)",
-        "config": {"workload": "%d blendenpik problems, m in [1000, 50000], n in [16, 256], m >= 8n, "
+        "config": {"workload": "%d blendenpik problems per rank, m in [1000, 50000], n in [16, 256], m >= 8n, "
                                "kappa 1e6, d = 4n, lsqr tol 1e-12, one rnla_solve_batched call per step"
                                % len(probs),
                    "problems": len(probs), "total_A_GB": sum(8.0 * m * n for m, n in shapes) / 1e9,
-                   "l2": "inputs larger than L2", "parallelism": "replicas" if ws > 1 else "single"},
+                   "l2": "inputs larger than L2",
+                   "parallelism": "problems sharded over %d ranks, no collective" % ws if ws > 1 else "single"},
         "accuracy": {"max_abs_diff_rel_residual_vs_lapack_first4": worst},
         "mean_iterations": float(np.mean(its)),
         "stages_mean_ms": {k: float(np.mean([s_[k] for s_ in stats]))

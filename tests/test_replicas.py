@@ -56,3 +56,17 @@ def test_reference_arm_runs_on_rank_zero_only():
     class Args:
         m, n, steps, warmup = 100000, 500, 1, 0
     assert bench.run_reference(Args, 1, 2) is None
+
+
+def test_batched_problems_shard_without_overlap():
+    """bench.py --workload batched under N ranks: rank r solves problems
+    [r P, (r + 1) P) of one seeded sequence, so the ranks' shares are
+    disjoint, equal in count, and together the single-rank sequence."""
+    sys.path.insert(0, ROOT)
+    import bench
+    P = 40
+    whole = bench.batched_shapes(3 * P)
+    parts = [bench.batched_shapes(P, rank=r, world=3) for r in range(3)]
+    assert all(len(p) == P for p in parts)
+    assert [x for p in parts for x in p] == whole
+    assert all(m >= 8 * n and 1000 <= m <= 50000 and 16 <= n <= 256 for _, (m, n) in whole)
