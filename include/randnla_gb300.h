@@ -201,8 +201,9 @@ RNLA_API int rnla_lsqr_dev(const double* a_dev, int64_t m, int64_t n, int64_t ld
  * by every GPU that loads it until the process exits); a problem needs
  * 8 * (10 + 4G + m + 5n + G n) bytes, G <= 4 x (number of SMs), and larger
  * problems return RNLA_ERR_INVALID_DIMENSIONS.  Calls share that array, so
- * calls that overlap on the GPU race; the first call on a device looks up the
- * array's address and should come before any stream capture.  Synchronises. */
+ * calls on one device are serialised (a per-device lock held until the call
+ * has synchronised); the first call on a device looks up the array's address
+ * and should come before any stream capture.  Synchronises. */
 RNLA_API int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda,
                                    const double* b_dev, double damp, double atol, double btol,
                                    double conlim, int64_t iter_lim, const double* x0_dev,

@@ -19,8 +19,10 @@
 //   * every call shares the array and leaves its contents behind; the words
 //     that must start at zero are cleared by each call, the rest is written
 //     before it is read;
-//   * calls that overlap on the GPU (two streams, or two threads) race on the
-//     array: serialise them;
+//   * calls on one device are serialised: each holds that device's lock
+//     from before its first launch until it has synchronised on its result,
+//     so calls from several host threads or streams never overlap on the
+//     array;
 //   * the first call on a device looks the array's device address up
 //     (cudaGetSymbolAddress, with that device current) and caches it; make
 //     that first call before any stream capture.
@@ -36,6 +38,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[RNLA_NOALLOC_SC
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
+std::mutex g_noalloc_call_mu[kMaxDevices];   // one call per device at a time
 void* g_noalloc_ptr[kMaxDevices] = {};
 int g_noalloc_sms[kMaxDevices] = {};
 
@@ -75,6 +78,9 @@ extern "C" int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, 
     if (lda < m) fail(RNLA_ERR_INVALID_PARAMETERS, "leading dimension smaller than rows");
     int dev = 0;
     RNLA_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) fail(RNLA_ERR_CUDA, "device index out of range");
+    // held until lsqr_run_in_workspace has synchronised on the result
+    std::lock_guard<std::mutex> call(g_noalloc_call_mu[dev]);
     int sms = 0;
     void* ws = noalloc_scratch(dev, &sms);
     const size_t need = lsqr_workspace_bytes(m, n, sms, nullptr, nullptr, nullptr);
