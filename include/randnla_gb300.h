@@ -118,7 +118,8 @@ RNLA_API int rnla_sketching_operator_f32_dev(int32_t dist, int64_t rows, int64_t
 typedef enum {
     RNLA_PREC_FP64 = 0,      /* every product in FP64 on CUDA cores: the plain FP64 GPU path */
     RNLA_PREC_BF16X = 1,     /* tensor-core bf16 digit-sliced products with exact chunk sums */
-    RNLA_PREC_BF16 = 2       /* single bf16 digit, FP32 accumulation (fast, low accuracy) */
+    RNLA_PREC_BF16 = 2       /* RNLA_PREC_BF16X with one 8-bit digit per operand (fast, low accuracy);
+                                other values: RNLA_ERR_INVALID_PARAMETERS */
 } rnla_precision;
 
 typedef enum {

@@ -31,10 +31,30 @@ struct StageTimer {
     }
 };
 
+// RNLA_PREC_BF16 is the tensor-core path with a single 8-bit digit per
+// operand; any other value than the three precisions is an error.
+static void resolve_precision(int32_t& prec, int32_t& digits_a, int32_t& digits_b) {
+    if (prec == RNLA_PREC_BF16) {
+        prec = RNLA_PREC_BF16X;
+        digits_a = 1;
+        digits_b = 1;
+    } else if (prec != RNLA_PREC_FP64 && prec != RNLA_PREC_BF16X) {
+        fail(RNLA_ERR_INVALID_PARAMETERS, "unknown precision");
+    }
+}
+
+// The caller's options (or the defaults) with the precision resolved and
+// the enumerations checked.
 static rnla_options opts_or_default(const rnla_options* o) {
     rnla_options d;
     rnla_options_default(&d);
-    return o ? *o : d;
+    if (o) d = *o;
+    resolve_precision(d.precision, d.digits_a, d.digits_b);
+    if (d.mode != RNLA_MODE_REFERENCE && d.mode != RNLA_MODE_RANDNLA)
+        fail(RNLA_ERR_INVALID_PARAMETERS, "unknown rand_svd mode");
+    if (d.inner_solver != RNLA_SOLVER_CGLS && d.inner_solver != RNLA_SOLVER_LSQR)
+        fail(RNLA_ERR_INVALID_PARAMETERS, "unknown inner solver");
+    return d;
 }
 
 static void check_mat(int64_t m, int64_t n, int64_t ld) {
@@ -1016,7 +1036,12 @@ int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsil
     if (count > 0 && (!probs || !status_out))
         return abi_error(RNLA_ERR_INVALID_PARAMETERS, "probs and status_out are required");
     if (count == 0) return abi_ok();
-    const rnla_options o = opts_or_default(opt);
+    rnla_options o;
+    try {
+        o = opts_or_default(opt);
+    } catch (const Error& e) {
+        return abi_error(e.code, e.what());
+    }
     int first = RNLA_OK;
     std::string first_msg;
     for (int64_t p = 0; p < count; ++p) {
@@ -1148,6 +1173,8 @@ int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64_t m, int
     if (d <= 0 || m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "empty sketch product");
     if (dist != RNLA_GAUSSIAN && dist != RNLA_UNIFORM && dist != RNLA_RADEMACHER)
         fail(RNLA_ERR_INVALID_PARAMETERS, "unknown distribution");
+    int32_t unused = 0;
+    resolve_precision(precision, digits, unused);
     Ctx ctx((cudaStream_t)stream);
     const RngKey key = key_of(rng);
     if (precision == RNLA_PREC_FP64) {
@@ -1183,6 +1210,7 @@ int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, co
     RNLA_API_BEGIN
     check_mat(k, mm, ldx);
     check_mat(k, nn, ldy);
+    resolve_precision(precision, digits_x, digits_y);
     Ctx ctx((cudaStream_t)stream);
     if (precision != RNLA_PREC_FP64 && !tc_available(ctx))
         fail(RNLA_ERR_UNSUPPORTED, "sm_103a tensor-core kernels unavailable");

@@ -72,6 +72,13 @@ def test_batched_argument_errors_need_no_device():
     assert lib.rnla_solve_batched((R.LsProblem * 1)(), 1, 1e-8, 10, 4.0, None, None, None, None) \
         == R.InvalidParameters.code
     assert lib.rnla_solve_batched(None, 0, 1e-8, 10, 4.0, None, None, None, None) == 0
+    # option enumerations are checked before any device work
+    one = (R.LsProblem * 1)()
+    for field, bad in (("precision", 7), ("mode", 3), ("inner_solver", 2)):
+        o = R.options()
+        setattr(o, field, bad)
+        assert lib.rnla_solve_batched(one, 1, 1e-8, 10, 4.0, ctypes.byref(o), st, None, None) \
+            == R.InvalidParameters.code, field
 
 
 def test_no_oracle_in_product():
