@@ -66,6 +66,11 @@ RNLA_API int rnla_device_count(void);
 /* Number of kernels this library has launched in the process so far (a
  * diagnostic counter; bench.py reports launches inside its timed region). */
 RNLA_API uint64_t rnla_kernel_launches(void);
+/* Scratch memory comes from one stream-ordered pool per device that keeps
+ * freed blocks for the next call (no context handle to create or destroy).
+ * This returns the blocks no call is using to the driver; call it when the
+ * library is idle.  A no-op before the first GPU call. */
+RNLA_API int rnla_release_cached_memory(void);
 
 /* ---- sketch distributions: src/sketch.rs:9-13 ---- */
 typedef enum { RNLA_GAUSSIAN = 0, RNLA_UNIFORM = 1, RNLA_RADEMACHER = 2 } rnla_distribution;

@@ -16,9 +16,15 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 // ---------------------------------------------------------------------------
 // Stream-ordered pool (one per device, never shrinks between calls)
 // ---------------------------------------------------------------------------
+// One stream-ordered pool per device, created on first use.  Its release
+// threshold is unlimited, so steady-state solves take every scratch buffer
+// from memory the pool already holds; rnla_release_cached_memory() trims it.
+static std::mutex g_pool_mu;
+static std::map<int, cudaMemPool_t> g_pools;
+
 static cudaMemPool_t device_pool(int dev) {
-    static std::mutex mu;
-    static std::map<int, cudaMemPool_t> pools;
+    std::mutex& mu = g_pool_mu;
+    std::map<int, cudaMemPool_t>& pools = g_pools;
     std::lock_guard<std::mutex> g(mu);
     auto it = pools.find(dev);
     if (it != pools.end()) return it->second;
@@ -294,6 +300,13 @@ const char* rnla_last_error_message(void) { return t_last_error.c_str(); }
 const char* rnla_version(void) { return "0.1.0 sm_103a"; }
 
 uint64_t rnla_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int rnla_release_cached_memory(void) {
+    RNLA_API_BEGIN
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    for (auto& kv : g_pools) RNLA_CUDA(cudaMemPoolTrimTo(kv.second, 0));
+    RNLA_API_END
+}
 
 int rnla_device_count(void) {
     int n = 0;

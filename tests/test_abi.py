@@ -61,6 +61,11 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.LsProblem) == 8 + 8 + 24 + 16
 
 
+def test_release_cached_memory_before_any_gpu_call():
+    import randnla_gb300 as R
+    assert R.lib().rnla_release_cached_memory() == 0
+
+
 def test_batched_argument_errors_need_no_device():
     """rnla_solve_batched rejects a negative count or missing arrays before
     touching the GPU; an empty batch is fine."""

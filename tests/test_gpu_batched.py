@@ -101,3 +101,18 @@ def test_batched_workload_sample(rnla):
 
 def test_empty_batch(rnla):
     assert rnla.solve_batched_dev([], 1e-12, 100, 4.0) == ([], [])
+
+
+def test_cached_memory_release_between_batches(rnla):
+    """rnla_release_cached_memory trims the pools; later solves allocate
+    again and give the same result."""
+    import torch
+    A, b = _problem(3000, 50, 1e5, 1e-6, seed=7)
+    p1, p2 = _dev(A, b), _dev(A, b)
+    o = _opts(rnla, rnla.Precision.BF16X)
+    assert rnla.solve_batched_dev([p1], 1e-12, 2000, 4.0, o)[0] == [0]
+    torch.cuda.synchronize()
+    assert rnla.lib().rnla_release_cached_memory() == 0
+    assert rnla.solve_batched_dev([p2], 1e-12, 2000, 4.0, o)[0] == [0]
+    torch.cuda.synchronize()
+    assert torch.equal(p1[2], p2[2])
