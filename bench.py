@@ -532,6 +532,24 @@ def cpu_sample(m_full, n, iters, sample_rows):
     return total, 1.0 / (total * m_full / ms)
 
 
+def lapack_sample(m_full, n, sample_rows):
+    """numpy/LAPACK FP64 least squares (gelsd through numpy.linalg.lstsq, all
+    host threads) on the same kind of row sample as cpu_sample.  Returns
+    (seconds for the sample, full-size solves/s by linear scaling in m: the
+    cost is O(m n^2))."""
+    import numpy as np
+    rng = np.random.default_rng(1)
+    U = np.linalg.qr(rng.standard_normal((sample_rows, n)))[0]
+    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    A = np.asfortranarray((U * np.logspace(0, -8, n)) @ V.T)
+    b = A @ rng.standard_normal(n) + 1e-6 * rng.standard_normal(sample_rows)
+    np.linalg.lstsq(A[:1000], b[:1000], rcond=None)          # load LAPACK once
+    t0 = time.perf_counter()
+    np.linalg.lstsq(A, b, rcond=None)
+    t = time.perf_counter() - t0
+    return t, 1.0 / (t * m_full / sample_rows)
+
+
 def run_reference(args, rank, ws):
     """The reference arm: the oracle's CPU restatement of the reference's
     path on the host cores, rank 0 only."""
@@ -588,6 +606,11 @@ def main():
                       "host threads, C sketch generator) on %d x %d rows, %d CGLS iterations "
                       "(the GPU's iteration count), %.2f s, scaled linearly in m to %d rows"
                       % (rows, args.n, iters, t, args.m)}
+        tl, vl = lapack_sample(args.m, args.n, rows)
+        line["cpu_baseline"]["lapack_lstsq"] = {
+            "value": vl, "unit": UNIT, "cores": os.cpu_count(),
+            "sample": "numpy.linalg.lstsq (LAPACK gelsd, FP64, all host threads) on %d x %d rows, "
+                      "%.2f s, scaled linearly in m to %d rows" % (rows, args.n, tl, args.m)}
     if rank == 0:
         print(json.dumps(line))
 
