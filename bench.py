@@ -179,6 +179,12 @@ def make_problem(m, n, kappa, noise, dev):
     return A, b
 
 
+def workload_name(m, n):
+    """The bench workload's name, shared by both arms' JSON lines."""
+    return "blendenpik_overdetermined %dx%d kappa=1e8 d=%d lsqr tol=1e-12" % (
+        m, n, int(CFG["sampling_factor"] * n))
+
+
 def rel_residual(A, x, b):
     return float((A @ x - b).norm() / b.norm())
 
@@ -346,8 +352,7 @@ def run_ours(args, rank, local, ws):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 digit-sliced sketch + float-float (fp32 pairs) QR/LSQR" if tc else "f64",
         "data": "synthetic (seeded torch CUDA generator)",
-        "config": {"workload": "blendenpik_overdetermined %dx%d kappa=1e8 d=%d lsqr tol=1e-12"
-                               % (m, n, int(CFG["sampling_factor"] * n)),
+        "config": {"workload": workload_name(m, n),
                    "m": m, "n": n, "d": int(CFG["sampling_factor"] * n), "kappa": CFG["kappa"],
                    "precision": "BF16X" if tc else "FP64", "inner_solver": "LSQR",
                    "l2": "inputs larger than L2 (A is %d MB)" % (elem >> 20),
@@ -570,9 +575,11 @@ def run_reference(args, rank, ws):
         "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy generator)",
         "impl": "reference",
-        "config": {"workload": "blendenpik_overdetermined %dx%d kappa=1e8 d=%d" %
-                               (args.m, args.n, int(CFG["sampling_factor"] * args.n)),
-                   "m": args.m, "n": args.n},
+        "config": {"workload": workload_name(args.m, args.n), "m": args.m, "n": args.n,
+                   "d": int(CFG["sampling_factor"] * args.n), "kappa": CFG["kappa"],
+                   "algorithm": "the reference's data flow: dense Gaussian S, S a, Householder QR, "
+                                "explicit a R^-1, CGLS (%d iterations, the count LSQR needs at "
+                                "tol 1e-12 on this problem, within a few)" % iters},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "oracle restatement of sketch_and_precondition.rs:26-59 "
                                    "(numpy/LAPACK on all host threads, C sketch generator) on "
