@@ -55,6 +55,8 @@ def lib():
         L.oracle_threefry2x64.argtypes = [u64p, u64p, u64p]
         L.oracle_word_stream.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
                                          ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p]
+        L.oracle_word_checksums.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64,
+                                            ctypes.c_uint64, ctypes.c_int64, u64p, u64p]
         L.oracle_sketch_fill.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                          ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_void_p, ctypes.c_int64]
@@ -109,6 +111,13 @@ def word_stream(gen, key0, key1, first_word, n):
     out = np.empty(n, dtype=np.uint32)
     lib().oracle_word_stream(gen, key0, key1, first_word, n, out.ctypes.data)
     return out
+
+
+def word_checksums(gen, key0, key1, first_word, n):
+    """(sum of the words, sum of word xor offset) of n stream words, mod 2^64."""
+    s1, s2 = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    lib().oracle_word_checksums(gen, key0, key1, first_word, n, ctypes.byref(s1), ctypes.byref(s2))
+    return s1.value, s2.value
 
 
 def sketch(dist, rows, cols, gen=GEN_PHILOX4X32, key0=0, key1=0, quantized=False):

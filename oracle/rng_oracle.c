@@ -180,6 +180,26 @@ void oracle_word_stream(int gen, uint64_t key0, uint64_t key1, uint64_t first_wo
     }
 }
 
+/* Checksums of n stream words from first_word, one block evaluation per
+ * four words: s1 = sum of the words, s2 = sum of (word xor the low 32 bits
+ * of its offset t), both mod 2^64.  s2 changes when words trade places. */
+void oracle_word_checksums(int gen, uint64_t key0, uint64_t key1, uint64_t first_word,
+                           int64_t n, uint64_t *s1, uint64_t *s2) {
+    uint64_t a = 0, b = 0;
+    int64_t t = 0;
+    while (t < n) {
+        uint64_t L = first_word + (uint64_t)t;
+        uint32_t w[4];
+        block_words(gen, key0, key1, L >> 2, w);
+        for (unsigned j = (unsigned)(L & 3); j < 4 && t < n; ++j, ++t) {
+            a += w[j];
+            b += (uint64_t)(w[j] ^ (uint32_t)t);
+        }
+    }
+    *s1 = a;
+    *s2 = b;
+}
+
 /* ------------------------------------------------------------------ */
 /* Sketch-entry transforms (this project's definition; see header)     */
 /* ------------------------------------------------------------------ */

@@ -30,6 +30,29 @@ def test_streams_match_oracle_at_offsets(rnla, gen):
         assert np.array_equal(g, o)
 
 
+@pytest.mark.parametrize("gen", [0, 1])
+def test_stream_checksums_over_1e8_counters(rnla, gen):
+    """1e8 generator counters (4e8 words) against the oracle's C generator:
+    the sum of the words and the sum of word xor offset, both exact."""
+    import ctypes
+    import torch
+    n = 400_000_000
+    key0, key1 = 0x0123456789ABCDEF, 77
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    r = rnla._rng(gen, key0, key1)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert rnla.lib().rnla_rng_words_dev(ctypes.byref(r), 0, n, ctypes.c_void_p(out.data_ptr()), stream) == 0
+    s1 = s2 = 0
+    chunk = 50_000_000
+    for c0 in range(0, n, chunk):
+        w = out[c0:c0 + chunk]
+        idx = torch.arange(c0, c0 + w.numel(), dtype=torch.int32, device="cuda")
+        s1 += int((w.long() & 0xFFFFFFFF).sum())
+        s2 += int(((w ^ idx).long() & 0xFFFFFFFF).sum())
+    del out
+    assert (s1, s2) == O.word_checksums(gen, key0, key1, 0, n)
+
+
 @pytest.mark.parametrize("dist", [0, 1, 2])
 @pytest.mark.parametrize("gen", [0, 1])
 def test_sketching_operator_bit_exact(rnla, dist, gen):

@@ -41,6 +41,15 @@ def test_word_stream_is_block_sequence(golden):
     assert np.array_equal(full[333:434], part)
 
 
+@pytest.mark.parametrize("gen", [0, 1])
+def test_word_checksums_match_the_stream(gen):
+    first, n = 5, 100003
+    w = O.word_stream(gen, 0x0123456789ABCDEF, 77, first, n)
+    s1, s2 = O.word_checksums(gen, 0x0123456789ABCDEF, 77, first, n)
+    assert s1 == int(w.astype(np.uint64).sum())
+    assert s2 == int((w ^ np.arange(n, dtype=np.uint32)).astype(np.uint64).sum())
+
+
 def test_counter_carry():
     """Block 2^32 carries into the second counter word (philox.rs:89-91)."""
     w = O.word_stream(O.GEN_PHILOX4X32, 5, 0, 4 * (1 << 32), 4)
