@@ -101,3 +101,13 @@ def test_rand_svd_randnla_fp64(rnla):
     Uo, so, Vto = O.rand_svd_randnla(A, 50, 10, 2, seed=42)
     np.testing.assert_allclose(np.diag(S), so, rtol=1e-10)
     assert np.allclose(U.T @ U, np.eye(50), atol=1e-12)
+    # the figures of the randomized range finder: ||A - U S Vt||_F against the
+    # oracle's and the optimal rank-50 error, the top-k sigma against the
+    # construction (oracle on this matrix: 1.0068 x optimal, 2.4% worst sigma)
+    err = np.linalg.norm(A - U @ S @ Vt)
+    err_o = np.linalg.norm(A - (Uo * so) @ Vto)
+    tail = np.sqrt(np.sum(sig[50:] ** 2))
+    assert abs(err - err_o) < 1e-8
+    assert err < 1.01 * tail
+    rel = np.abs(np.diag(S) - sig[:50]) / sig[:50]
+    assert rel.max() < 0.03 and rel[0] < 1e-6
