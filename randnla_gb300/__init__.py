@@ -379,7 +379,18 @@ def _stream():
 
 
 def _dptr(t):
-    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+    """Device pointer of a torch CUDA tensor on the current device (None
+    passes through).  Any other tensor is refused here, before the library
+    could use its address as device memory."""
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise ValueError("expected a CUDA tensor, got one on %s" % t.device)
+    import torch
+    if t.device.index != torch.cuda.current_device():
+        raise ValueError("tensor on %s, but the current device is cuda:%d"
+                         % (t.device, torch.cuda.current_device()))
+    return ctypes.c_void_p(t.data_ptr())
 
 
 def _ld(t):

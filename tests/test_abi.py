@@ -93,3 +93,18 @@ def test_no_oracle_in_product():
             with open(path) as f:
                 txt = f.read()
             assert "oracle" not in txt.lower(), path
+
+
+def test_device_wrappers_refuse_host_tensors():
+    """The _dev wrappers check every tensor before the library sees its
+    address: a CPU tensor is a ValueError, not a device access."""
+    import torch
+    import randnla_gb300 as R
+    a = torch.zeros((100, 10), dtype=torch.float64).t().contiguous().t()
+    b = torch.zeros(100, dtype=torch.float64)
+    x = torch.zeros(10, dtype=torch.float64)
+    with pytest.raises(ValueError):
+        R.blendenpik_dev(a, b, x, 1e-8, 10, 4.0)
+    with pytest.raises(ValueError):
+        R.solve_batched_dev([(a, b, x)], 1e-8, 10, 4.0)
+    assert R._dptr(None) is None
