@@ -13,6 +13,7 @@ matrices of the solver/driver tests, so nothing here is typed by hand:
 * src/solvers.rs:290-338                 upper-triangular solve cases
 * src/solvers.rs:391-410                 lsqr 3x2 system, x ~ [1, -1]
 * src/cg.rs:130-184                      cgls 3x3 cases
+* src/lora_drivers.rs:506-514, 702-710   the 3 x 3 matrix rand_evd1 / rand_evd2 reject
 
 The fixtures are committed; the tests read only the JSON, never the
 reference tree.
@@ -59,6 +60,8 @@ def main(ref):
         solvers = f.read()
     with open(os.path.join(ref, "src/cg.rs")) as f:
         cg = f.read()
+    with open(os.path.join(ref, "src/lora_drivers.rs")) as f:
+        drivers = f.read()
 
     rng = {
         "source": "rust-random123/src/philox.rs:242-295, threefry.rs:97-110",
@@ -113,8 +116,16 @@ def main(ref):
         cg_cases.append({"name": name.split()[-1], "a_rowmajor": a, "b": b,
                          "tolerance": tol, "num_iterations": iters, "x0": x0})
 
-    solv = {"source": "src/solvers.rs, src/cg.rs", "upper_triangular": tri,
-            "lsqr_simple": lsqr_case, "cgls": cg_cases}
+    # the non-symmetric matrix both rand_evd drivers must reject
+    evd = {}
+    for name in ("fn test_wrong_hermitian", "fn test_wrong_psd"):
+        j = drivers.index(name)
+        m = re.search(r"dmatrix!\[(.*?)\];", drivers[j:], re.S)
+        rows = [[float(t) for t in row.split(",")] for row in m.group(1).split(";")]
+        evd[name.split()[-1]] = rows
+
+    solv = {"source": "src/solvers.rs, src/cg.rs, src/lora_drivers.rs", "upper_triangular": tri,
+            "lsqr_simple": lsqr_case, "cgls": cg_cases, "rand_evd_reject": evd}
 
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "rng_kat.json"), "w") as f:

@@ -63,7 +63,7 @@ def test_errors(rnla):
         rnla.rand_evd2(C, 3, 2)
 
 
-def test_reference_known_answers(rnla):
+def test_reference_known_answers(rnla, golden):
     """The reference's rand_evd tests with fixed answers
     (lora_drivers.rs:506-514, 532-563, 702-710, 725-746, 748-776)."""
     Z = np.zeros((5, 5))
@@ -76,7 +76,7 @@ def test_reference_known_answers(rnla):
     assert V.shape == (5, 3) and len(lam) == 3
     V, lam = rnla.rand_evd2(np.eye(5), 3, 2)
     assert V.shape == (5, 3) and len(lam) == 3
-    W = np.array([[1.0, 2.0, 3.0], [100.0, 200.0, 4.0], [3.0, 38.0, 1.0]])
+    W = np.array(golden["solvers"]["rand_evd_reject"]["test_wrong_hermitian"])
     with pytest.raises(rnla.NotHermitian):
         rnla.rand_evd1(W, 3, 1e-6, 2)
     with pytest.raises(rnla.RandNLAError):

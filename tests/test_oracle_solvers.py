@@ -195,7 +195,7 @@ def test_rand_evd_restatements():
     np.testing.assert_allclose(lam2, [20.0, 10.0, 5.0], rtol=1e-3)
 
 
-def test_rand_evd_reference_known_answers():
+def test_rand_evd_reference_known_answers(golden):
     """The reference's rand_evd tests with fixed answers
     (lora_drivers.rs:506-514, 532-563, 702-710, 725-746, 748-776)."""
     Z = np.zeros((5, 5))
@@ -206,7 +206,7 @@ def test_rand_evd_reference_known_answers():
         O.rand_evd2(Z, 3, 2)                                   # Cholesky of S^T 0 fails
     assert len(O.rand_evd1(np.eye(5), 3, 1e-6, 2)[1]) == 3
     assert len(O.rand_evd2(np.eye(5), 3, 2)[1]) == 3
-    W = np.array([[1.0, 2.0, 3.0], [100.0, 200.0, 4.0], [3.0, 38.0, 1.0]])
+    W = np.array(golden["solvers"]["rand_evd_reject"]["test_wrong_hermitian"])
     with pytest.raises(O.NotHermitian):
         O.rand_evd1(W, 3, 1e-6, 2)
     with pytest.raises(ValueError):
