@@ -285,7 +285,8 @@ RNLA_API int rnla_rand_svd(const double* a, int64_t m, int64_t n, int64_t lda, i
                   int64_t ldvt, int64_t* r_out);
 /* Extended form: options select reference / RandNLA mode, precision, q and
  * the generator; `singular_values` (nullable, r values) receives the
- * diagonal of S; stats (nullable). */
+ * diagonal of S; stats (nullable).  Both modes run in FP64; a tensor-core
+ * precision returns RNLA_ERR_UNSUPPORTED. */
 RNLA_API int rnla_rand_svd_ex(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double epsilon,
                      int64_t s, const rnla_options* opt, double* u, int64_t ldu, double* sigma,
                      int64_t lds, double* vt, int64_t ldvt, int64_t* r_out, rnla_stats* stats);
@@ -413,9 +414,10 @@ RNLA_API int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64
                                       int64_t d, int32_t dist, const rnla_rng* rng, int32_t precision,
                                       int32_t digits, double* y_dev, int64_t ldy, void* stream);
 
-/* C (ldc) = X^T Y for X (k x mm, ldx) and Y (k x nn, ldy), both double,
- * in the given precision (FP64 CUDA cores or bf16 digit-sliced tensor cores
- * with exact chunk sums). */
+/* C (ldc) = X^T Y for X (k x mm, ldx) and Y (k x nn, ldy), both double, on
+ * the FP64 CUDA cores.  The tensor-core precisions return
+ * RNLA_ERR_UNSUPPORTED: a two-sided digit-sliced GEMM is not built (the
+ * tensor-core kernel applies a generated sketch to one data operand). */
 RNLA_API int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, const double* y_dev,
                      int64_t nn, int64_t ldy, int32_t precision, int32_t digits_x,
                      int32_t digits_y, double* c_dev, int64_t ldc, void* stream);

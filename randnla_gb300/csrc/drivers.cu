@@ -384,38 +384,29 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
         tm.mark();
         r = svd_finish(ctx, o.precision, Q.p(), m, cq, B, n, k, U, ldu, sig, Vt, ldvt);
     } else {
-        // Gaussian range finder, q power iterations, re-orthonormalised after every product
+        // Gaussian range finder, q power iterations, re-orthonormalised after
+        // every product.  FP64 only: A^T Q and Q^T A would need a two-sided
+        // digit-sliced tensor-core GEMM, which is not built (the tensor-core
+        // kernel applies a generated sketch to one data operand).
+        const int prec = o.precision;
+        if (prec != RNLA_PREC_FP64)
+            fail(RNLA_ERR_UNSUPPORTED, "rand_svd in RandNLA mode runs in FP64 only");
         int64_t l = k + s;
         const int64_t mn = m < n ? m : n;
         if (l > mn) l = mn;
-        const int prec = o.precision;
-        if (prec != RNLA_PREC_FP64 && !tc_available(ctx))
-            fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
         const RngKey key = key_of(&o.rng);
         DevBuf<double> Y((size_t)m * l, ctx.stream), Z((size_t)n * l, ctx.stream);
         const bool force_hh = (o.orth == 1);
-        if (prec == RNLA_PREC_FP64) {
+        {
             DevBuf<double> Om((size_t)n * l, ctx.stream);
             sketch_fill_f64(ctx, DIST_GAUSSIAN, key, n, l, Om, n);
             gemm_f64(ctx, 'N', 'N', m, l, n, 1.0, A, ld, Om, n, 0.0, Y, m);
-        } else {
-            // Y = A Omega = (Omega^T A^T)^T: the sketch kernel applies Omega^T (l x n) to A^T
-            DevBuf<double> At((size_t)n * m, ctx.stream), Yt((size_t)l * m, ctx.stream);
-            transpose(ctx, m, n, A, ld, At, n);
-            tc_sketch_apply(ctx, key, At, false, n, m, n, nullptr, l, o.digits_a, Yt, l);
-            transpose(ctx, l, m, Yt, l, Y, m);
         }
         fallbacks += orthonormalize(ctx, Y, m, l, m, force_hh);
         for (int it = 0; it < o.power_iters; ++it) {
             product_tn(ctx, prec, A, m, n, ld, Y, l, m, o.digits_a, o.digits_b, Z, n);   // Z = A^T Q
             fallbacks += orthonormalize(ctx, Z, n, l, n, force_hh);
-            if (prec == RNLA_PREC_FP64) gemm_f64(ctx, 'N', 'N', m, l, n, 1.0, A, ld, Z, n, 0.0, Y, m);
-            else {
-                DevBuf<double> At((size_t)n * m, ctx.stream), Yt((size_t)l * m, ctx.stream);
-                transpose(ctx, m, n, A, ld, At, n);
-                product_tn(ctx, prec, Z, n, l, n, At, m, n, o.digits_b, o.digits_a, Yt, l);
-                transpose(ctx, l, m, Yt, l, Y, m);
-            }
+            gemm_f64(ctx, 'N', 'N', m, l, n, 1.0, A, ld, Z, n, 0.0, Y, m);            // Y = A Z
             fallbacks += orthonormalize(ctx, Y, m, l, m, force_hh);
         }
         tm.mark();

@@ -111,3 +111,22 @@ def test_rand_svd_randnla_fp64(rnla):
     assert err < 1.01 * tail
     rel = np.abs(np.diag(S) - sig[:50]) / sig[:50]
     assert rel.max() < 0.03 and rel[0] < 1e-6
+
+
+def test_tensor_core_precision_is_refused_where_not_built(rnla):
+    """rand_svd's products A^T Q and Q^T A would need a two-sided tensor-core
+    GEMM, which is not built: both the driver and the GEMM entry say so
+    instead of computing something else."""
+    import torch
+    A = np.random.default_rng(6).standard_normal((200, 100))
+    o = rnla.options(precision=rnla.Precision.BF16X, mode=rnla.Mode.RandNLA)
+    with pytest.raises(rnla.Unsupported):
+        rnla.rand_svd(A, 10, 1e-6, 5, o)
+    x = torch.randn((64, 16), dtype=torch.float64, device="cuda").t().contiguous().t()
+    y = torch.randn((64, 8), dtype=torch.float64, device="cuda").t().contiguous().t()
+    c = torch.zeros((16, 8), dtype=torch.float64, device="cuda").t().contiguous().t()
+    with pytest.raises(rnla.Unsupported):
+        rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X)
+    rnla.gemm_tn_dev(x, y, c)                       # FP64 is the built path
+    torch.cuda.synchronize()
+    assert torch.allclose(c, x.t() @ y, rtol=1e-12, atol=1e-12)
