@@ -188,7 +188,9 @@ typedef struct {
  * var (n values) is filled when calc_var != 0 and var != NULL.  arnorms,
  * if not NULL, receives the history of ||A^T r|| estimates (at most
  * iter_lim values, count = result->itn, or 1 for the early exit of
- * solvers.rs:180-182). */
+ * solvers.rs:180-182).  The persistent kernel holds the n-vectors across
+ * its threads: n <= 4096 (RNLA_ERR_UNSUPPORTED above; the reference has no
+ * limit), which also bounds the drivers built on it. */
 RNLA_API int rnla_lsqr(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double damp,
               double atol, double btol, double conlim, int64_t iter_lim, int32_t calc_var,
               const double* x0, double* x, rnla_lsqr_result* result, double* arnorms, double* var);
@@ -221,7 +223,7 @@ RNLA_API int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, in
  * ||A^T r||_2 < tolerance (absolute) or after num_iterations.  The
  * reference's alpha = ||s||^2 / ||A p||^2 is kept as written, so a zero
  * right-hand side yields NaN as it does there.  iterations_out (nullable)
- * receives the iteration count. */
+ * receives the iteration count.  n <= 4096, as for rnla_lsqr. */
 RNLA_API int rnla_cgls(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double tolerance,
               int64_t num_iterations, const double* x0, double* x, int64_t* iterations_out);
 RNLA_API int rnla_cgls_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda, const double* b_dev,
