@@ -53,6 +53,14 @@ def test_library_loads_and_answers_host_queries():
     assert lib.rnla_rand_svd_rank(10, 2, 3, 2, 0) == 2
 
 
+def test_python_mirror_declares_every_entry_point():
+    """Every C entry point has a ctypes declaration in the Python mirror."""
+    from randnla_gb300 import _lib
+    with open(_lib.__file__) as f:
+        declared = set(re.findall(r'\("(rnla_\w+)"', f.read()))
+    assert declared == declared_symbols()
+
+
 def test_struct_layouts_match_header():
     from randnla_gb300 import _lib
     assert ctypes.sizeof(_lib.Rng) == 24
