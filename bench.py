@@ -1,27 +1,35 @@
 #!/usr/bin/env python3
 """Benchmark of the sketch-and-precondition least-squares hot path.
 
-Workload (the configuration the headline metric is quoted on): overdetermined
-least squares with A of 100000 x 500, A = U diag(sigma) V^T, sigma log-spaced
-from 1 to 1e-8 (kappa = 1e8), b = A x* + 1e-6 N(0,1), Gaussian sketch
-d = 4n = 2000, preconditioned LSQR to relative tolerance 1e-12.  Inputs are
-seeded synthetic data generated on the GPU (torch CUDA generator); A (400 MB)
-is larger than L2, so no flush is needed between steps.
+Workloads (`--workload`, seeded synthetic inputs of the stated shapes; no
+dataset is involved):
+
+  precision_ls (default)  overdetermined least squares, A of 1048576 x 1024
+                          stored in FP32, A = U diag(sigma) V^T with U, V the
+                          orthonormal factors of seeded Gaussian matrices and
+                          sigma log-spaced 1 -> 1e-6 (kappa 1e6); b = A x* +
+                          1e-8 N(0,1) in FP64; Gaussian sketch d = 4096;
+                          preconditioned LSQR to tolerance 1e-10.
+  plain_ls                A of 100000 x 500 in FP64, sigma 1 -> 1e-8
+                          (kappa 1e8), b = A x* + 1e-6 N(0,1), d = 2000,
+                          LSQR to tolerance 1e-12.
+  batched                 many independent problems of mixed shape through
+                          one rnla_solve_batched call per step.
 
 One step = one blendenpik solve (sketch S [A b], QR of the sketch, R^-1,
 preconditioned LSQR, x = R^-1 z) through the library's device-pointer entry
 point.  `value` is solves/s with inputs resident in HBM; `e2e` is the same
 metric through the host-pointer entry point with pinned host buffers (A and b
-copied in, x copied out inside the timed region).
+copied in, x copied out inside the timed region).  A is larger than L2 in
+every workload, so no flush is needed between steps.
+
+The CPU legs (`cpu_baseline` and `--impl reference`) run the oracle's
+restatement of the reference path at the FULL size of the workload: no row
+sampling, no extrapolation; each CPU solve runs in a subprocess with a
+10-minute cap and is reported as "not finished (cap)" if it exceeds it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-    python bench.py --workload batched [--problems P]   # secondary line
-
-`--workload batched` times many independent problems of mixed shape
-(m in [1000, 50000], n in [16, 256], m >= 8 n, kappa 1e6) through one
-rnla_solve_batched call per step, beside a loop of plain FP64 solves.
-Under torchrun each rank takes its own P problems of the sequence (no
-collective): value = all ranks' problems / the slowest rank's time.
+                    [--workload precision_ls|plain_ls|batched]
 
 With N > 1 (torchrun) every rank solves its own replica (the path has no
 exchange step); value = all ranks' solves / max-over-ranks time.
@@ -41,24 +49,56 @@ sys.path.insert(0, ROOT)
 
 METRIC = "rand_svd & sketch-LS solves/sec on 1 GB300: BF16-sketch vs plain FP64 at stated error"
 UNIT = "solves/s"
-CFG = dict(m=100000, n=500, kappa=1e8, noise=1e-6, sampling_factor=4.0, tol=1e-12)
+CPU_CAP_S = 600.0
+WORKLOADS = {
+    "precision_ls": dict(m=1048576, n=1024, kappa=1e6, noise=1e-8, sampling_factor=4.0, tol=1e-10,
+                         f32=True, seeds=(8, 9, 10, 11)),
+    "plain_ls": dict(m=100000, n=500, kappa=1e8, noise=1e-6, sampling_factor=4.0, tol=1e-12,
+                     f32=False, seeds=(1, 2, 3, 4)),
+}
+# DRAM bytes (read + write) per row and pass of lsqr_ff_kernel from one ncu
+# capture (40000 x 500, float-float copy, 36 passes: 5.8198 GB read + 0.0375
+# GB written); per row and pass the kernel moves 8 ldf + 16 bytes.
 LSQR_DRAM_BYTES_PER_ROW_PASS = (5.819774e9 + 0.0375055e9) / (36 * 40000)
+LSQR_NCU_ALGO_BYTES_PER_ROW_PASS = 8 * 500 + 16
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--m", type=int, default=CFG["m"])
-    p.add_argument("--n", type=int, default=CFG["n"])
+    p.add_argument("--workload", choices=["precision_ls", "plain_ls", "batched"], default="precision_ls")
+    p.add_argument("--m", type=int, default=None, help="rows (default: the workload's)")
+    p.add_argument("--n", type=int, default=None, help="columns (default: the workload's)")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison path")
-    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    p.add_argument("--workload", choices=["blendenpik", "batched"], default="blendenpik",
-                   help="batched: many small problems through rnla_solve_batched (secondary line)")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
     p.add_argument("--problems", type=int, default=512, help="problems in the batched workload")
-    return p.parse_args()
+    p.add_argument("--cpu-leg", choices=["port", "lapack"], default=None, help=argparse.SUPPRESS)
+    return p.parse_args(argv)
+
+
+def workload(args):
+    """The workload's parameters with the command line's --m / --n applied."""
+    wl = dict(WORKLOADS[args.workload])
+    if args.m:
+        wl["m"] = args.m
+    if args.n:
+        wl["n"] = args.n
+    wl["d"] = int(wl["sampling_factor"] * wl["n"])
+    return wl
+
+
+def workload_config(args, wl, ws):
+    """The `config` object both arms print (identical, so the lines compare)."""
+    return {"workload": "blendenpik_overdetermined %dx%d %s kappa=%g d=%d lsqr tol=%g"
+                        % (wl["m"], wl["n"], "fp32" if wl["f32"] else "fp64", wl["kappa"], wl["d"], wl["tol"]),
+            "name": args.workload, "m": wl["m"], "n": wl["n"], "d": wl["d"], "kappa": wl["kappa"],
+            "a_storage": "fp32" if wl["f32"] else "fp64", "tol": wl["tol"],
+            "l2": "inputs larger than L2 (A is %d MB)" % ((wl["m"] * wl["n"] * (4 if wl["f32"] else 8)) >> 20),
+            "parallelism": "replicas" if ws > 1 else "single"}
 
 
 # ---------------------------------------------------------------------------
@@ -156,46 +196,79 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # problem generation (seeded, on the GPU)
 # ---------------------------------------------------------------------------
-def make_problem(m, n, kappa, noise, dev):
-    """A = U diag(sigma) V^T with U, V the orthonormal factors (this library's
-    Householder Orth) of seeded Gaussian matrices; b = A x* + noise."""
+def make_problem(wl, dev):
+    """A = U diag(sigma) V^T with U, V the orthonormal factors of seeded
+    Gaussian matrices (m x n and n x n), sigma log-spaced 1 -> 1/kappa;
+    b = A x* + noise N(0, 1) (FP64).  The FP32 workload rounds A to FP32 and
+    forms b from the rounded A.  Returns column-major A (ld = m) and b."""
     import numpy as np
     import torch
     import randnla_gb300 as R
+    m, n = wl["m"], wl["n"]
+    su, sv, sx, sb = wl["seeds"]
     g = torch.Generator(device=dev)
-    g.manual_seed(1)
-    U = R.Orth(torch.randn(n, m, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
-    g.manual_seed(2)
-    V = R.Orth(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
-    sig = np.logspace(0, -math.log10(kappa), n)
-    Ut = torch.from_numpy(np.asfortranarray(U)).to(dev)
-    Vt = torch.from_numpy(np.ascontiguousarray(V.T * sig[:, None])).to(dev)   # diag(sigma) V^T
-    A = (Ut @ Vt).t().contiguous().t()            # column-major, ld = m
-    del Ut
-    g.manual_seed(3)
+    if wl["f32"]:
+        sig = torch.logspace(0, -math.log10(wl["kappa"]), n, device=dev, dtype=torch.float64)
+        g.manual_seed(su)
+        U = torch.linalg.qr(torch.randn(m, n, generator=g, device=dev, dtype=torch.float64))[0]
+        g.manual_seed(sv)
+        V = torch.linalg.qr(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64))[0]
+        At = (V * sig) @ U.t()                   # A^T, row-major n x m = A column-major
+        del U
+        A = At.float().t()
+        del At
+        Ad = A.double()
+    else:
+        g.manual_seed(su)
+        U = R.Orth(torch.randn(n, m, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
+        g.manual_seed(sv)
+        V = R.Orth(torch.randn(n, n, generator=g, device=dev, dtype=torch.float64).t().cpu().numpy())
+        sig = np.logspace(0, -math.log10(wl["kappa"]), n)
+        Ut = torch.from_numpy(np.asfortranarray(U)).to(dev)
+        Vt = torch.from_numpy(np.ascontiguousarray(V.T * sig[:, None])).to(dev)   # diag(sigma) V^T
+        A = (Ut @ Vt).t().contiguous().t()            # column-major, ld = m
+        del Ut
+        Ad = A
+    g.manual_seed(sx)
     xs = torch.randn(n, generator=g, device=dev, dtype=torch.float64)
-    g.manual_seed(4)
-    b = A @ xs + noise * torch.randn(m, generator=g, device=dev, dtype=torch.float64)
+    g.manual_seed(sb)
+    b = Ad @ xs + wl["noise"] * torch.randn(m, generator=g, device=dev, dtype=torch.float64)
     return A, b
 
 
-def workload_name(m, n):
-    """The bench workload's name, shared by both arms' JSON lines."""
-    return "blendenpik_overdetermined %dx%d kappa=1e8 d=%d lsqr tol=1e-12" % (
-        m, n, int(CFG["sampling_factor"] * n))
+def accuracy(A, x, b, xref=None):
+    """Relative residual ||b - A x|| / ||b||, the normwise backward error
+    ||A^T r|| / (||A||_F ||r||) and, given xref, ||x - xref|| / ||xref||,
+    all in FP64 on the GPU."""
+    Ad = A if A.dtype == x.dtype else A.to(x.dtype)
+    r = b - Ad @ x
+    rn = float(r.norm())
+    out = {"rel_residual": rn / float(b.norm()),
+           "backward_error": float((Ad.t() @ r).norm()) / (float(Ad.norm()) * rn) if rn > 0 else 0.0}
+    if xref is not None:
+        out["x_rel_diff"] = float((x - xref).norm() / xref.norm())
+    return out
 
 
-def rel_residual(A, x, b):
-    return float((A @ x - b).norm() / b.norm())
-
-
-def lapack_rel_residual(A, b):
-    """Relative residual of numpy/LAPACK least squares (host, FP64)."""
+def lapack_solve(A, b):
+    """numpy/LAPACK FP64 least squares on the host through Householder QR
+    (geqrf/orgqr, all host threads): (x, seconds)."""
     import numpy as np
-    Ah = A.cpu().numpy()
+    Ah = np.asfortranarray(A.double().cpu().numpy())
     bh = b.cpu().numpy()
-    xl = np.linalg.lstsq(Ah, bh, rcond=None)[0]
-    return float(np.linalg.norm(Ah @ xl - bh) / np.linalg.norm(bh))
+    t0 = time.perf_counter()
+    q, r = np.linalg.qr(Ah, mode="reduced")
+    import scipy.linalg
+    x = scipy.linalg.solve_triangular(r, q.T @ bh, lower=False)
+    return x, time.perf_counter() - t0
+
+
+def load_peaks():
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as f:
+            return json.load(f), "measured"
+    return {}, "fallback"
 
 
 # ---------------------------------------------------------------------------
@@ -209,33 +282,46 @@ def run_ours(args, rank, local, ws):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     lib = R.lib()
-    m, n = args.m, args.n
-    A, b = make_problem(m, n, CFG["kappa"], CFG["noise"], dev)
+    wl = workload(args)
+    m, n, d = wl["m"], wl["n"], wl["d"]
+    A, b = make_problem(wl, dev)
     x = torch.zeros(n, dtype=torch.float64, device=dev)
-    tol = CFG["tol"]
-    sf = CFG["sampling_factor"]
+    tol = wl["tol"]
+    sf = wl["sampling_factor"]
     l = 10 * n
+    esz = 4 if wl["f32"] else 8
 
-    tc = True
-    o_fast = R.options(precision=R.Precision.BF16X, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol,
-                       seed=42)
-    try:
-        R.blendenpik_dev(A, b, x, tol, l, sf, o_fast)
-    except R.Unsupported:
-        tc = False
+    o = R.options(precision=R.Precision.BF16X, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol, seed=42)
     o_fp64 = R.options(precision=R.Precision.FP64, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol,
                        seed=42)
-    o = o_fast if tc else o_fp64
+    stream = torch.cuda.current_stream()
 
-    # accuracy of the timed path against the plain FP64 path and LAPACK (cuSOLVER QR)
-    st = R.blendenpik_dev(A, b, x, tol, l, sf, o)
+    # accuracy of the timed path against the plain FP64 GPU path (same
+    # problem, same solver settings); the FP64 solve is also timed
+    R.blendenpik_dev(A, b, x, tol, l, sf, o)
     torch.cuda.synchronize()
-    rr = rel_residual(A, x, b)
     x64 = torch.zeros_like(x)
-    st64 = R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
-    torch.cuda.synchronize()
-    rr64 = rel_residual(A, x64, b)
-    rrl = lapack_rel_residual(A, b)
+    fp64 = None
+    st64 = None
+    if not args.no_fp64:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        st64 = R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = t0.elapsed_time(t1)
+        if ms64 < 2000.0:                       # short enough to repeat for a steadier figure
+            reps = 2
+            t0.record(stream)
+            for _ in range(reps):
+                R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
+            t1.record(stream)
+            torch.cuda.synchronize()
+            ms64 = t0.elapsed_time(t1) / reps
+        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_solve": ms64,
+                "iterations": st64["iterations"], "stages_ms": {k: st64[k] for k in
+                                                               ("ms_sketch", "ms_factor", "ms_solve")}}
 
     # the clock sampler runs from before the warm-up to after the timed steps
     clocks = ClockSampler(local)
@@ -247,7 +333,6 @@ def run_ours(args, rank, local, ws):
     barrier(ws)
     torch.cuda.synchronize()
     launches0 = lib.rnla_kernel_launches()
-    stream = torch.cuda.current_stream()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     solve_ms = []
@@ -264,109 +349,104 @@ def run_ours(args, rank, local, ws):
     ms_max = max_over_ranks(ms, ws)
     value = ws * args.steps / (ms_max / 1e3)
 
-    # plain FP64 GPU path throughput (same problem, same solver settings)
-    fp64 = None
-    if not args.no_fp64 and tc:
-        t0 = torch.cuda.Event(enable_timing=True)
-        t1 = torch.cuda.Event(enable_timing=True)
-        R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
-        reps = 2
-        t0.record(stream)
-        for _ in range(reps):
-            R.blendenpik_dev(A, b, x64, tol, l, sf, o_fp64)
-        t1.record(stream)
-        torch.cuda.synchronize()
-        fp64 = {"value": reps / (t0.elapsed_time(t1) / 1e3), "unit": UNIT,
-                "rel_residual": rr64, "iterations": st64["iterations"]}
+    acc = accuracy(A, x, b)
+    acc64 = accuracy(A, x64, b) if fp64 else None
+    acc["x_rel_diff_vs_fp64_path"] = float((x - x64).norm() / x64.norm()) if fp64 else None
+    if fp64:
+        acc["rel_residual_fp64_path"] = acc64["rel_residual"]
+        acc["backward_error_fp64_path"] = acc64["backward_error"]
+        acc["abs_diff_rel_residual_vs_fp64"] = abs(acc["rel_residual"] - acc64["rel_residual"])
 
     # end to end through the host-pointer entry point with pinned buffers
-    Ah = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()   # column-major host
-    Ah.copy_(A.cpu())
-    bh = torch.empty(m, dtype=torch.float64, pin_memory=True)
-    bh.copy_(b.cpu())
-    xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
-    st_e = R.Stats()
-    o_c = o
+    e2e = None
+    if not args.no_e2e:
+        dt = torch.float32 if wl["f32"] else torch.float64
+        Ah = torch.empty((n, m), dtype=dt, pin_memory=True).t()   # column-major host
+        Ah.copy_(A.cpu())
+        bh = torch.empty(m, dtype=torch.float64, pin_memory=True)
+        bh.copy_(b.cpu())
+        xh = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        st_e = R.Stats()
+        fn = lib.rnla_blendenpik_overdetermined_f32_ex if wl["f32"] else lib.rnla_blendenpik_overdetermined_ex
 
-    def e2e_call():
-        rc = lib.rnla_blendenpik_overdetermined_ex(
-            ctypes.c_void_p(Ah.data_ptr()), m, n, m, ctypes.c_void_p(bh.data_ptr()), tol, l, sf,
-            ctypes.byref(o_c), ctypes.c_void_p(xh.data_ptr()), ctypes.byref(st_e))
-        if rc != 0:
-            raise RuntimeError(lib.rnla_last_error_message().decode())
+        def e2e_call():
+            rc = fn(ctypes.c_void_p(Ah.data_ptr()), m, n, m, ctypes.c_void_p(bh.data_ptr()), tol, l, sf,
+                    ctypes.byref(o), ctypes.c_void_p(xh.data_ptr()), ctypes.byref(st_e))
+            if rc != 0:
+                raise RuntimeError(lib.rnla_last_error_message().decode())
 
-    for _ in range(2):
-        e2e_call()
-    barrier(ws)
-    t_start = time.perf_counter()
-    ke = max(2, args.steps // 2)
-    for _ in range(ke):
-        e2e_call()
-    t_e2e = time.perf_counter() - t_start
-    t_e2e = max_over_ranks(t_e2e, ws)
-    e2e_val = ws * ke / t_e2e
+        for _ in range(2):
+            e2e_call()
+        barrier(ws)
+        t_start = time.perf_counter()
+        ke = max(2, args.steps // 2)
+        for _ in range(ke):
+            e2e_call()
+        t_e2e = time.perf_counter() - t_start
+        t_e2e = max_over_ranks(t_e2e, ws)
+        e2e = {"value": ws * ke / t_e2e, "unit": UNIT, "h2d_bytes_per_step": m * n * esz + m * 8,
+               "d2h_bytes_per_step": n * 8, "steps": ke}
+        del Ah
 
     # roofline of the dominant kernel
     ms_solve = sum(s[0] for s in solve_ms) / len(solve_ms)
     ms_sketch = sum(s[2] for s in solve_ms) / len(solve_ms)
     ms_factor = sum(s[3] for s in solve_ms) / len(solve_ms)
+    ms_kernel = sum(s[4] for s in solve_ms) / len(solve_ms)
     iters = solve_ms[-1][1]
-    peaks = {}
-    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk):
-        with open(pk) as f:
-            peaks = json.load(f)
+    peaks, peak_src = load_peaks()
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    ms_kernel = sum(s[4] for s in solve_ms) / len(solve_ms)
-    elem = m * n * 8
-    # one launch = iters + 1 streamed passes; each reads the float-float copy
-    # of A (8 bytes per element) and reads + writes u (2 x 8 bytes per row)
+    # one lsqr_ff_kernel launch = iters + 1 streamed passes; each reads the
+    # row-major float-float copy of A (8 bytes per element, rows padded to
+    # even length) and reads + writes u (2 x 8 bytes per row)
+    ldf = (n + 1) & ~1
     passes = iters + 1
-    lsqr_bytes = passes * (elem + 2 * 8 * m)
+    lsqr_bytes = passes * (8.0 * m * ldf + 16.0 * m)
     lsqr_gbs = lsqr_bytes / (ms_kernel / 1e3) / 1e9 if ms_kernel > 0 else None
-    # DRAM bytes (read + write) per row and pass of lsqr_ff_kernel from one ncu
-    # capture (40000 x 500, 36 passes: 5.8198 GB read + 0.0375 GB written),
-    # scaled by rows and passes
-    lsqr_traffic = LSQR_DRAM_BYTES_PER_ROW_PASS * m * passes if n == 500 else None
-    sketch_flops = 2.0 * int(CFG["sampling_factor"] * n) * m * (n + 1)   # S [A b]
+    # DRAM traffic scaled from the ncu capture by rows, passes and bytes per row
+    lsqr_traffic = (LSQR_DRAM_BYTES_PER_ROW_PASS / LSQR_NCU_ALGO_BYTES_PER_ROW_PASS
+                    * (8.0 * ldf + 16.0) * m * passes)
+    sketch_flops = 2.0 * d * m * (n + 1)   # S [A b], algorithmic
     sketch_tflops = sketch_flops / (ms_sketch / 1e3) / 1e12
-    stages = {"sketch_ms": ms_sketch, "qr_rinv_ms": ms_factor, "lsqr_ms": ms_solve,
-              "lsqr_iterations": iters}
-    if (ms_solve >= ms_sketch or not tc) and lsqr_gbs is not None:
-        roof = {"bound": "hbm",
-                "kernel": "lsqr_ff_kernel (one streamed A y / A^T u pass over the float-float copy of A "
-                          "per LSQR iteration)",
-                "achieved": lsqr_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": lsqr_gbs / hbm_peak,
-                "traffic": lsqr_traffic, "peak_source": peak_src, "kernel_ms_per_launch": ms_kernel,
-                "algorithmic_bytes_per_launch": lsqr_bytes}
-    else:
-        roof = {"bound": "tensor", "kernel": "sketch_tc (digit-sliced bf16 S [A b])",
-                "achieved": sketch_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": sketch_tflops / bf16_peak, "traffic": None, "peak_source": peak_src,
-                "algorithmic_flops_per_launch": sketch_flops}
+    stages = {"sketch_ms": ms_sketch, "qr_rinv_ms": ms_factor, "lsqr_ms": ms_solve, "lsqr_kernel_ms": ms_kernel,
+              "lsqr_iterations": iters, "sketch_algorithmic_tflops": sketch_tflops}
+    roof = {"bound": "hbm",
+            "kernel": "lsqr_ff_kernel (one streamed A y / A^T u pass over the row-major float-float copy of "
+                      "A per LSQR iteration)",
+            "achieved": lsqr_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": lsqr_gbs / hbm_peak if lsqr_gbs else None,
+            "traffic": lsqr_traffic, "peak_source": peak_src, "kernel_ms_per_launch": ms_kernel,
+            "algorithmic_bytes_per_launch": lsqr_bytes}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16 digit-sliced sketch + float-float (fp32 pairs) QR/LSQR" if tc else "f64",
+        "dtype": "bf16 digit-sliced sketch + float-float (fp32 pairs) QR/LSQR",
         "data": "synthetic (seeded torch CUDA generator)",
-        "config": {"workload": workload_name(m, n),
-                   "m": m, "n": n, "d": int(CFG["sampling_factor"] * n), "kappa": CFG["kappa"],
-                   "precision": "BF16X" if tc else "FP64", "inner_solver": "LSQR",
-                   "l2": "inputs larger than L2 (A is %d MB)" % (elem >> 20),
-                   "parallelism": "replicas" if ws > 1 else "single"},
-        "accuracy": {"rel_residual": rr, "rel_residual_fp64_path": rr64, "rel_residual_lapack": rrl,
-                     "abs_diff_vs_fp64": abs(rr - rr64), "abs_diff_vs_lapack": abs(rr - rrl)},
+        "config": workload_config(args, wl, ws),
+        "path": "BF16X (tcgen05 digit-sliced sketch, float-float QR or FP64 QR, float-float LSQR)",
+        "accuracy": acc,
         "stages": stages,
         "fp64_path": fp64,
-        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": elem + m * 8,
-                "d2h_bytes_per_step": n * 8},
+        "speedup_vs_fp64_path": (value / ws) / fp64["value"] if fp64 else None,
+        "e2e": e2e,
         "gpu_launches": int(launches),
         "roofline": roof,
         "clocks": clk,
     }
+    if rank == 0 and not args.no_cpu:
+        line["accuracy_lapack"] = None
+        try:
+            xl, tl = lapack_solve(A, b)
+            xl = torch.from_numpy(xl).to(dev)
+            al = accuracy(A, xl, b)
+            line["accuracy_lapack"] = {"rel_residual": al["rel_residual"], "backward_error": al["backward_error"],
+                                       "abs_diff_rel_residual": abs(acc["rel_residual"] - al["rel_residual"]),
+                                       "x_rel_diff": float((x - xl).norm() / xl.norm()), "seconds": tl}
+        except MemoryError:
+            pass
+    del A
     return line
 
 
@@ -420,7 +500,7 @@ def run_batched(args, rank, local, ws):
     indexed = batched_shapes(args.problems, rank=rank, world=ws)
     probs = make_batched(indexed, dev)
     shapes = [mn for _, mn in indexed]
-    tol, sf = 1e-12, CFG["sampling_factor"]
+    tol, sf = 1e-12, 4.0
     o = R.options(precision=R.Precision.BF16X, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol)
     o64 = R.options(precision=R.Precision.FP64, inner_solver=R.InnerSolver.LSQR, atol=tol, btol=tol)
     l = 2000
@@ -509,88 +589,115 @@ def run_batched(args, rank, local, ws):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle's restatement of the reference algorithm
+# CPU legs: the oracle's restatement of the reference path at full size
 # ---------------------------------------------------------------------------
-def cpu_sample(m_full, n, iters, sample_rows):
-    """Reference blendenpik (sketch_and_precondition.rs:26-59: dense Gaussian
-    S, S a, QR, R^-1, explicit a R^-1, CGLS) on a row-subsampled problem with
-    the same n, kappa and d; CGLS runs `iters` iterations.  Returns
-    (seconds for the sample, full-size solves/s by linear scaling in m)."""
+def make_problem_host(wl):
+    """The workload's construction on the host with numpy (seeded): A =
+    U diag(sigma) V^T (FP32-rounded for the FP32 workload, then widened: the
+    reference takes FP64 matrices), b = A x* + noise."""
+    import numpy as np
+    m, n = wl["m"], wl["n"]
+    su, sv, sx, sb = wl["seeds"]
+    U = np.linalg.qr(np.random.default_rng(su).standard_normal((m, n)))[0]
+    V = np.linalg.qr(np.random.default_rng(sv).standard_normal((n, n)))[0]
+    A = (U * np.logspace(0, -math.log10(wl["kappa"]), n)) @ V.T
+    del U
+    if wl["f32"]:
+        A = A.astype(np.float32).astype(np.float64)
+    A = np.asfortranarray(A)
+    b = A @ np.random.default_rng(sx).standard_normal(n) + wl["noise"] * np.random.default_rng(sb).standard_normal(m)
+    return A, b
+
+
+def cpu_child(args):
+    """`bench.py --cpu-leg port`: runs in its own process; prints one JSON
+    line per full-size solve of the oracle port (sketch_and_precondition.rs:
+    26-59: Gaussian S, S a, Householder QR, R^-1, explicit a R^-1, CGLS to the
+    workload's tolerance, x = R^-1 z), stopping after --steps solves or once
+    four minutes have passed."""
     import numpy as np
     from oracle import oracle as O
-    ms = sample_rows
-    d = int(CFG["sampling_factor"] * n)
-    rng = np.random.default_rng(0)
-    U = np.linalg.qr(rng.standard_normal((ms, n)))[0]
-    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
-    A = (U * np.logspace(0, -8, n)) @ V.T
-    b = A @ rng.standard_normal(n) + 1e-6 * rng.standard_normal(ms)
-    S = O.sketch(O.DIST_GAUSSIAN, d, ms)
-    t0 = time.perf_counter()
-    O.blendenpik_overdetermined(A, b, 1e-300, iters, CFG["sampling_factor"], S=S)
-    t = time.perf_counter() - t0
-    # the sketch generation is part of the reference call (sketch.rs:102-130); time it too
-    t1 = time.perf_counter()
-    O.sketch(O.DIST_GAUSSIAN, d, min(ms, 20000))
-    tg = (time.perf_counter() - t1) * ms / min(ms, 20000)
-    total = t + tg
-    return total, 1.0 / (total * m_full / ms)
+    wl = workload(args)
+    m, n = wl["m"], wl["n"]
+    A, b = make_problem_host(wl)
+    ms = max(4 * int(wl["sampling_factor"] * n), m // 64)
+    O.blendenpik_overdetermined_blocked(A[:ms], b[:ms], wl["tol"], 10, wl["sampling_factor"])   # load libraries
+    t_all = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        x, it = O.blendenpik_overdetermined_blocked(A, b, wl["tol"], 10 * n, wl["sampling_factor"],
+                                                    return_iters=True)
+        t = time.perf_counter() - t0
+        rr = float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+        print(json.dumps({"seconds": t, "cgls_iterations": it, "rel_residual": rr}), flush=True)
+        if time.perf_counter() - t_all > 240.0:
+            break
 
 
-def lapack_sample(m_full, n, sample_rows):
-    """numpy/LAPACK FP64 least squares (gelsd through numpy.linalg.lstsq, all
-    host threads) on the same kind of row sample as cpu_sample.  Returns
-    (seconds for the sample, full-size solves/s by linear scaling in m: the
-    cost is O(m n^2))."""
-    import numpy as np
-    rng = np.random.default_rng(1)
-    U = np.linalg.qr(rng.standard_normal((sample_rows, n)))[0]
-    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
-    A = np.asfortranarray((U * np.logspace(0, -8, n)) @ V.T)
-    b = A @ rng.standard_normal(n) + 1e-6 * rng.standard_normal(sample_rows)
-    np.linalg.lstsq(A[:1000], b[:1000], rcond=None)          # load LAPACK once
-    t0 = time.perf_counter()
-    np.linalg.lstsq(A, b, rcond=None)
-    t = time.perf_counter() - t0
-    return t, 1.0 / (t * m_full / sample_rows)
+def cpu_port_runs(args, steps):
+    """Full-size oracle-port solves in a child process (capped): returns
+    (list of per-solve results, note)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-leg", "port", "--workload", args.workload,
+           "--steps", str(steps)]
+    if args.m:
+        cmd += ["--m", str(args.m)]
+    if args.n:
+        cmd += ["--n", str(args.n)]
+    env = dict(os.environ)
+    env.pop("RANK", None)
+    env.pop("WORLD_SIZE", None)
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env)
+    note = "finished"
+    try:
+        out, err = proc.communicate(timeout=CPU_CAP_S + 300.0)   # + problem generation
+    except subprocess.TimeoutExpired:
+        proc.kill()
+        out, err = proc.communicate()
+        note = "not finished (cap %d s)" % CPU_CAP_S
+    runs = [json.loads(ln) for ln in out.splitlines() if ln.startswith("{")]
+    if proc.returncode not in (0, None) and note == "finished":
+        note = "failed: " + (err.strip().splitlines() or ["?"])[-1][:200]
+    return runs, note
 
 
 def run_reference(args, rank, ws):
     """The reference arm: the oracle's CPU restatement of the reference's
-    path on the host cores, rank 0 only."""
+    path at the workload's full size on the host cores, rank 0 only.  A
+    step is one full solve; the steps stop after four minutes (at least one
+    solve), and the line says how many ran."""
     if rank != 0:
         return None
-    import numpy as np
-    iters = 40
-    rows = max(2 * int(CFG["sampling_factor"] * args.n), 10000)
-    samples = []
-    for _ in range(args.warmup):
-        cpu_sample(args.m, args.n, iters, rows)
-    for _ in range(args.steps):
-        samples.append(cpu_sample(args.m, args.n, iters, rows)[1])
-    v = float(np.median(samples))
+    wl = workload(args)
+    runs, note = cpu_port_runs(args, args.steps)
     cores = os.cpu_count()
-    return {
-        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+    line = {
+        "metric": METRIC, "value": None, "unit": UNIT, "n_gpus": ws, "steps": len(runs),
+        "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy generator)",
-        "impl": "reference",
-        "config": {"workload": workload_name(args.m, args.n), "m": args.m, "n": args.n,
-                   "d": int(CFG["sampling_factor"] * args.n), "kappa": CFG["kappa"],
-                   "algorithm": "the reference's data flow: dense Gaussian S, S a, Householder QR, "
-                                "explicit a R^-1, CGLS (%d iterations, the count LSQR needs at "
-                                "tol 1e-12 on this problem, within a few)" % iters},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "oracle restatement of sketch_and_precondition.rs:26-59 "
-                                   "(numpy/LAPACK on all host threads, C sketch generator) on "
-                                   "%d x %d rows with %d CGLS iterations, scaled linearly in m "
-                                   "to %d rows" % (rows, args.n, iters, args.m)},
-        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "config": workload_config(args, wl, ws),
+        "algorithm": "the reference's data flow (sketch_and_precondition.rs:26-59): dense Gaussian S "
+                     "(generated in column blocks), S a, Householder QR, explicit R^-1 and a R^-1, CGLS to "
+                     "tolerance %g, x = R^-1 z" % wl["tol"],
+        "status": note, "runs": runs,
     }
+    if runs:
+        sec = sum(r["seconds"] for r in runs) / len(runs)
+        v = 1.0 / sec
+        line.update({"value": v, "ms_per_step": 1e3 * sec})
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "%d full-size solve(s) of the oracle restatement (numpy/LAPACK on "
+                                          "all %d host threads, C sketch generator on %d threads); no "
+                                          "sampling or extrapolation" % (len(runs), cores, cores)}
+        line["e2e"] = {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    return line
 
 
 def main():
     args = parse()
+    if args.cpu_leg:
+        cpu_child(args)
+        return
     rank, local, ws = dist_init()
     if args.impl == "reference":
         line = run_reference(args, rank, ws)
@@ -604,20 +711,22 @@ def main():
         return
     line = run_ours(args, rank, local, ws)
     if rank == 0 and not args.no_cpu:
-        iters = line["stages"]["lsqr_iterations"]
-        rows = max(2 * int(CFG["sampling_factor"] * args.n), 10000)
-        t, v = cpu_sample(args.m, args.n, max(iters, 1), rows)
-        line["cpu_baseline"] = {
-            "value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": "oracle restatement of sketch_and_precondition.rs:26-59 (numpy/LAPACK on all "
-                      "host threads, C sketch generator) on %d x %d rows, %d CGLS iterations "
-                      "(the GPU's iteration count), %.2f s, scaled linearly in m to %d rows"
-                      % (rows, args.n, iters, t, args.m)}
-        tl, vl = lapack_sample(args.m, args.n, rows)
-        line["cpu_baseline"]["lapack_lstsq"] = {
-            "value": vl, "unit": UNIT, "cores": os.cpu_count(),
-            "sample": "numpy.linalg.lstsq (LAPACK gelsd, FP64, all host threads) on %d x %d rows, "
-                      "%.2f s, scaled linearly in m to %d rows" % (rows, args.n, tl, args.m)}
+        cores = os.cpu_count()
+        runs, note = cpu_port_runs(args, 1)
+        cb = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "status": note}
+        if runs:
+            cb["value"] = 1.0 / runs[0]["seconds"]
+            cb["sample"] = ("one full-size solve (%.1f s, %d CGLS iterations) of the oracle restatement of "
+                            "sketch_and_precondition.rs:26-59 (numpy/LAPACK on all %d host threads, C sketch "
+                            "generator); no sampling or extrapolation"
+                            % (runs[0]["seconds"], runs[0]["cgls_iterations"], cores))
+        al = line.get("accuracy_lapack")
+        if al:
+            cb["lapack_qr_lstsq"] = {"value": 1.0 / al["seconds"], "unit": UNIT, "cores": cores,
+                                     "sample": "numpy.linalg.qr + triangular solve (LAPACK geqrf/orgqr, FP64, "
+                                               "all host threads) on the same A, full size, %.1f s"
+                                               % al["seconds"]}
+        line["cpu_baseline"] = cb
     if rank == 0:
         print(json.dumps(line))
 

@@ -208,10 +208,13 @@ RNLA_API int rnla_lsqr_dev(const double* a_dev, int64_t m, int64_t n, int64_t ld
  * All scratch lives in a fixed 32 MiB device array inside the library (held
  * by every GPU that loads it until the process exits); a problem needs
  * 8 * (10 + 4G + m + 5n + G n) bytes, G <= 4 x (number of SMs), and larger
- * problems return RNLA_ERR_INVALID_DIMENSIONS.  Calls share that array, so
- * calls on one device are serialised (a per-device lock held until the call
- * has synchronised); the first call on a device looks up the array's address
- * and should come before any stream capture.  Synchronises. */
+ * problems return RNLA_ERR_INVALID_DIMENSIONS; n > 4096 returns
+ * RNLA_ERR_UNSUPPORTED.  Calls share that array, so calls on one device are
+ * serialised (a per-device lock held until the call has synchronised); the
+ * first call on a device looks up the array's address and should come
+ * before any stream capture.  Every call clears its words with
+ * cudaMemsetAsync and synchronises the given stream on its result before it
+ * returns. */
 RNLA_API int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda,
                                    const double* b_dev, double damp, double atol, double btol,
                                    double conlim, int64_t iter_lim, const double* x0_dev,
@@ -317,6 +320,14 @@ RNLA_API int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64
                                       const double* b, double epsilon, int64_t l,
                                       double sampling_factor, const rnla_options* opt, double* x,
                                       rnla_stats* stats);
+/* The same with A stored in FP32 on the host (b and x stay FP64): the
+ * reference takes &DMatrix<f64> only; FP32 storage halves the bytes of A
+ * moved and streamed for large problems.  A goes up in 64-column chunks and
+ * the sketch starts on each chunk as it lands. */
+RNLA_API int rnla_blendenpik_overdetermined_f32_ex(const float* a, int64_t m, int64_t n, int64_t lda,
+                                          const double* b, double epsilon, int64_t l,
+                                          double sampling_factor, const rnla_options* opt, double* x,
+                                          rnla_stats* stats);
 /* Device-pointer form; a_dev is double or float (a_is_f32). Synchronises. */
 RNLA_API int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m, int64_t n,
                                        int64_t lda, const double* b_dev, double epsilon,

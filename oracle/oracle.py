@@ -60,6 +60,9 @@ def lib():
         L.oracle_sketch_fill.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
                                          ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
                                          ctypes.c_void_p, ctypes.c_int64]
+        L.oracle_sketch_fill_cols.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint64,
+                                              ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                              ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64]
         L.oracle_qgauss_t.argtypes = [ctypes.c_uint32]
         L.oracle_qgauss_t.restype = ctypes.c_int
         L.oracle_sketch_fill_quantized.argtypes = [ctypes.c_int, ctypes.c_uint64,
@@ -132,6 +135,27 @@ def sketch(dist, rows, cols, gen=GEN_PHILOX4X32, key0=0, key1=0, quantized=False
         lib().oracle_sketch_fill_quantized_dist(dist, gen, key0, key1, rows, cols, out.ctypes.data, rows)
     else:
         lib().oracle_sketch_fill(dist, gen, key0, key1, rows, cols, out.ctypes.data, rows)
+    return out.astype(np.float64)
+
+
+def sketch_cols(dist, rows, j0, j1, gen=GEN_PHILOX4X32, key0=0, key1=0, threads=None):
+    """Columns [j0, j1) of sketch(dist, rows, cols) (float64, column-major),
+    generated by `threads` host threads in column blocks (the C fill releases
+    the GIL).  Entry values are those of sketch()."""
+    import concurrent.futures as cf
+    cols = j1 - j0
+    out = np.empty((rows, cols), dtype=np.float32, order="F")
+    threads = threads or os.cpu_count() or 1
+    step = max(1, -(-cols // threads))
+    L = lib()
+
+    def fill(c0):
+        c1 = min(cols, c0 + step)
+        L.oracle_sketch_fill_cols(dist, gen, key0, key1, rows, j0 + c0, j0 + c1,
+                                  out.ctypes.data + 4 * rows * c0, rows)
+
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(fill, range(0, cols, step)))
     return out.astype(np.float64)
 
 
@@ -515,6 +539,38 @@ def blendenpik_overdetermined(a, b, epsilon, l, sampling_factor, S=None, return_
         S = sketch(DIST_GAUSSIAN, d, m)
     a_sk = S @ a
     b_sk = S @ b
+    q, r = np.linalg.qr(a_sk, mode="reduced")
+    z0 = q.T @ b_sk
+    rinv = _upper_inverse(r)
+    a_pre = a @ rinv
+    z, iters = cgls(a_pre, b, epsilon, l, z0, return_iters=True)
+    x = rinv @ z
+    return (x, iters) if return_iters else x
+
+
+def blendenpik_overdetermined_blocked(a, b, epsilon, l, sampling_factor, block=65536, threads=None,
+                                      return_iters=False):
+    """blendenpik_overdetermined with the same S formed in column blocks:
+    S a and S b accumulate block by block (block columns of S generated by
+    `threads` host threads), so the d x m operator is never held whole.  The
+    rest of the data flow (QR, z0 = Q^T S b, explicit R^-1 and a R^-1, CGLS,
+    x = R^-1 z) is that of sketch_and_precondition.rs:26-59."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64).reshape(-1)
+    m, n = a.shape
+    if m < n:
+        raise NotOverdetermined("NotOverdetermined")
+    if sampling_factor < 1.0 or not epsilon > 0.0 or l == 0:
+        raise InvalidParameters("invalid blendenpik parameters")
+    d = sketch_rows(m, n, sampling_factor)
+    a_sk = np.zeros((d, n))
+    b_sk = np.zeros(d)
+    for k0 in range(0, m, block):
+        k1 = min(m, k0 + block)
+        S = sketch_cols(DIST_GAUSSIAN, d, k0, k1, threads=threads)
+        a_sk += S @ a[k0:k1]
+        b_sk += S @ b[k0:k1]
+        del S
     q, r = np.linalg.qr(a_sk, mode="reduced")
     z0 = q.T @ b_sk
     rinv = _upper_inverse(r)

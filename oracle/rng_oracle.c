@@ -305,6 +305,16 @@ void oracle_sketch_fill(int dist, int gen, uint64_t key0, uint64_t key1,
             out[i + j * ld] = oracle_sketch_entry(dist, gen, key0, key1, rows, i, j);
 }
 
+/* Columns [j0, j1) of the same dense operator into out (column j - j0), so
+   callers can generate a large sketch in column blocks (and in parallel,
+   one block per thread) without holding all of it. */
+void oracle_sketch_fill_cols(int dist, int gen, uint64_t key0, uint64_t key1,
+                             int64_t rows, int64_t j0, int64_t j1, float *out, int64_t ld) {
+    for (int64_t j = j0; j < j1; ++j)
+        for (int64_t i = 0; i < rows; ++i)
+            out[i + (j - j0) * ld] = oracle_sketch_entry(dist, gen, key0, key1, rows, i, j);
+}
+
 /* Quantised Gaussian used by the tensor-core sketch: t = round(8 g) clamped
    to [-63, 63], g ~ N(0, 1), drawn from one 32-bit word with the Walker
    alias table of rnla_qgauss_table.h (generated by make_qgauss_table.py:

@@ -98,6 +98,9 @@ SIGNATURES = [
     ("rnla_blendenpik_overdetermined_ex", ctypes.c_int,
      [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
       ctypes.POINTER(Stats)]),
+    ("rnla_blendenpik_overdetermined_f32_ex", ctypes.c_int,
+     [c_vp, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
+      ctypes.POINTER(Stats)]),
     ("rnla_blendenpik_overdetermined_dev", ctypes.c_int,
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
       ctypes.POINTER(Stats), c_vp]),

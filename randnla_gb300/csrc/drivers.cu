@@ -507,8 +507,8 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     // BF16X + LSQR: the float-float copies of A and b for the solver are built
     // on the side stream while the QR runs
     LsqrFFInput lsqr_in;
-    if (o.precision != RNLA_PREC_FP64 && o.inner_solver != RNLA_SOLVER_CGLS && !a_f32 && lsqr_ff_supported(n))
-        lsqr_ff_prepare(ctx, static_cast<const double*>(Av), m, n, lda, b, lsqr_in);
+    if (o.precision != RNLA_PREC_FP64 && o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n))
+        lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
     DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
     bool inv_ok;
@@ -969,21 +969,23 @@ int rnla_blendenpik_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int6
 
 // Host-pointer blendenpik / lsrn: A goes up in column tiles on the copy
 // stream and the solve starts on the first tile while the rest is in flight.
-static int blendenpik_host(const double* a, int64_t m, int64_t n, int64_t lda, const double* b, double epsilon,
-                           int64_t l, double sampling_factor, const rnla_options* opt, double* x,
+static int blendenpik_host(const void* a, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
+                           double epsilon, int64_t l, double sampling_factor, const rnla_options* opt, double* x,
                            rnla_stats* stats, bool lsrn) {
     RNLA_API_BEGIN
     check_mat(m, n, lda);
     blendenpik_validate(m, n, epsilon, l, sampling_factor);
     cudaStream_t s = host_stream();
-    DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
+    const size_t es = a_f32 ? sizeof(float) : sizeof(double);
+    DevBuf<unsigned char> A((size_t)m * n * es, s);
+    DevBuf<double> B(m, s), X(n, s);
     RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
     ColumnFeed feed;
-    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
+    h2d_columns_async(A.get(), a, es, m, n, lda, TC_TILE_COLS, s, feed);
     Ctx ctx(s);
     const rnla_options o = opts_or_default(opt);
     if (stats) memset(stats, 0, sizeof *stats);
-    blendenpik_impl(ctx, A.get(), false, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed, lsrn);
+    blendenpik_impl(ctx, A.get(), a_f32, m, n, m, B, epsilon, l, sampling_factor, o, X, stats, &feed, lsrn);
     RNLA_CUDA(cudaMemcpyAsync(x, X.get(), n * sizeof(double), cudaMemcpyDeviceToHost, s));
     RNLA_CUDA(cudaStreamSynchronize(s));
     RNLA_API_END
@@ -993,7 +995,14 @@ int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64_t n, int
                                       const double* b, double epsilon, int64_t l,
                                       double sampling_factor, const rnla_options* opt, double* x,
                                       rnla_stats* stats) {
-    return blendenpik_host(a, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, false);
+    return blendenpik_host(a, false, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, false);
+}
+
+int rnla_blendenpik_overdetermined_f32_ex(const float* a, int64_t m, int64_t n, int64_t lda,
+                                          const double* b, double epsilon, int64_t l,
+                                          double sampling_factor, const rnla_options* opt, double* x,
+                                          rnla_stats* stats) {
+    return blendenpik_host(a, true, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, false);
 }
 
 int rnla_blendenpik_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
@@ -1072,7 +1081,7 @@ int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsil
 int rnla_lsrn_overdetermined_ex(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
                                 double epsilon, int64_t l, double sampling_factor, const rnla_options* opt,
                                 double* x, rnla_stats* stats) {
-    return blendenpik_host(a, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, true);
+    return blendenpik_host(a, false, m, n, lda, b, epsilon, l, sampling_factor, opt, x, stats, true);
 }
 
 int rnla_lsrn_overdetermined(const double* a, int64_t m, int64_t n, int64_t lda, const double* b,
@@ -1136,7 +1145,7 @@ static int sketched_ls_host(const double* a, int64_t m, int64_t n, int64_t lda, 
     DevBuf<double> A((size_t)m * n, s), B(m, s), X(n, s);
     RNLA_CUDA(cudaMemcpyAsync(B.get(), b, m * sizeof(double), cudaMemcpyHostToDevice, s));
     ColumnFeed feed;
-    h2d_columns_async(A, a, m, n, lda, TC_TILE_COLS, s, feed);
+    h2d_columns_async(A.get(), a, sizeof(double), m, n, lda, TC_TILE_COLS, s, feed);
     Ctx ctx(s);
     const rnla_options o = opts_or_default(opt);
     sketch_solve_impl(ctx, A.get(), false, m, n, m, B, use_svd, o, X, &feed);

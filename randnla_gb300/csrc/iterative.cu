@@ -595,7 +595,7 @@ __device__ void row_pass_ff2(const IterArgs& a, double* __restrict__ smem_d, dou
 template <typename TA, int NACC, int MODE>
 __device__ __forceinline__ void do_pass(const IterArgs& a, double* smem, double c1, double c2, double c3,
                                         double* vec, bool want_b2, bool acc_at) {
-    if constexpr (MODE == 0) do_pass<TA, NACC, MODE>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
+    if constexpr (MODE == 0) row_pass<TA, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
     else if constexpr (MODE == 1) row_pass_stream<TA, false, NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
     else if constexpr (std::is_same<TA, double>::value)
         row_pass_ff2<NACC>(a, smem, c1, c2, c3, vec, want_b2, acc_at);
@@ -1007,8 +1007,10 @@ LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, 
                       const LsqrFFInput* pre, LsqrPending* pend) {
     if (n > (int64_t)IT_THREADS * IT_MAXACC)
         fail(RNLA_ERR_UNSUPPORTED, "lsqr: n > 4096 is not supported by the fused kernel");
-    if (ffp && a64 && lsqr_ff_supported(n))
-        return lsqr_ff_solve(ctx, a64, m, n, lda, M, b, x0, prm, x, var, arnorms_dev, pre, pend);
+    if (ffp && lsqr_ff_supported(n)) {
+        const void* A = a64 ? (const void*)a64 : (const void*)a32;
+        return lsqr_ff_solve(ctx, A, a64 == nullptr, m, n, lda, M, b, x0, prm, x, var, arnorms_dev, pre, pend);
+    }
     IterArgs a;
     IterBufs B;
     int G;
@@ -1056,6 +1058,10 @@ int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int
 // preconditioner).  Sets *grid to the cooperative grid it will use.
 size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_t* smem_out,
                             const void** kernel_out) {
+    // the kernels hold each thread's share of the n-vectors in registers:
+    // columns beyond IT_THREADS * IT_MAXACC would never be written
+    if (n > (int64_t)IT_THREADS * IT_MAXACC)
+        fail(RNLA_ERR_UNSUPPORTED, "lsqr: n > 4096 is not supported by the fused kernel");
     const int mode = (n <= STREAM_MAX_N) ? 1 : 0;
     const void* k = select_kernel<true>(false, mode, n);
     int64_t red_off = 0;

@@ -1081,15 +1081,20 @@ __global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
 
 // Row-major float-float copy in column-pair order: row i is hp = ldf / 2
 // chunks of 16 bytes, chunk p = (hi_2p, hi_2p+1, lo_2p, lo_2p+1); zero for
-// columns in [n, ldf).  32 x 32 tiles through shared memory.
-__global__ void rowmajor_split_kernel(const double* __restrict__ A, int64_t m, int64_t n, int64_t lda,
+// columns in [n, ldf).  FP32 data has lo = 0.  32 x 32 tiles through shared
+// memory.
+__device__ __forceinline__ float2 ff_of(double v) { return ff_split(v); }
+__device__ __forceinline__ float2 ff_of(float v) { return make_float2(v, 0.f); }
+
+template <typename TA>
+__global__ void rowmajor_split_kernel(const TA* __restrict__ A, int64_t m, int64_t n, int64_t lda,
                                       float* __restrict__ AF, int64_t ldf) {
     __shared__ float2 tile[32][33];
     const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
     for (int k = threadIdx.y; k < 32; k += 8) {
         const int64_t i = i0 + threadIdx.x, j = j0 + k;
         float2 v = make_float2(0.f, 0.f);
-        if (i < m && j < n) v = ff_split(A[i + j * lda]);
+        if (i < m && j < n) v = ff_of(A[i + j * lda]);
         tile[k][threadIdx.x] = v;
     }
     __syncthreads();
@@ -1148,11 +1153,16 @@ bool lsqr_ff_supported(int64_t n) { return n >= 1 && n <= lsff::MAX_N; }
 
 // Float-float copies of A (row-major, column-pair order) and b, enqueued on
 // `st`.
-static void build_ff_input(Ctx& ctx, cudaStream_t st, const double* A, int64_t m, int64_t n, int64_t lda,
-                           const double* b, int64_t ldf, float2* AF, float2* bF) {
+static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32, int64_t m, int64_t n,
+                           int64_t lda, const double* b, int64_t ldf, float2* AF, float2* bF) {
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
-    rowmajor_split_kernel<<<grid, dim3(32, 8), 0, st>>>(A, m, n, lda, reinterpret_cast<float*>(AF), ldf);
+    if (a_f32)
+        rowmajor_split_kernel<float><<<grid, dim3(32, 8), 0, st>>>(static_cast<const float*>(A), m, n, lda,
+                                                                   reinterpret_cast<float*>(AF), ldf);
+    else
+        rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,
+                                                                    reinterpret_cast<float*>(AF), ldf);
     RNLA_LAUNCH_CHECK();
     int g = (int)div_up(m, 256);
     if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
@@ -1160,7 +1170,7 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const double* A, int64_t m
     RNLA_LAUNCH_CHECK();
 }
 
-void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* b,
+void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
                      LsqrFFInput& in) {
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
     in.A = A; in.m = m; in.n = n;
@@ -1169,13 +1179,13 @@ void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t ld
     in.bF.alloc(m, ctx.stream);
     const cudaStream_t side = side_stream(ctx.device);
     stream_wait(side, ctx.stream);                 // buffers allocated, A and b written
-    build_ff_input(ctx, side, A, m, n, lda, b, in.ldf, in.AF, in.bF);
+    build_ff_input(ctx, side, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
     RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     in.owner = ctx.stream;
     RNLA_CUDA(cudaEventRecord(in.ready, side));
 }
 
-LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
+LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
                          double* arnorms_dev, const LsqrFFInput* pre, LsqrPending* pend) {
     using namespace lsff;
@@ -1213,7 +1223,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_
     } else {
         AFo.alloc((size_t)m * ldf, st);
         bFo.alloc(m, st);
-        build_ff_input(ctx, st, A, m, n, lda, b, ldf, AFo, bFo);
+        build_ff_input(ctx, st, A, a_f32, m, n, lda, b, ldf, AFo, bFo);
         AF = AFo.get();
         bF = bFo.get();
     }

@@ -23,9 +23,14 @@
 //     from before its first launch until it has synchronised on its result,
 //     so calls from several host threads or streams never overlap on the
 //     array;
+//   * n is at most 4096 (as for rnla_lsqr_dev); a larger n returns
+//     RNLA_ERR_UNSUPPORTED;
 //   * the first call on a device looks the array's device address up
 //     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture.
+//     that first call before any stream capture;
+//   * every call clears its words with cudaMemsetAsync, queries the kernel's
+//     occupancy and synchronises the stream it is given on its result
+//     before it returns.
 #include "rnla_abi.h"
 #include <mutex>
 
@@ -81,6 +86,16 @@ extern "C" int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, 
     if (dev < 0 || dev >= kMaxDevices) fail(RNLA_ERR_CUDA, "device index out of range");
     // held until lsqr_run_in_workspace has synchronised on the result
     std::lock_guard<std::mutex> call(g_noalloc_call_mu[dev]);
+    // each of m and n alone must fit the array as doubles before the size
+    // arithmetic below (which cannot overflow then: n <= 4096 is checked next)
+    if ((uint64_t)m > RNLA_NOALLOC_SCRATCH_BYTES / 8 || (uint64_t)n > RNLA_NOALLOC_SCRATCH_BYTES / 8) {
+        char buf[200];
+        snprintf(buf, sizeof buf,
+                 "rnla_lsqr_noalloc_dev: an %lld x %lld problem needs more than the %u bytes of scratch "
+                 "the allocation-free entry point holds",
+                 (long long)m, (long long)n, (unsigned)RNLA_NOALLOC_SCRATCH_BYTES);
+        fail(RNLA_ERR_INVALID_DIMENSIONS, buf);
+    }
     int sms = 0;
     void* ws = noalloc_scratch(dev, &sms);
     const size_t need = lsqr_workspace_bytes(m, n, sms, nullptr, nullptr, nullptr);

@@ -119,13 +119,13 @@ LsqrResult lsqr_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, 
 int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int64_t n,
                    int64_t lda, const double* M, const double* b, const double* x0,
                    double tolerance, int64_t num_iterations, double* x, bool* converged);
-// Float-float LSQR (lsqr_ff.cu) on FP64 data, 1 <= n <= 1024; same contract
+// Float-float LSQR (lsqr_ff.cu) on FP64 or FP32 data, 1 <= n <= 1024; same contract
 // as lsqr_solve.  lsqr_ff_prepare builds the float-float copies of A and b
 // on the side stream (so they overlap earlier work on ctx.stream);
 // lsqr_ff_solve waits for them (or builds them itself when `pre` is null).
 struct LsqrFFInput {
     DevBuf<float2> AF, bF;
-    const double* A = nullptr;
+    const void* A = nullptr;
     int64_t m = 0, n = 0, ldf = 0;
     cudaEvent_t ready = nullptr;
     cudaStream_t owner = nullptr;   // stream the buffers are freed on
@@ -142,9 +142,9 @@ struct LsqrFFInput {
     }
 };
 bool lsqr_ff_supported(int64_t n);
-void lsqr_ff_prepare(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* b,
+void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
                      LsqrFFInput& in);
-LsqrResult lsqr_ff_solve(Ctx& ctx, const double* A, int64_t m, int64_t n, int64_t lda, const double* M,
+LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
                          double* arnorms_dev, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
 // Workspace-based LSQR used by the allocation-free entry point (noalloc.cu).
@@ -186,9 +186,10 @@ struct ColumnFeed {
         for (cudaEvent_t e : ready) RNLA_CUDA(cudaStreamWaitEvent(s, e, 0));
     }
 };
-// Copies the host matrix a (m x n, lda) to dev (ld m) in column chunks on
-// the device's copy stream, after the work already enqueued on `s`.
-void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64_t lda, int64_t chunk,
+// Copies the host matrix a (m x n, lda, elements of esize bytes) to dev (ld
+// m) in column chunks on the device's copy stream, after the work already
+// enqueued on `s`.
+void h2d_columns_async(void* dev, const void* a, size_t esize, int64_t m, int64_t n, int64_t lda, int64_t chunk,
                        cudaStream_t s, ColumnFeed& feed);
 
 bool tc_available(Ctx& ctx);

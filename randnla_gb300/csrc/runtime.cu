@@ -96,7 +96,7 @@ cudaStream_t copy_stream(int dev) {
     return device_stream(cache, mu, dev);
 }
 
-void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64_t lda, int64_t chunk,
+void h2d_columns_async(void* dev, const void* a, size_t esize, int64_t m, int64_t n, int64_t lda, int64_t chunk,
                        cudaStream_t s, ColumnFeed& feed) {
     int d = 0;
     RNLA_CUDA(cudaGetDevice(&d));
@@ -106,8 +106,9 @@ void h2d_columns_async(double* dev, const double* a, int64_t m, int64_t n, int64
     feed.owner = s;
     for (int64_t j0 = 0; j0 < n; j0 += chunk) {
         const int64_t c = std::min(chunk, n - j0);
-        RNLA_CUDA(cudaMemcpy2DAsync(dev + j0 * m, m * sizeof(double), a + j0 * lda, lda * sizeof(double),
-                                    m * sizeof(double), c, cudaMemcpyHostToDevice, cp));
+        RNLA_CUDA(cudaMemcpy2DAsync(static_cast<char*>(dev) + (size_t)j0 * m * esize, m * esize,
+                                    static_cast<const char*>(a) + (size_t)j0 * lda * esize, lda * esize,
+                                    m * esize, c, cudaMemcpyHostToDevice, cp));
         cudaEvent_t ev;
         RNLA_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
         feed.ready.push_back(ev);

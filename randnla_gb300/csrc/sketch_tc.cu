@@ -34,8 +34,9 @@
 //                      digit tiles of each stage with cp.async.bulk into a
 //                      4-stage mbarrier ring that runs on across units;
 //                      warp 1 allocates TMEM and issues tcgen05.mma
-//                      (M = 128, N = 64, K = 16, bf16 x bf16 -> f32, one
-//                      accumulator per digit, two accumulator sets so the
+//                      (M = 128, N = 64 P, K = 16, bf16 x bf16 -> f32: the
+//                      P digit tiles are one operand, so digit p accumulates
+//                      in TMEM columns [64 p, 64 p + 64); two sets so the
 //                      MMAs of a window overlap the drain of the previous
 //                      one) from one lane; warps 2-5 drain TMEM after each
 //                      window.  Units that share an S tile are adjacent in
@@ -288,7 +289,10 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
     } else if (warp == 1) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            constexpr uint32_t idesc = idesc_bf16(BM, BN);
+            // the P digit tiles of a stage are contiguous rows of one K-major
+            // operand, so one MMA of N = P * BN covers every digit: the S tile
+            // is read from shared memory once per K step, not P times
+            constexpr uint32_t idesc = idesc_bf16(BM, P * BN);
             int g = 0, slot = 0;          // stages consumed; ring slot
             uint32_t fph = 0;             // full-barrier parity of slot
             int win = 0;                  // windows started
@@ -309,14 +313,11 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                     if (!mbar_wait(&full[slot], fph, err)) { ok = false; break; }
                     tc_after();
                     const uint32_t a0 = smem_u32(sS + slot * S_BYTES);
+                    const uint32_t b0 = smem_u32(sY + slot * P * YD_BYTES);
 #pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        const uint32_t b0 = smem_u32(sY + (slot * P + p) * YD_BYTES);
-#pragma unroll
-                        for (int kk = 0; kk < BK / 16; ++kk)
-                            mma_bf16(acc + p * BN, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
-                                     (in_win > 0 || kk > 0) ? 1u : 0u);
-                    }
+                    for (int kk = 0; kk < BK / 16; ++kk)
+                        mma_bf16(acc, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
+                                 (in_win > 0 || kk > 0) ? 1u : 0u);
                     mma_commit(&empty[slot]);
                     if (++slot == STAGES) { slot = 0; fph ^= 1u; }
                     ++g;
@@ -664,7 +665,9 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
                      const ColumnFeed* feed, int dist) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
-    if (digits <= 0) digits = 4;
+    // default digits: 4 for FP64 data (32 bits below each column's maximum),
+    // 3 for FP32 data (its 24-bit significands)
+    if (digits <= 0) digits = x_f32 ? 3 : 4;
     switch (digits) {
         case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
         case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;

@@ -1,8 +1,8 @@
 """Extract the reference crate's own known-answer vectors into JSON fixtures.
 
-Run in a container where the reference checkout is mounted:
+Run with the path of a reference checkout as the only argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path-to-reference-checkout>
 
 It parses the test constants of the vendored generator crate and the literal
 matrices of the solver/driver tests, so nothing here is typed by hand:
@@ -136,4 +136,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path-to-reference-checkout>")
+    main(sys.argv[1])

@@ -100,3 +100,30 @@ def test_cgls_zero_rhs_propagates_nan(rnla):
     got = rnla.cgls(a, np.zeros(20), 1e-8, 5)
     ref = O.cgls(a, np.zeros(20), 1e-8, 5)
     assert np.isnan(got).all() and np.isnan(ref).all()
+
+
+@pytest.mark.parametrize("m,n,x0", [(3000, 1100, False), (2500, 2049, True)])
+def test_lsqr_wide_columns_staged_pass(rnla, m, n, x0):
+    """n > 1024 takes the staged (mode 0) pass of the FP64 solver kernels."""
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((m, n))
+    b = rng.standard_normal(m)
+    xx = rng.standard_normal(n) if x0 else None
+    got = rnla.lsqr(a, b, 0.0, 1e-12, 1e-12, 1e8, 4 * n, False, xx)
+    ref = O.lsqr(a, b, 0.0, 1e-12, 1e-12, 1e8, 4 * n, False, xx)
+    assert got[1] == ref[1] == 2
+    assert abs(got[2] - ref[2]) <= 1
+    xl = np.linalg.lstsq(a, b, rcond=None)[0]
+    np.testing.assert_allclose(got[0], xl, rtol=1e-9, atol=1e-10)
+    r = b - a @ got[0]
+    assert np.linalg.norm(a.T @ r) / (np.linalg.norm(a) * np.linalg.norm(r)) < 1e-12
+
+
+def test_cgls_wide_columns_staged_pass(rnla):
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((3000, 1100))
+    b = rng.standard_normal(3000)
+    got, it = rnla.cgls(a, b, 1e-9, 500, None, return_iterations=True)
+    ref, rit = O.cgls(a, b, 1e-9, 500, None, return_iters=True)
+    assert abs(it - rit) <= 1
+    np.testing.assert_allclose(got.ravel(), np.linalg.lstsq(a, b, rcond=None)[0], rtol=1e-7, atol=1e-9)

@@ -31,7 +31,10 @@ def _call(lib, fn, A, b, x, extra_dev):
     return res
 
 
-@pytest.mark.parametrize("m,n", [(3000, 40), (20000, 300)])
+# (3000, 40) and (20000, 300) take the streaming kernel (n <= 1024); (4001,
+# 1500) the staged kernel with an odd m, so the vectors carved after u start
+# on an 8-byte (not 16-byte) boundary; (6000, 4096) the largest n.
+@pytest.mark.parametrize("m,n", [(3000, 40), (20000, 300), (4001, 1500), (6000, 4096)])
 def test_noalloc_matches_regular_entry_point_twice(rnla, m, n):
     import torch
     lib = rnla.lib()
@@ -61,3 +64,30 @@ def test_noalloc_rejects_oversized_problem(rnla):
                                    ctypes.byref(res), None)
     assert rc == rnla.InvalidDimensions.code
     assert "needs" in lib.rnla_last_error_message().decode()
+
+
+def test_noalloc_rejects_n_above_4096(rnla):
+    import torch
+    lib = rnla.lib()
+    from randnla_gb300 import _lib
+    m, n = 5000, 4097
+    A = torch.zeros((1, 1), dtype=torch.float64, device="cuda")   # never read: rejected first
+    res = _lib.LsqrResult()
+    rc = lib.rnla_lsqr_noalloc_dev(ctypes.c_void_p(A.data_ptr()), m, n, m, ctypes.c_void_p(A.data_ptr()),
+                                   0.0, 1e-8, 1e-8, 1e8, 10, None, ctypes.c_void_p(A.data_ptr()),
+                                   ctypes.byref(res), None)
+    assert rc == rnla.Unsupported.code
+    assert "4096" in lib.rnla_last_error_message().decode()
+
+
+def test_noalloc_rejects_sizes_that_would_overflow(rnla):
+    import torch
+    lib = rnla.lib()
+    from randnla_gb300 import _lib
+    A = torch.zeros((1, 1), dtype=torch.float64, device="cuda")   # never read: rejected first
+    res = _lib.LsqrResult()
+    m = 1 << 61
+    rc = lib.rnla_lsqr_noalloc_dev(ctypes.c_void_p(A.data_ptr()), m, 2, m, ctypes.c_void_p(A.data_ptr()),
+                                   0.0, 1e-8, 1e-8, 1e8, 10, None, ctypes.c_void_p(A.data_ptr()),
+                                   ctypes.byref(res), None)
+    assert rc == rnla.InvalidDimensions.code
