@@ -56,11 +56,21 @@ WORKLOADS = {
     "plain_ls": dict(m=100000, n=500, kappa=1e8, noise=1e-6, sampling_factor=4.0, tol=1e-12,
                      f32=False, seeds=(1, 2, 3, 4)),
 }
+# rand_svd workloads: A = U diag(sigma) V^T (+ noise floor), Gaussian range
+# finder with k + p columns and q power iterations (RandNLA mode, Philox key 42)
+SVD_WORKLOADS = {
+    "precision_svd": dict(m=65536, n=16384, rank=1536, decay="exp(-i/64)", noise=1e-6, k=256, p=32, q=2,
+                          f32=True, seeds=(5, 6, 7)),
+    "plain_svd": dict(m=2000, n=1000, rank=1000, decay="10^(-i/100)", noise=0.0, k=50, p=10, q=2,
+                      f32=False, seeds=(1, 2, 0)),
+}
 # DRAM bytes (read + write) per row and pass of lsqr_ff_kernel from one ncu
 # capture (40000 x 500, float-float copy, 36 passes: 5.8198 GB read + 0.0375
 # GB written); per row and pass the kernel moves 8 ldf + 16 bytes.
 LSQR_DRAM_BYTES_PER_ROW_PASS = (5.819774e9 + 0.0375055e9) / (36 * 40000)
 LSQR_NCU_ALGO_BYTES_PER_ROW_PASS = 8 * 500 + 16
+# the same ratio for FP32 rows (None until an ncu capture of that layout is recorded)
+LSQR_F32_DRAM_RATIO = None
 
 
 def parse(argv=None):
@@ -69,7 +79,8 @@ def parse(argv=None):
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["precision_ls", "plain_ls", "batched"], default="precision_ls")
+    p.add_argument("--workload", choices=["precision_ls", "plain_ls", "precision_svd", "plain_svd", "batched"],
+                   default="precision_ls")
     p.add_argument("--m", type=int, default=None, help="rows (default: the workload's)")
     p.add_argument("--n", type=int, default=None, help="columns (default: the workload's)")
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison path")
@@ -82,6 +93,14 @@ def parse(argv=None):
 
 def workload(args):
     """The workload's parameters with the command line's --m / --n applied."""
+    if args.workload in SVD_WORKLOADS:
+        wl = dict(SVD_WORKLOADS[args.workload])
+        if args.m:
+            wl["m"] = args.m
+        if args.n:
+            wl["n"] = args.n
+        wl["rank"] = min(wl["rank"], wl["m"], wl["n"])
+        return wl
     wl = dict(WORKLOADS[args.workload])
     if args.m:
         wl["m"] = args.m
@@ -93,6 +112,16 @@ def workload(args):
 
 def workload_config(args, wl, ws):
     """The `config` object both arms print (identical, so the lines compare)."""
+    if args.workload in SVD_WORKLOADS:
+        return {"workload": "rand_svd %dx%d %s sigma_i=%s (rank %d) noise=%g k=%d p=%d q=%d"
+                            % (wl["m"], wl["n"], "fp32" if wl["f32"] else "fp64", wl["decay"], wl["rank"],
+                               wl["noise"], wl["k"], wl["p"], wl["q"]),
+                "name": args.workload, "m": wl["m"], "n": wl["n"], "k": wl["k"], "p": wl["p"], "q": wl["q"],
+                "a_storage": "fp32" if wl["f32"] else "fp64",
+                "l2": "A is %d MB%s" % ((wl["m"] * wl["n"] * (4 if wl["f32"] else 8)) >> 20,
+                                        " (larger than L2)" if wl["m"] * wl["n"] * 4 > 129e6 else
+                                        " (fits in L2: no flush between steps)"),
+                "parallelism": "replicas" if ws > 1 else "single"}
     return {"workload": "blendenpik_overdetermined %dx%d %s kappa=%g d=%d lsqr tol=%g"
                         % (wl["m"], wl["n"], "fp32" if wl["f32"] else "fp64", wl["kappa"], wl["d"], wl["tol"]),
             "name": args.workload, "m": wl["m"], "n": wl["n"], "d": wl["d"], "kappa": wl["kappa"],
@@ -398,22 +427,24 @@ def run_ours(args, rank, local, ws):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     # one lsqr_ff_kernel launch = iters + 1 streamed passes; each reads the
-    # row-major float-float copy of A (8 bytes per element, rows padded to
-    # even length) and reads + writes u (2 x 8 bytes per row)
-    ldf = (n + 1) & ~1
+    # row-major copy of A -- FP32 rows of n rounded up to 4 (4 bytes per
+    # element) for FP32-stored A, float-float rows of n rounded up to 2 (8
+    # bytes) for FP64 A -- and reads + writes u (2 x 8 bytes per row)
+    row_bytes = 4.0 * ((n + 3) & ~3) if wl["f32"] else 8.0 * ((n + 1) & ~1)
     passes = iters + 1
-    lsqr_bytes = passes * (8.0 * m * ldf + 16.0 * m)
+    lsqr_bytes = passes * (row_bytes * m + 16.0 * m)
     lsqr_gbs = lsqr_bytes / (ms_kernel / 1e3) / 1e9 if ms_kernel > 0 else None
-    # DRAM traffic scaled from the ncu capture by rows, passes and bytes per row
-    lsqr_traffic = (LSQR_DRAM_BYTES_PER_ROW_PASS / LSQR_NCU_ALGO_BYTES_PER_ROW_PASS
-                    * (8.0 * ldf + 16.0) * m * passes)
+    # DRAM traffic: the ncu ratio of DRAM bytes to algorithmic bytes of the
+    # matching row layout, scaled by rows and passes
+    ratio = LSQR_F32_DRAM_RATIO if wl["f32"] else LSQR_DRAM_BYTES_PER_ROW_PASS / LSQR_NCU_ALGO_BYTES_PER_ROW_PASS
+    lsqr_traffic = ratio * lsqr_bytes if ratio else None
     sketch_flops = 2.0 * d * m * (n + 1)   # S [A b], algorithmic
     sketch_tflops = sketch_flops / (ms_sketch / 1e3) / 1e12
     stages = {"sketch_ms": ms_sketch, "qr_rinv_ms": ms_factor, "lsqr_ms": ms_solve, "lsqr_kernel_ms": ms_kernel,
               "lsqr_iterations": iters, "sketch_algorithmic_tflops": sketch_tflops}
     roof = {"bound": "hbm",
-            "kernel": "lsqr_ff_kernel (one streamed A y / A^T u pass over the row-major float-float copy of "
-                      "A per LSQR iteration)",
+            "kernel": "lsqr_ff_kernel (one streamed A y / A^T u pass over the row-major copy of A per LSQR "
+                      "iteration: FP32 rows for FP32-stored A, float-float rows for FP64 A)",
             "achieved": lsqr_gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": lsqr_gbs / hbm_peak if lsqr_gbs else None,
             "traffic": lsqr_traffic, "peak_source": peak_src, "kernel_ms_per_launch": ms_kernel,
@@ -448,6 +479,203 @@ def run_ours(args, rank, local, ws):
             pass
     del A
     return line
+
+
+# ---------------------------------------------------------------------------
+# rand_svd workloads
+# ---------------------------------------------------------------------------
+def make_svd_problem(wl, dev):
+    """A = U diag(sigma) V^T (+ the noise floor noise * G / (sqrt m + sqrt n)),
+    U, V orthonormal factors of seeded Gaussian m x r and n x r matrices,
+    sigma from the workload's decay law; stored FP32 or FP64, column-major."""
+    import torch
+    m, n, r = wl["m"], wl["n"], wl["rank"]
+    su, sv, se = wl["seeds"]
+    i = torch.arange(r, device=dev, dtype=torch.float64)
+    sig = torch.exp(-i / 64.0) if wl["decay"].startswith("exp") else 10.0 ** (-i / 100.0)
+    g = torch.Generator(device=dev)
+    g.manual_seed(su)
+    U = torch.linalg.qr(torch.randn(m, r, generator=g, device=dev, dtype=torch.float64))[0]
+    g.manual_seed(sv)
+    V = torch.linalg.qr(torch.randn(n, r, generator=g, device=dev, dtype=torch.float64))[0]
+    At = (V * sig) @ U.t()                            # A^T row-major = A column-major
+    del U, V
+    if wl["noise"] > 0:
+        g.manual_seed(se)
+        At += (wl["noise"] / (math.sqrt(m) + math.sqrt(n))) * torch.randn(n, m, generator=g, device=dev,
+                                                                        dtype=torch.float64)
+    A = (At.float() if wl["f32"] else At).t()
+    return A
+
+
+def run_svd(args, rank, local, ws):
+    import torch
+    import randnla_gb300 as R
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = R.lib()
+    wl = workload(args)
+    m, n, k, p, q = wl["m"], wl["n"], wl["k"], wl["p"], wl["q"]
+    l = min(k + p, m, n)
+    A = make_svd_problem(wl, dev)
+    stream = torch.cuda.current_stream()
+
+    def outputs():
+        U = torch.zeros((l, m), dtype=torch.float64, device=dev).t()
+        sg = torch.zeros(l, dtype=torch.float64, device=dev)
+        Vt = torch.zeros((n, l), dtype=torch.float64, device=dev).t()
+        return U, sg, Vt
+
+    o = R.options(precision=R.Precision.BF16X, mode=R.Mode.RandNLA, power_iters=q, seed=42)
+    o64 = R.options(precision=R.Precision.FP64, mode=R.Mode.RandNLA, power_iters=q, seed=42)
+    U, sg, Vt = outputs()
+    R.rand_svd_dev(A, k, 1e-6, p, U, sg, Vt, o)
+    torch.cuda.synchronize()
+    U64, sg64, Vt64 = outputs()
+    fp64 = None
+    if not args.no_fp64:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        _, st64 = R.rand_svd_dev(A, k, 1e-6, p, U64, sg64, Vt64, o64)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = t0.elapsed_time(t1)
+        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_solve": ms64,
+                "stages_ms": {"range_finder": st64["ms_sketch"], "projection": st64["ms_factor"],
+                              "svd_finish": st64["ms_solve"]}}
+
+    # L2 flush between steps when A fits in L2 (a 512 MB write, outside the per-step events)
+    a_bytes = m * n * (4 if wl["f32"] else 8)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev) if a_bytes < (256 << 20) else None
+    clocks = ClockSampler(local)
+    clocks.start()
+    clocks.wait_first()
+    for _ in range(args.warmup):
+        R.rand_svd_dev(A, k, 1e-6, p, U, sg, Vt, o)
+    torch.cuda.synchronize()
+    barrier(ws)
+    launches0 = lib.rnla_kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stages = []
+    for i in range(args.steps):
+        if flush is not None:
+            flush.fill_(i & 255)
+        ev[i][0].record(stream)
+        _, st = R.rand_svd_dev(A, k, 1e-6, p, U, sg, Vt, o)
+        ev[i][1].record(stream)
+        stages.append((st["ms_sketch"], st["ms_factor"], st["ms_solve"]))
+    torch.cuda.synchronize()
+    launches = lib.rnla_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms_max = max_over_ranks(ms, ws)
+    value = ws * args.steps / (ms_max / 1e3)
+
+    # accuracy: top-k sigma against the FP64 path with the same Omega, and
+    # the approximation error ||A - U S V^T||_F of both
+    acc = {}
+    Ad = A.double()
+    err = float((Ad - (U[:, :k] * sg[:k]) @ Vt[:k]).norm())
+    acc["approx_error_fro"] = err
+    if fp64:
+        s1, s0 = sg[:k], sg64[:k]
+        acc["topk_sigma_max_rel_err_vs_fp64"] = float(((s1 - s0).abs() / s0).max())
+        acc["approx_error_fro_fp64_path"] = float((Ad - (U64[:, :k] * s0) @ Vt64[:k]).norm())
+    acc["U_orthonormality"] = float((U[:, :k].t() @ U[:, :k] - torch.eye(k, device=dev, dtype=torch.float64)).abs().max())
+    del Ad
+
+    peaks, peak_src = load_peaks()
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    rf = sum(x[0] for x in stages) / len(stages)
+    pr = sum(x[1] for x in stages) / len(stages)
+    fin = sum(x[2] for x in stages) / len(stages)
+    # the range finder streams A (as bf16 planes) 2q + 1 times and the
+    # projection once more; algorithmic bytes: A's own size per pass
+    passes = 2 * q + 2
+    rf_flops = 2.0 * m * n * l * (2 * q + 1)
+    esz = 4 if wl["f32"] else 8
+    rf_gbs = (2 * q + 1) * m * n * esz / (rf / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "split-bf16 tcgen05 GEMMs (2 planes power iterations, 3 planes projection/Gram) + FP64 Cholesky/SVD",
+        "data": "synthetic (seeded torch CUDA generator)",
+        "config": workload_config(args, wl, ws),
+        "path": "BF16X rand_svd (RandNLA mode): split-bf16 tensor-core range finder, CholeskyQR2, FP64 SVD finish",
+        "accuracy": acc,
+        "stages": {"range_finder_ms": rf, "projection_ms": pr, "svd_finish_ms": fin, "passes_over_A": passes},
+        "fp64_path": fp64,
+        "speedup_vs_fp64_path": (value / ws) / fp64["value"] if fp64 else None,
+        "e2e": None,
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "tensor", "kernel": "bfx_gemm_kernel (range-finder products, algorithmic 2 m n l "
+                                                  "flops each; 3 plane pairs at level 2)",
+                     "achieved": rf_flops / (rf / 1e3) / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                     "frac": rf_flops / (rf / 1e3) / 1e12 / bf16_peak, "traffic": None, "peak_source": peak_src,
+                     "range_finder_hbm_gbs_equivalent": rf_gbs, "hbm_peak": hbm_peak},
+        "clocks": clk,
+    }
+    if not args.no_e2e:
+        dt = torch.float32 if wl["f32"] else torch.float64
+        Ah = torch.empty((n, m), dtype=dt, pin_memory=True).t()
+        Ah.copy_(A.cpu())
+        Uh = torch.empty((l, m), dtype=torch.float64, pin_memory=True).t()
+        sh = torch.empty(l, dtype=torch.float64, pin_memory=True)
+        Vh = torch.empty((n, l), dtype=torch.float64, pin_memory=True).t()
+        Ad_ = torch.empty_like(A)
+        Ud, sd, Vd = outputs()
+
+        def e2e_call():
+            Ad_.copy_(Ah, non_blocking=True)
+            R.rand_svd_dev(Ad_, k, 1e-6, p, Ud, sd, Vd, o)
+            Uh.copy_(Ud, non_blocking=True)
+            sh.copy_(sd, non_blocking=True)
+            Vh.copy_(Vd, non_blocking=True)
+            torch.cuda.synchronize()
+
+        e2e_call()
+        t0 = time.perf_counter()
+        ke = max(2, args.steps // 2)
+        for _ in range(ke):
+            e2e_call()
+        t = max_over_ranks(time.perf_counter() - t0, ws)
+        line["e2e"] = {"value": ws * ke / t, "unit": UNIT, "h2d_bytes_per_step": m * n * esz,
+                       "d2h_bytes_per_step": 8 * (m * l + l + l * n), "steps": ke,
+                       "api": "rnla_rand_svd_dev with pinned host copies in and out on the same stream"}
+    return line
+
+
+def svd_cpu_child(args):
+    """`bench.py --cpu-leg port --workload *_svd`: the oracle restatement of the
+    reference rand_svd (lora_drivers.rs:30-69, reference semantics: the
+    tsog1 data flow of lora_helpers.rs:58-105) at full size, one JSON line per
+    solve, at most --steps solves or four minutes."""
+    import numpy as np
+    from oracle import oracle as O
+    wl = workload(args)
+    m, n, r = wl["m"], wl["n"], wl["rank"]
+    su, sv, se = wl["seeds"]
+    U = np.linalg.qr(np.random.default_rng(su).standard_normal((m, r)))[0]
+    V = np.linalg.qr(np.random.default_rng(sv).standard_normal((n, r)))[0]
+    i = np.arange(r)
+    sig = np.exp(-i / 64.0) if wl["decay"].startswith("exp") else 10.0 ** (-i / 100.0)
+    A = (U * sig) @ V.T
+    del U, V
+    if wl["noise"] > 0:
+        A += (wl["noise"] / (math.sqrt(m) + math.sqrt(n))) * np.random.default_rng(se).standard_normal((m, n))
+    if wl["f32"]:
+        A = A.astype(np.float32).astype(np.float64)
+    A = np.asfortranarray(A)
+    O.rand_svd(A[: max(wl["k"] + wl["p"], m // 64)], wl["k"], 1e-6, wl["p"])     # load libraries
+    t_all = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        O.rand_svd(A, wl["k"], 1e-6, wl["p"])
+        print(json.dumps({"seconds": time.perf_counter() - t0}), flush=True)
+        if time.perf_counter() - t_all > 240.0:
+            break
 
 
 # ---------------------------------------------------------------------------
@@ -610,6 +838,12 @@ def make_problem_host(wl):
 
 
 def cpu_child(args):
+    if args.workload in SVD_WORKLOADS:
+        return svd_cpu_child(args)
+    return ls_cpu_child(args)
+
+
+def ls_cpu_child(args):
     """`bench.py --cpu-leg port`: runs in its own process; prints one JSON
     line per full-size solve of the oracle port (sketch_and_precondition.rs:
     26-59: Gaussian S, S a, Householder QR, R^-1, explicit a R^-1, CGLS to the
@@ -676,9 +910,12 @@ def run_reference(args, rank, ws):
         "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy generator)",
         "impl": "reference", "config": workload_config(args, wl, ws),
-        "algorithm": "the reference's data flow (sketch_and_precondition.rs:26-59): dense Gaussian S "
-                     "(generated in column blocks), S a, Householder QR, explicit R^-1 and a R^-1, CGLS to "
-                     "tolerance %g, x = R^-1 z" % wl["tol"],
+        "algorithm": ("the reference rand_svd (lora_drivers.rs:30-69) with its tsog1 / RF1 / QB1 data flow "
+                      "(lora_helpers.rs:17-105), k=%d, s=%d" % (wl["k"], wl["p"]))
+                     if args.workload in SVD_WORKLOADS else
+                     ("the reference's data flow (sketch_and_precondition.rs:26-59): dense Gaussian S "
+                      "(generated in column blocks), S a, Householder QR, explicit R^-1 and a R^-1, CGLS to "
+                      "tolerance %g, x = R^-1 z" % wl["tol"]),
         "status": note, "runs": runs,
     }
     if runs:
@@ -709,17 +946,25 @@ def main():
         if rank == 0:
             print(json.dumps(line))
         return
-    line = run_ours(args, rank, local, ws)
+    if args.workload in SVD_WORKLOADS:
+        line = run_svd(args, rank, local, ws)
+    else:
+        line = run_ours(args, rank, local, ws)
     if rank == 0 and not args.no_cpu:
         cores = os.cpu_count()
         runs, note = cpu_port_runs(args, 1)
         cb = {"value": None, "unit": UNIT, "cores": cores, "kind": "port", "status": note}
         if runs:
             cb["value"] = 1.0 / runs[0]["seconds"]
-            cb["sample"] = ("one full-size solve (%.1f s, %d CGLS iterations) of the oracle restatement of "
-                            "sketch_and_precondition.rs:26-59 (numpy/LAPACK on all %d host threads, C sketch "
-                            "generator); no sampling or extrapolation"
-                            % (runs[0]["seconds"], runs[0]["cgls_iterations"], cores))
+            if args.workload in SVD_WORKLOADS:
+                cb["sample"] = ("one full-size rand_svd (%.1f s) of the oracle restatement of lora_drivers.rs:30-69 "
+                                "with the reference's tsog1 data flow (numpy/LAPACK on all %d host threads); no "
+                                "sampling or extrapolation" % (runs[0]["seconds"], cores))
+            else:
+                cb["sample"] = ("one full-size solve (%.1f s, %d CGLS iterations) of the oracle restatement of "
+                                "sketch_and_precondition.rs:26-59 (numpy/LAPACK on all %d host threads, C sketch "
+                                "generator); no sampling or extrapolation"
+                                % (runs[0]["seconds"], runs[0]["cgls_iterations"], cores))
         al = line.get("accuracy_lapack")
         if al:
             cb["lapack_qr_lstsq"] = {"value": 1.0 / al["seconds"], "unit": UNIT, "cores": cores,

@@ -71,6 +71,16 @@ RNLA_API uint64_t rnla_kernel_launches(void);
  * This returns the blocks no call is using to the driver; call it when the
  * library is idle.  A no-op before the first GPU call. */
 RNLA_API int rnla_release_cached_memory(void);
+/* Bounded-wait self-check (no counterpart in the reference).  Every device
+ * wait of the library (grid barriers of the persistent solvers, mbarrier
+ * phases of the bulk-copy rings) gives up after a time limit and reports
+ * RNLA_ERR_TIMEOUT instead of hanging.  This runs one such wait that cannot
+ * complete -- which = 0: a grid barrier over every SM whose arrival count
+ * never reaches the grid size; which = 1: an mbarrier phase that receives
+ * one of two arrivals -- with a limit of limit_us (1 .. 2e6) microseconds,
+ * and returns RNLA_ERR_TIMEOUT when the wait expired as designed.  The CUDA
+ * context stays usable.  Synchronises. */
+RNLA_API int rnla_check_bounded_wait(int32_t which, int64_t limit_us, void* stream);
 
 /* ---- sketch distributions: src/sketch.rs:9-13 ---- */
 typedef enum { RNLA_GAUSSIAN = 0, RNLA_UNIFORM = 1, RNLA_RADEMACHER = 2 } rnla_distribution;
@@ -290,8 +300,14 @@ RNLA_API int rnla_rand_svd(const double* a, int64_t m, int64_t n, int64_t lda, i
                   int64_t ldvt, int64_t* r_out);
 /* Extended form: options select reference / RandNLA mode, precision, q and
  * the generator; `singular_values` (nullable, r values) receives the
- * diagonal of S; stats (nullable).  Both modes run in FP64; a tensor-core
- * precision returns RNLA_ERR_UNSUPPORTED. */
+ * diagonal of S; stats (nullable).  Reference mode runs in FP64 (a
+ * tensor-core precision returns RNLA_ERR_UNSUPPORTED).  RandNLA mode under
+ * RNLA_PREC_BF16X runs the range finder (A Omega, A^T Q, A Z) and the
+ * projection B = Q^T A as split-bf16 tcgen05 GEMMs with FP32 accumulation
+ * (digits_a = planes of the power-iteration products, default 2; the
+ * projection and the CholeskyQR2 Grams and triangular products use 3), the
+ * Cholesky, R^-1 and small SVD in FP64; Omega is the FP64 path's Gaussian,
+ * so the two precisions can be compared on the same Omega. */
 RNLA_API int rnla_rand_svd_ex(const double* a, int64_t m, int64_t n, int64_t lda, int64_t k, double epsilon,
                      int64_t s, const rnla_options* opt, double* u, int64_t ldu, double* sigma,
                      int64_t lds, double* vt, int64_t ldvt, int64_t* r_out, rnla_stats* stats);
@@ -427,10 +443,11 @@ RNLA_API int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64
                                       int64_t d, int32_t dist, const rnla_rng* rng, int32_t precision,
                                       int32_t digits, double* y_dev, int64_t ldy, void* stream);
 
-/* C (ldc) = X^T Y for X (k x mm, ldx) and Y (k x nn, ldy), both double, on
- * the FP64 CUDA cores.  The tensor-core precisions return
- * RNLA_ERR_UNSUPPORTED: a two-sided digit-sliced GEMM is not built (the
- * tensor-core kernel applies a generated sketch to one data operand). */
+/* C (ldc) = X^T Y for X (k x mm, ldx) and Y (k x nn, ldy), both double:
+ * RNLA_PREC_FP64 on the FP64 CUDA cores; RNLA_PREC_BF16X on the split-bf16
+ * tcgen05 GEMM, each operand cut into max(digits_x, digits_y) bf16 planes
+ * (1..3, default 3) and the plane pairs p + q < planes accumulated in FP32
+ * (3 planes: ~24 significant bits per operand); RNLA_PREC_BF16 = one plane. */
 RNLA_API int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, const double* y_dev,
                      int64_t nn, int64_t ldy, int32_t precision, int32_t digits_x,
                      int32_t digits_y, double* c_dev, int64_t ldc, void* stream);

@@ -414,6 +414,19 @@ def blendenpik_dev(a, b, x, epsilon, l, sampling_factor, opts=None):
     return st.as_dict()
 
 
+def lsrn_dev(a, b, x, epsilon, l, sampling_factor, opts=None):
+    """rnla_lsrn_overdetermined_dev on torch CUDA tensors (same conventions
+    as blendenpik_dev)."""
+    import torch
+    o = opts if opts is not None else options()
+    st = Stats()
+    m, n = a.shape
+    _check(lib().rnla_lsrn_overdetermined_dev(
+        _dptr(a), int(a.dtype == torch.float32), m, n, _ld(a), _dptr(b), epsilon, l, sampling_factor,
+        ctypes.byref(o), _dptr(x), ctypes.byref(st), _stream()))
+    return st.as_dict()
+
+
 def solve_batched_dev(problems, epsilon, l, sampling_factor, opts=None):
     """rnla_solve_batched: problems is a sequence of (a, b, x) torch CUDA
     tensors as for blendenpik_dev.  Returns (statuses, stats): one status

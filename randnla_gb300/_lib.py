@@ -113,6 +113,7 @@ SIGNATURES = [
      [c_vp, c_i32, c_i64, c_i64, c_i64, c_vp, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options), c_vp,
       ctypes.POINTER(Stats), c_vp]),
     ("rnla_release_cached_memory", ctypes.c_int, []),
+    ("rnla_check_bounded_wait", ctypes.c_int, [c_i32, c_i64, c_vp]),
     ("rnla_solve_batched", ctypes.c_int,
      [ctypes.POINTER(LsProblem), c_i64, c_dbl, c_i64, c_dbl, ctypes.POINTER(Options),
       ctypes.POINTER(c_i32), ctypes.POINTER(Stats), c_vp]),

@@ -337,6 +337,84 @@ static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_
     return r;
 }
 
+// Orthonormal basis of Y (m x l, ld m, m >= l) in place: CholeskyQR2 with
+// the Grams and the triangular products on the split-bf16 tensor-core GEMM
+// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP64; the
+// FP64 Householder basis when a Cholesky pivot fails.  Returns 1 on fallback.
+static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l) {
+    if (m < l) return orthonormalize(ctx, Y, m, l, m, true), 1;
+    DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), T((size_t)m * l, ctx.stream);
+    for (int pass = 0; pass < 2; ++pass) {
+        {
+            BfxPlanes ya, yb;
+            bfx_planes(ctx, ya, Y, false, l, m, m, 1, bfx_tile_rows(3, true), 3);     // columns of Y
+            bfx_planes(ctx, yb, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
+            bfx_gemm(ctx, 3, ya, yb, G, l, false);                                    // G = Y^T Y
+        }
+        if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
+            orthonormalize(ctx, Y, m, l, m, true);
+            return 1;
+        }
+        {
+            BfxPlanes yr, wr;
+            bfx_planes(ctx, yr, Y, false, m, l, 1, m, bfx_tile_rows(3, true), 3);     // rows of Y
+            bfx_planes(ctx, wr, Ri, false, l, l, l, 1, bfx_tile_rows(3, false), 3);   // columns of R^-1
+            bfx_gemm(ctx, 3, yr, wr, T, m, false);                                    // T = Y R^-1
+        }
+        copy_matrix(ctx, m, l, T, m, Y, m);
+    }
+    return 0;
+}
+
+// The RandNLA-mode range finder and projection on the tensor cores
+// (lora_helpers.rs:17-44 with a Gaussian Omega and q power iterations):
+// Y = A Omega, q times {Z = orth(A^T Y), Y = orth(A Z)}, B = Q^T A, then the
+// FP64 small-SVD finish of lora_drivers.rs:51-68.  A is read as bf16 planes
+// made once: its rows at level 2 for the A Z products and its columns with
+// three planes (A^T Y at level 2, B = Q^T A at level 3, which holds FP32
+// data exactly).  Omega is the FP64 Gaussian of the FP64 path (same key).
+static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda, int64_t k,
+                            int64_t l, const rnla_options& o, double* U, int64_t ldu, double* sig, double* Vt,
+                            int64_t ldvt, int& fallbacks, StageTimer& tm) {
+    const int LP = (o.digits_a >= 1 && o.digits_a <= 3) ? o.digits_a : 2;   // power-iteration level
+    const RngKey key = key_of(&o.rng);
+    BfxPlanes arow, acol;
+    bfx_planes(ctx, arow, Av, a_f32, m, n, 1, lda, bfx_tile_rows(LP, true), LP);   // A(i, k) = A[i + k lda]
+    bfx_planes(ctx, acol, Av, a_f32, n, m, lda, 1, bfx_tile_rows(3, true), 3);    // A^T(i, k) = A[k + i lda]
+    DevBuf<double> Y((size_t)m * l, ctx.stream), Z((size_t)n * l, ctx.stream);
+    {
+        DevBuf<double> Om((size_t)n * l, ctx.stream);
+        sketch_fill_f64(ctx, DIST_GAUSSIAN, key, n, l, Om, n);
+        BfxPlanes op;
+        bfx_planes(ctx, op, Om, false, l, n, n, 1, bfx_tile_rows(LP, false), LP);
+        bfx_gemm(ctx, LP, arow, op, Y, m, false);                                    // Y = A Omega
+    }
+    fallbacks += orthonormalize_bfx(ctx, Y, m, l);
+    for (int it = 0; it < o.power_iters; ++it) {
+        {
+            BfxPlanes yp;
+            bfx_planes(ctx, yp, Y, false, l, m, m, 1, bfx_tile_rows(LP, false), LP);
+            bfx_gemm(ctx, LP, acol, yp, Z, n, false);                                // Z = A^T Q
+        }
+        fallbacks += orthonormalize_bfx(ctx, Z, n, l);
+        {
+            BfxPlanes zp;
+            bfx_planes(ctx, zp, Z, false, l, n, n, 1, bfx_tile_rows(LP, false), LP);
+            bfx_gemm(ctx, LP, arow, zp, Y, m, false);                                // Y = A Z
+        }
+        fallbacks += orthonormalize_bfx(ctx, Y, m, l);
+    }
+    tm.mark();
+    DevBuf<double> B((size_t)l * n, ctx.stream);
+    {
+        BfxPlanes qp;
+        bfx_planes(ctx, qp, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
+        bfx_gemm(ctx, 3, acol, qp, B, l, true);                                      // B = Q^T A (as (A^T Q)^T)
+    }
+    tm.mark();
+    return svd_finish(ctx, RNLA_PREC_FP64, Y, m, l, B, n, k, U, ldu, sig, Vt, ldvt);
+}
+
 static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,
                              int64_t k, double epsilon, int64_t s, const rnla_options& o, double* U,
                              int64_t ldu, double* sig, double* Vt, int64_t ldvt, rnla_stats* st) {
@@ -360,11 +438,12 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
     if (m <= 0 || n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must be non-empty");
     StageTimer tm(ctx.stream);
     tm.mark();
-    // A as double (stored-FP32 inputs are widened once for the FP64 products)
+    // A as double for the FP64 products (stored-FP32 inputs are widened once);
+    // the tensor-core path reads FP32 or FP64 A directly
     DevBuf<double> Aw;
     const double* A = static_cast<const double*>(Av);
     int64_t ld = lda;
-    if (a_f32) {
+    if (a_f32 && o.precision == RNLA_PREC_FP64) {
         Aw.alloc((size_t)m * n, ctx.stream);
         copy_matrix_f32_to_f64(ctx, m, n, static_cast<const float*>(Av), lda, Aw, m);
         A = Aw.get();
@@ -372,7 +451,14 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
     }
     int64_t r = 0;
     int fallbacks = 0;
-    if (o.mode == RNLA_MODE_REFERENCE) {
+    if (o.mode == RNLA_MODE_RANDNLA && o.precision != RNLA_PREC_FP64) {
+        if (!tc_available(ctx))
+            fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
+        int64_t l = k + s;
+        const int64_t mn = m < n ? m : n;
+        if (l > mn) l = mn;
+        r = rand_svd_bfx(ctx, Av, a_f32, m, n, lda, k, l, o, U, ldu, sig, Vt, ldvt, fallbacks, tm);
+    } else if (o.mode == RNLA_MODE_REFERENCE) {
         if (o.precision != RNLA_PREC_FP64)
             fail(RNLA_ERR_UNSUPPORTED, "reference mode runs in FP64 only");
         const bool finite = all_finite(ctx, m, n, A, ld);
@@ -385,12 +471,8 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
         r = svd_finish(ctx, o.precision, Q.p(), m, cq, B, n, k, U, ldu, sig, Vt, ldvt);
     } else {
         // Gaussian range finder, q power iterations, re-orthonormalised after
-        // every product.  FP64 only: A^T Q and Q^T A would need a two-sided
-        // digit-sliced tensor-core GEMM, which is not built (the tensor-core
-        // kernel applies a generated sketch to one data operand).
+        // every product, on the FP64 CUDA cores.
         const int prec = o.precision;
-        if (prec != RNLA_PREC_FP64)
-            fail(RNLA_ERR_UNSUPPORTED, "rand_svd in RandNLA mode runs in FP64 only");
         int64_t l = k + s;
         const int64_t mn = m < n ? m : n;
         if (l > mn) l = mn;
@@ -516,9 +598,16 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // float-float factorization on the FP32 pipe (qr_ff.cu)
         householder_qr_ff(ctx, SK, d, n, nc, d);
         inv_ok = upper_inverse_ff(ctx, SK, n, d, Mi, n);
+    } else if (o.precision != RNLA_PREC_FP64 && qr_ff_tsqr_supported(ctx, d, n, nc)) {
+        // taller sketches (d = 4096 at n = 1024): two row halves, then their R blocks
+        householder_qr_ff_tsqr(ctx, SK, d, n, nc, d);
+        inv_ok = upper_inverse_ff(ctx, SK, n, d, Mi, n);
     } else {
         householder_qr(ctx, SK, d, n, nc, d, tau);
         inv_ok = upper_inverse(ctx, SK, n, d, Mi, n);               // line 55
+        // the float-float LSQR applies M rounded to ~48 bits; x = M z must use
+        // that same M (with kappa(R) = 1e6 the difference would show in x)
+        if (inv_ok && lsqr_in.ready) ff_round_upper(ctx, Mi, n, n);
     }
     if (!inv_ok) fail(RNLA_ERR_SINGULAR_MATRIX, "the R factor of the sketch is singular");
     tm.mark();
@@ -621,6 +710,8 @@ static void sketch_solve_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, i
     }
     if (o.precision != RNLA_PREC_FP64 && qr_ff_supported(ctx, d, n, nc)) {
         householder_qr_ff(ctx, SK, d, n, nc, d);
+    } else if (o.precision != RNLA_PREC_FP64 && qr_ff_tsqr_supported(ctx, d, n, nc)) {
+        householder_qr_ff_tsqr(ctx, SK, d, n, nc, d);
     } else {
         DevBuf<double> tau(n, ctx.stream);
         householder_qr(ctx, SK, d, n, nc, d, tau);

@@ -63,8 +63,9 @@ constexpr int NB_URDY = 1;      // + (k & 1): u of tile k written
 constexpr int NB_UFREE = 3;     // + (k & 1): u of tile k consumed
 
 struct Args {
-    const float2* AF;           // row-major float-float copy of A, m x ldf
+    const float2* AF;           // row-major copy of A, m rows of rowq 16-byte chunks
     int64_t m, n, ldf, hp;      // hp = ldf / 2 column pairs
+    int64_t rowq;               // 16-byte chunks per row: hp (float-float rows) or ldf / 4 (FP32 rows)
     int R;                      // rows per tile (multiple of 8)
     int ST;                     // ring stages
     int64_t ntiles;
@@ -130,9 +131,10 @@ __device__ __forceinline__ void ring_issue(const Args& a, Ring& rg) {
         const int64_t t = (int64_t)blockIdx.x + rg.ik * (int64_t)gridDim.x;
         const int64_t r0 = t * a.R;
         const int64_t rows = min((int64_t)a.R, a.m - r0);
-        const uint32_t bytes = (uint32_t)(rows * a.ldf * 8);
+        const uint32_t bytes = (uint32_t)(rows * a.rowq * 16);
         mbar_expect_tx(&rg.full[rg.ist], bytes);
-        bulk_g2s(rg.tiles + (size_t)rg.ist * a.R * a.hp, a.AF + r0 * a.ldf, bytes, &rg.full[rg.ist]);
+        bulk_g2s(rg.tiles + (size_t)rg.ist * a.R * a.rowq, reinterpret_cast<const float4*>(a.AF) + r0 * a.rowq,
+                 bytes, &rg.full[rg.ist]);
         rg.ist = (rg.ist + 1 == a.ST) ? 0 : rg.ist + 1;
         rg.ik = (rg.ik + 1 == rg.ntl) ? 0 : rg.ik + 1;
         ++rg.inflight;
@@ -149,9 +151,10 @@ __device__ __forceinline__ void ring_copy(const Args& a, const Ring& rg, int st,
     const int64_t t = (int64_t)blockIdx.x + ik * (int64_t)gridDim.x;
     const int64_t r0 = t * a.R;
     const int64_t rows = min((int64_t)a.R, a.m - r0);
-    const uint32_t bytes = (uint32_t)(rows * a.ldf * 8);
+    const uint32_t bytes = (uint32_t)(rows * a.rowq * 16);
     mbar_expect_tx(&rg.full[st], bytes);
-    bulk_g2s(rg.tiles + (size_t)st * a.R * a.hp, a.AF + r0 * a.ldf, bytes, &rg.full[st]);
+    bulk_g2s(rg.tiles + (size_t)st * a.R * a.rowq, reinterpret_cast<const float4*>(a.AF) + r0 * a.rowq, bytes,
+             &rg.full[st]);
 }
 
 // Fused roles: the stage a warp has just read into registers is released
@@ -613,6 +616,206 @@ __device__ bool ff_pass_fused(const Args& a, Ring& rg, float4* scratch, float2 c
     return *err == 0;
 }
 
+// The fused pass over FP32 rows (A stored in FP32: rows of ldf floats, ldf =
+// n rounded up to a multiple of 4, 4 bytes per element instead of 8).  Chunk
+// c of a row holds columns 4c .. 4c+3; lane l of every warp takes chunks
+// c = l + 32 kk (KC per lane), i.e. the column pairs 2c and 2c+1, so y and the
+// A^T u accumulators are 2 KC packed pairs per lane.  The data are exact in
+// FP32, so each product is a * (y_hi + y_lo) with the FMA error term of
+// a * y_hi (one multiply-add fewer than a float-float element).  Everything
+// else -- ring, row ownership, u, the per-warp column sums -- is as in
+// ff_pass_fused.
+template <int KC, int RW>
+__device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, float2 c1, float2 c2, float2 c3,
+                                  bool dot, const float2* oldv, const float2* bvec, float2* dst, bool want_b2,
+                                  bool acc_at, volatile int* err) {
+    constexpr int R = WF * RW;
+    constexpr int KP = 2 * KC;
+    __shared__ float2 wred[WF][2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int hp = (int)a.hp;
+    const int hq = (int)a.rowq;
+    const int64_t ntl = rg.ntl;
+    f32x2 yh[KP], nyh[KP], yl[KP];
+#pragma unroll
+    for (int kk = 0; kk < KC; ++kk) {
+        const int c = lane + 32 * kk;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
+            if (dot && c < hq) { y0 = a.yF[4 * c + 2 * h]; y1 = a.yF[4 * c + 2 * h + 1]; }
+            yh[2 * kk + h] = pk2(y0.x, y1.x);
+            nyh[2 * kk + h] = pk2(-y0.x, -y1.x);
+            yl[2 * kk + h] = pk2(y0.y, y1.y);
+        }
+    }
+    f32x2 ah[KP], al[KP];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) { ah[k] = 0ull; al[k] = 0ull; }
+    float sqh = 0.f, sql = 0.f, b2h = 0.f, b2l = 0.f;
+    constexpr int SHL = (RW == 1) ? 5 : (RW == 2) ? 4 : (RW == 4) ? 3 : 2;
+    const bool owner = (lane & ((1 << SHL) - 1)) == 0;
+    const int rw = lane >> SHL;
+    auto row_of = [&](int64_t kk) { return ((int64_t)blockIdx.x + kk * (int64_t)gridDim.x) * R + warp + WF * rw; };
+    auto fetch = [&](int64_t kk, float2& u, float2& bv) {
+        u = make_float2(0.f, 0.f);
+        bv = make_float2(0.f, 0.f);
+        if (owner && kk < ntl) {
+            const int64_t i = row_of(kk);
+            if (i < a.m) {
+                if (oldv) u = oldv[i];
+                if (bvec) bv = bvec[i];
+            }
+        }
+    };
+    float2 qu0, qb0, qu1, qb1;
+    fetch(0, qu0, qb0);
+    fetch(1, qu1, qb1);
+#pragma unroll 1
+    for (int64_t k = 0; k < ntl; ++k) {
+        const float2 uo = qu0, bb = qb0;
+        qu0 = qu1;
+        qb0 = qb1;
+        fetch(k + 2, qu1, qb1);
+        const int st = rg.cst;
+        const bool ok = mbar_wait(&rg.full[st], rg.cph, err);
+        ring_advance(a, rg);
+        const int64_t r0 = ((int64_t)blockIdx.x + k * (int64_t)gridDim.x) * R;
+        const int rows = (int)min((int64_t)R, a.m - r0);
+        const ulonglong2* tile = reinterpret_cast<const ulonglong2*>(rg.tiles) + (size_t)st * R * hq;
+        ulonglong2 v[RW][KC];
+#pragma unroll
+        for (int w = 0; w < RW; ++w) {
+            const int r = warp + WF * w;
+            const bool rv = ok && r < rows;
+#pragma unroll
+            for (int kk = 0; kk < KC; ++kk) {
+                const int c = lane + 32 * kk;
+                v[w][kk] = (rv && c < hq) ? tile[(size_t)r * hq + c] : make_ulonglong2(0ull, 0ull);
+            }
+        }
+        ring_release(a, rg, st, lane, err);
+        float tvh[RW], tvl[RW];
+#pragma unroll
+        for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
+        if (dot) {
+            f32x2 sh[RW][2], sl[RW][2];
+#pragma unroll
+            for (int w = 0; w < RW; ++w) { sh[w][0] = sh[w][1] = sl[w][0] = sl[w][1] = 0ull; }
+#pragma unroll
+            for (int kk = 0; kk < KC; ++kk) {
+#pragma unroll
+                for (int w = 0; w < RW; ++w) {
+                    ff2_madd_x(v[w][kk].x, yh[2 * kk], nyh[2 * kk], yl[2 * kk], sh[w][0], sl[w][0]);
+                    ff2_madd_x(v[w][kk].y, yh[2 * kk + 1], nyh[2 * kk + 1], yl[2 * kk + 1], sh[w][1], sl[w][1]);
+                }
+            }
+#pragma unroll
+            for (int w = 0; w < RW; ++w) {
+                ff2_acc(sh[w][0], sl[w][0], sh[w][1], sl[w][1]);
+                const float2 H = upk2(sh[w][0]), L = upk2(sl[w][0]);
+                float h = H.x, l = L.x;
+                ff_acc(h, l, H.y, L.y);
+                tvh[w] = h;
+                tvl[w] = l;
+            }
+            int off = 16;
+#pragma unroll
+            for (int half = RW / 2; half >= 1; half /= 2) {
+                const bool up = (lane & off) != 0;
+#pragma unroll
+                for (int k2 = 0; k2 < half; ++k2) {
+                    const float sh_ = up ? tvh[k2] : tvh[k2 + half], sl_ = up ? tvl[k2] : tvl[k2 + half];
+                    float kh = up ? tvh[k2 + half] : tvh[k2], kl = up ? tvl[k2 + half] : tvl[k2];
+                    const float rh = __shfl_xor_sync(0xffffffffu, sh_, off);
+                    const float rl = __shfl_xor_sync(0xffffffffu, sl_, off);
+                    ff_acc(kh, kl, rh, rl);
+                    tvh[k2] = kh;
+                    tvl[k2] = kl;
+                }
+                off >>= 1;
+            }
+            for (; off >= 1; off >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, tvh[0], off);
+                const float ol = __shfl_xor_sync(0xffffffffu, tvl[0], off);
+                ff_acc(tvh[0], tvl[0], oh, ol);
+            }
+        }
+        float2 nv = make_float2(0.f, 0.f);
+        if (owner) {
+            const float2 tv = ff_norm(tvh[0], tvl[0]);
+            nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
+            const int r = warp + WF * rw;
+            if (ok && r < rows) {
+                dst[r0 + r] = nv;
+                ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
+                if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
+            }
+        }
+        if (acc_at) {
+            f32x2 uh[RW], nuh[RW], ul[RW];
+#pragma unroll
+            for (int w = 0; w < RW; ++w) {
+                const float x = __shfl_sync(0xffffffffu, nv.x, w << SHL);
+                const float y = __shfl_sync(0xffffffffu, nv.y, w << SHL);
+                uh[w] = pk2(x, x);
+                nuh[w] = pk2(-x, -x);
+                ul[w] = pk2(y, y);
+            }
+#pragma unroll
+            for (int kk = 0; kk < KC; ++kk) {
+#pragma unroll
+                for (int w = 0; w < RW; ++w) {
+                    ff2_madd_x(v[w][kk].x, uh[w], nuh[w], ul[w], ah[2 * kk], al[2 * kk]);
+                    ff2_madd_x(v[w][kk].y, uh[w], nuh[w], ul[w], ah[2 * kk + 1], al[2 * kk + 1]);
+                }
+            }
+        }
+    }
+    const float2 sq = ff_warp_sum(sqh, sql);
+    const float2 b2 = ff_warp_sum(b2h, b2l);
+    if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
+    if (acc_at) {
+#pragma unroll
+        for (int kk = 0; kk < KC; ++kk) {
+            const int c = lane + 32 * kk;
+            if (c < hq) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float2 H = upk2(ah[2 * kk + h]), L = upk2(al[2 * kk + h]);
+                    scratch[(size_t)warp * hp + 2 * c + h] = make_float4(H.x, L.x, H.y, L.y);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (acc_at) {
+        float4* P4 = reinterpret_cast<float4*>(a.partF) + (size_t)blockIdx.x * hp;
+        for (int p = tid; p < hp; p += TF) {
+            float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+#pragma unroll
+            for (int w = 0; w < WF; ++w) {
+                const float4 q = scratch[(size_t)w * hp + p];
+                ff_acc(h0, l0, q.x, q.y);
+                ff_acc(h1, l1, q.z, q.w);
+            }
+            const float2 c0 = ff_norm(h0, l0), c1v = ff_norm(h1, l1);
+            P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
+        }
+    }
+    if (tid == 0) {
+        float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
+        for (int w = 0; w < WF; ++w) {
+            ff_acc(h, l, wred[w][0].x, wred[w][0].y);
+            ff_acc(h2, l2, wred[w][1].x, wred[w][1].y);
+        }
+        a.spF[blockIdx.x * 4 + 0] = ff_norm(h, l);
+        a.spF[blockIdx.x * 4 + 3] = ff_norm(h2, l2);
+    }
+    __syncthreads();
+    return *err == 0;
+}
+
 // Sum over CTAs of scalar slot `slot` (warp-level, identical in every CTA).
 __device__ __forceinline__ float2 sum_slot(const Args& a, int slot, int lane) {
     float h = 0.f, l = 0.f;
@@ -719,7 +922,7 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 
 // FUSED selects the pass: fused roles on TF threads, or split row/column
 // roles on T threads.
-template <int KP, int RW, bool FUSED>
+template <int KP, int RW, bool FUSED, bool F32 = false>
 __global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
     constexpr int NT = FUSED ? TF : T;
     constexpr int NWC = NT / 32;
@@ -750,7 +953,7 @@ __global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
     rg.issued = &issued;
     rg.consumed = 0;
     // split roles: the u hand-off buffers; fused roles: the column scratch
-    unsigned char* extra = dsm + (size_t)a.ST * a.R * a.ldf * 8;
+    unsigned char* extra = dsm + (size_t)a.ST * a.R * a.rowq * 16;
     ulonglong2* usm = reinterpret_cast<ulonglong2*>(extra);
     float4* scratch = reinterpret_cast<float4*>(extra);
     volatile int* err = &err_s;
@@ -799,7 +1002,8 @@ __global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
 #define LSFF_PASS(...)                                                                 \
     do {                                                                               \
         bool pass_ok;                                                                  \
-        if constexpr (FUSED) pass_ok = ff_pass_fused<KP, RW>(a, rg, scratch, __VA_ARGS__, err); \
+        if constexpr (F32) pass_ok = ff_pass_fused_f32<KP / 2, RW>(a, rg, scratch, __VA_ARGS__, err); \
+        else if constexpr (FUSED) pass_ok = ff_pass_fused<KP, RW>(a, rg, scratch, __VA_ARGS__, err); \
         else pass_ok = ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err);                  \
         if (!pass_ok) {                                                                \
             set_status(a, KSTATUS_BARRIER_TIMEOUT);                                    \
@@ -1109,9 +1313,39 @@ __global__ void rowmajor_split_kernel(const TA* __restrict__ A, int64_t m, int64
     }
 }
 
+// Row-major FP32 copy: row i is ldq floats (n rounded up to a multiple of 4,
+// zero beyond n), so a 16-byte chunk holds 4 consecutive columns.  32 x 32
+// tiles through shared memory.
+__global__ void rowmajor_f32_kernel(const float* __restrict__ A, int64_t m, int64_t n, int64_t lda,
+                                    float* __restrict__ AQ, int64_t ldq) {
+    __shared__ float tile[32][33];
+    const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int64_t i = i0 + threadIdx.x, j = j0 + k;
+        tile[k][threadIdx.x] = (i < m && j < n) ? A[i + j * lda] : 0.f;
+    }
+    __syncthreads();
+    for (int k = threadIdx.y; k < 32; k += 8) {
+        const int64_t i = i0 + k, j = j0 + threadIdx.x;
+        if (i < m && j < ldq) AQ[i * ldq + j] = tile[threadIdx.x][k];
+    }
+}
+
 __global__ void vec_split_kernel(const double* __restrict__ v, int64_t n, float2* __restrict__ out) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         out[i] = ff_split(v[i]);
+}
+
+// M <- hi + lo of its float-float split (upper part, in place).
+__global__ void ff_round_kernel(double* __restrict__ M, int64_t n, int64_t ldm) {
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n * n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % n, j = idx / n;
+        if (i <= j) {
+            const float2 v = ff_split(M[i + j * ldm]);
+            M[i + j * ldm] = (double)v.x + (double)v.y;
+        }
+    }
 }
 
 // MF = split(M) (column-major, upper part), MtF = its transpose.
@@ -1126,8 +1360,8 @@ __global__ void msplit_kernel(const double* __restrict__ M, int64_t n, int64_t l
     }
 }
 
-template <int KP, int RW, bool FUSED>
-static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW, FUSED>; }
+template <int KP, int RW, bool FUSED, bool F32 = false>
+static const void* kernel_kp() { return (const void*)lsqr_ff_kernel<KP, RW, FUSED, F32>; }
 
 // Kernel for hp column pairs: the y registers cover hp (KP chunks of 32
 // pairs per lane) and a tile (R rows) is at most 64 KB, so the ring holds 3
@@ -1146,10 +1380,26 @@ static KernelPick pick_kernel(int64_t hp) {
     if (hp <= 256) return {kernel_kp<8, 2, true>(), WF * 2, TF, true};
     return {kernel_kp<16, 1, false>(), WA * 1, T, false};
 }
+// FP32 rows: hq 16-byte chunks (4 columns each) per row, KC = KP / 2 chunks
+// per lane, fused roles throughout (n <= 1024: 8 chunks per lane, one row
+// per warp).
+static KernelPick pick_kernel_f32(int64_t hq) {
+    if (hq <= 32) return {kernel_kp<2, 8, true, true>(), WF * 8, TF, true};
+    if (hq <= 64) return {kernel_kp<4, 4, true, true>(), WF * 4, TF, true};
+    if (hq <= 128) return {kernel_kp<8, 2, true, true>(), WF * 2, TF, true};
+    return {kernel_kp<16, 1, true, true>(), WF * 1, TF, true};
+}
 
 }  // namespace lsff
 
 bool lsqr_ff_supported(int64_t n) { return n >= 1 && n <= lsff::MAX_N; }
+
+void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm) {
+    int g = (int)div_up(n * n, 256);
+    if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+    lsff::ff_round_kernel<<<g, 256, 0, ctx.stream>>>(M, n, ldm);
+    RNLA_LAUNCH_CHECK();
+}
 
 // Float-float copies of A (row-major, column-pair order) and b, enqueued on
 // `st`.
@@ -1158,8 +1408,8 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
     if (a_f32)
-        rowmajor_split_kernel<float><<<grid, dim3(32, 8), 0, st>>>(static_cast<const float*>(A), m, n, lda,
-                                                                   reinterpret_cast<float*>(AF), ldf);
+        rowmajor_f32_kernel<<<grid, dim3(32, 8), 0, st>>>(static_cast<const float*>(A), m, n, lda,
+                                                          reinterpret_cast<float*>(AF), ldf);
     else
         rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,
                                                                     reinterpret_cast<float*>(AF), ldf);
@@ -1174,8 +1424,11 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
                      LsqrFFInput& in) {
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
     in.A = A; in.m = m; in.n = n;
-    in.ldf = (n + 1) & ~1LL;
-    in.AF.alloc((size_t)m * in.ldf, ctx.stream);
+    in.f32 = a_f32;
+    // FP32 data: a row-major FP32 copy (ldf = n rounded up to 4 floats);
+    // FP64 data: the float-float copy (ldf = n rounded up to 2 pairs)
+    in.ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
+    in.AF.alloc(a_f32 ? (size_t)m * in.ldf / 2 : (size_t)m * in.ldf, ctx.stream);
     in.bF.alloc(m, ctx.stream);
     const cudaStream_t side = side_stream(ctx.device);
     stream_wait(side, ctx.stream);                 // buffers allocated, A and b written
@@ -1190,19 +1443,22 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
                          double* arnorms_dev, const LsqrFFInput* pre, LsqrPending* pend) {
     using namespace lsff;
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
-    if (pre && (pre->A != A || pre->m != m || pre->n != n)) pre = nullptr;
+    if (pre && (pre->A != A || pre->m != m || pre->n != n || pre->f32 != a_f32)) pre = nullptr;
     cudaStream_t st = ctx.stream;
-    const int64_t ldf = (n + 1) & ~1LL;
+    const int64_t ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
     const int64_t hp = ldf / 2;
-    const KernelPick kp = pick_kernel(hp);
+    const int64_t rowq = a_f32 ? ldf / 4 : hp;
+    const KernelPick kp = a_f32 ? pick_kernel_f32(rowq) : pick_kernel(hp);
     const void* k = kp.fn;
     const int R = kp.R;
-    const size_t stage = (size_t)R * ldf * 8;
-    int STn = (int)(RING_BYTES / stage);
-    STn = STn > MAX_ST ? MAX_ST : STn;
-    if (STn < 3) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): tile ring does not fit");
+    const size_t stage = (size_t)R * rowq * 16;
     // fused: per-warp column scratch; split: the two u hand-off buffers
     const size_t extra = kp.fused ? (size_t)WF * hp * 16 : (size_t)2 * R * 16;
+    int STn = (int)(RING_BYTES / stage);
+    STn = STn > MAX_ST ? MAX_ST : STn;
+    const size_t smem_cap = 224 * 1024;            // dynamic shared memory per CTA (static use is < 2 KB)
+    if ((size_t)STn * stage + extra > smem_cap) STn = extra < smem_cap ? (int)((smem_cap - extra) / stage) : 0;
+    if (STn < 3) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): tile ring does not fit");
     const size_t smem = (size_t)STn * stage + extra;
     RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nb = 0;
@@ -1221,7 +1477,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
         AF = pre->AF.get();
         bF = pre->bF.get();
     } else {
-        AFo.alloc((size_t)m * ldf, st);
+        AFo.alloc(a_f32 ? (size_t)m * ldf / 2 : (size_t)m * ldf, st);
         bFo.alloc(m, st);
         build_ff_input(ctx, st, A, a_f32, m, n, lda, b, ldf, AFo, bFo);
         AF = AFo.get();
@@ -1256,7 +1512,8 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
         RNLA_LAUNCH_CHECK();
         a.x0F = x0F.get();
     }
-    a.AF = AF; a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.R = R; a.ST = STn; a.ntiles = div_up(m, R);
+    a.AF = AF; a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.rowq = rowq; a.R = R; a.ST = STn;
+    a.ntiles = div_up(m, R);
     a.bF = bF;
     a.uF = uF.get(); a.yF = yF.get(); a.gF = gF.get(); a.vF = vF.get(); a.wF = wF.get(); a.xF = xF.get();
     a.vunF = vunF.get(); a.varF = varF.get(); a.partF = partF.get(); a.spF = spF.get(); a.colsq = colsq.get();

@@ -524,6 +524,48 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     ctx.check_status("householder_qr (float-float)");
 }
 
+// T (2n x nc) = the first n rows of the two factored halves of X stacked
+// (rows [0, n) of the top half, then of the bottom half starting at row h),
+// with the strictly lower parts of their first n columns (the reflector
+// storage) zeroed: T = [R_top c_top; R_bot c_bot].
+__global__ void tsqr_stack_kernel(const double* __restrict__ X, int64_t ld, int64_t h, int64_t n, int64_t nc,
+                                  double* __restrict__ Tm) {
+    const int64_t rows = 2 * n;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < rows * nc;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = idx % rows, j = idx / rows;
+        const int64_t li = i < n ? i : i - n;
+        const int64_t src = (i < n ? i : h + li) + j * ld;
+        Tm[i + j * rows] = (j < n && li > j) ? 0.0 : X[src];
+    }
+}
+
+bool qr_ff_tsqr_supported(const Ctx& ctx, int64_t m, int64_t n, int64_t nc) {
+    const int64_t h = (m + 1) / 2;
+    return n >= 1 && m - h >= n && qr_ff_supported(ctx, h, n, nc) && qr_ff_supported(ctx, 2 * n, n, nc);
+}
+
+// Two-level TSQR in float-float for sketches whose rows do not fit the
+// shared memory of one factorization: QR of each row half, then QR of their
+// stacked R blocks (with the carried columns n..nc-1).  The first n rows of X
+// receive R and (Q^T X)[:n, n:nc], the same contract as householder_qr_ff;
+// the rows below n are not meaningful afterwards.
+void householder_qr_ff_tsqr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld) {
+    if (!qr_ff_tsqr_supported(ctx, m, n, nc)) fail(RNLA_ERR_UNSUPPORTED, "float-float TSQR: shape not supported");
+    const int64_t h = (m + 1) / 2;
+    householder_qr_ff(ctx, X, h, n, nc, ld);
+    householder_qr_ff(ctx, X + h, m - h, n, nc, ld);
+    DevBuf<double> Tm((size_t)2 * n * nc, ctx.stream);
+    {
+        int g = (int)div_up(2 * n * nc, 256);
+        if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+        tsqr_stack_kernel<<<g, 256, 0, ctx.stream>>>(X, ld, h, n, nc, Tm);
+        RNLA_LAUNCH_CHECK();
+    }
+    householder_qr_ff(ctx, Tm, 2 * n, n, nc, 2 * n);
+    copy_matrix(ctx, n, nc, Tm, 2 * n, X, ld);
+}
+
 bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi) {
     using namespace qrff;
     if (n <= 0) return true;

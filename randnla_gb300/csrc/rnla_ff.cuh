@@ -199,6 +199,19 @@ __device__ __forceinline__ void ff2_madd(f32x2 ah, f32x2 al, f32x2 bh, f32x2 nbh
     sl = add2(sl, add2(t, c));
 }
 
+// (sh, sl) += a (bh + bl) on both lanes for an exact FP32 pair a (a value
+// with no low part): ff2_madd without the al bh term, 11 instructions.
+__device__ __forceinline__ void ff2_madd_x(f32x2 a, f32x2 bh, f32x2 nbh, f32x2 bl, f32x2& sh, f32x2& sl) {
+    const f32x2 np = mul2(a, nbh);                         // -p, p = a bh
+    const f32x2 e = fma2(a, bh, np);                       // a bh - p, exact
+    const f32x2 c = fma2(a, bl, e);
+    const f32x2 s = sub2(sh, np);                          // sh + p
+    const f32x2 bp = sub2(s, sh);
+    const f32x2 t = sub2(sub2(sh, sub2(s, bp)), add2(np, bp));
+    sh = s;
+    sl = add2(sl, add2(t, c));
+}
+
 // (h, l) += (oh, ol) on both lanes (see ff_acc)
 __device__ __forceinline__ void ff2_acc(f32x2& h, f32x2& l, f32x2 oh, f32x2 ol) {
     const f32x2 s = add2(h, oh);

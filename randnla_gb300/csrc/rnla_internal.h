@@ -46,6 +46,11 @@ void householder_form_q(Ctx& ctx, const double* V, int64_t m, int64_t n, int64_t
 // fit in shared memory.
 bool qr_ff_supported(const Ctx& ctx, int64_t m, int64_t n, int64_t nc);
 void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld);
+// The same for sketches too tall for one factorization: two row halves, then
+// their stacked R blocks (two-level TSQR); only the first n rows of X are
+// meaningful afterwards.
+bool qr_ff_tsqr_supported(const Ctx& ctx, int64_t m, int64_t n, int64_t nc);
+void householder_qr_ff_tsqr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64_t ld);
 // Float-float R^-1 (qr_ff.cu); false on an exactly zero pivot (synchronises).
 bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Rinv, int64_t ldi);
 // Rinv (n x n, upper) = R^-1; returns false on an exactly zero pivot (synchronises).
@@ -126,6 +131,7 @@ int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int
 struct LsqrFFInput {
     DevBuf<float2> AF, bF;
     const void* A = nullptr;
+    bool f32 = false;               // AF holds FP32 rows (A stored in FP32)
     int64_t m = 0, n = 0, ldf = 0;
     cudaEvent_t ready = nullptr;
     cudaStream_t owner = nullptr;   // stream the buffers are freed on
@@ -142,6 +148,9 @@ struct LsqrFFInput {
     }
 };
 bool lsqr_ff_supported(int64_t n);
+// M (n x n upper) <- the FP64 value of its float-float split, so that the
+// float-float LSQR operator A M and a later FP64 product M z use the same M.
+void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm);
 void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
                      LsqrFFInput& in);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
@@ -203,6 +212,24 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
                      const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN);
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
+// ---- split-bf16 tensor-core GEMM (gemm_bfx.cu) ----
+// An operand as bf16 planes (X = X_0 + X_1 + ..., each the bf16 rounding of
+// the remainder) in K-major SWIZZLE_128B tiles of TR rows x 64 K.
+struct BfxPlanes {
+    DevBuf<uint8_t> buf;
+    int64_t R = 0, K = 0;
+    int TR = 0, planes = 0, tiles = 0, Ks = 0;
+};
+// Tile height an operand image needs: 128 on the X (M) side; on the Y (N)
+// side 96 for level 2 and 64 for level 3.
+int bfx_tile_rows(int level, bool x_side);
+// Element (r, k) of the operand (R x K) is src[r sr + k sk] (FP32 or FP64).
+void bfx_planes(Ctx& ctx, BfxPlanes& P, const void* src, bool f32, int64_t R, int64_t K, int64_t sr, int64_t sk,
+                int TR, int planes);
+// C (X.R x Y.R, FP64, ldc) = X^T Y keeping the plane pairs p + q < level
+// (2 or 3); trans stores C^T instead (C[j + i ldc]).
+void bfx_gemm(Ctx& ctx, int level, const BfxPlanes& X, const BfxPlanes& Y, double* C, int64_t ldc, bool trans);
+
 // C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.
 void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                 int64_t NN, int64_t ldy, int dx, int dy, double* C, int64_t ldc);

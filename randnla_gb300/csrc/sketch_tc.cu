@@ -48,6 +48,7 @@
 // records an error, drains its own bulk copies and MMAs, frees TMEM and exits.
 #include "rnla_internal.h"
 #include "rnla_async.cuh"
+#include "rnla_tc.cuh"
 #include <cuda_bf16.h>
 #include <vector>
 #include <algorithm>
@@ -70,58 +71,6 @@ constexpr int S_BYTES = BM * BK * 2;                 // 16 KB sketch tile
 constexpr int ROW_BYTES = BK * 2;                    // 128
 constexpr int YD_BYTES = BN * ROW_BYTES;             // one digit tile, 8 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;
-
-__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
-    d |= (uint64_t)1 << 16;                              // leading byte offset (unused for SW128 K-major)
-    d |= (uint64_t)(1024u >> 4) << 32;                   // stride byte offset
-    d |= (uint64_t)1 << 46;                              // descriptor version for tcgen05
-    d |= (uint64_t)2 << 61;                              // SWIZZLE_128B
-    return d;
-}
-
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128, N = BN.
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accum) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accum)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-          "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                   "=r"(r[7])
-                 : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // acc += (integer value of the FP32 word f) * 2^sh, exact in int64 (sh < 31)
 __device__ __forceinline__ void acc_digit(long long& acc, uint32_t f, int sh) {
@@ -562,8 +511,10 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     constexpr int WIN_MAX = 32000;
     const int sm = ctx.sm_count;
     const int64_t tiles = (int64_t)tiles_m * tiles_n;
-    // with a feed, each column tile is its own launch as its columns arrive
-    const int64_t tiles_launch = feed ? (int64_t)tiles_m : tiles;
+    // with a feed and a small S, each column tile is its own launch as its
+    // columns arrive (below)
+    const bool per_tile = feed && (double)tiles_m * Ks * S_BYTES * tiles_n <= 4.0e9;
+    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : tiles;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -634,11 +585,23 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
         RNLA_LAUNCH_CHECK();
     } else {
+        // Each column tile's digit planes are made as soon as its columns
+        // have landed.  The MMA runs per column tile too (overlapping the
+        // rest of the upload) while re-reading S once per tile stays cheap;
+        // when S is large (every tile re-reads all of it from HBM) one MMA
+        // launch after the last tile keeps S reads to about one.
         for (int jt = 0; jt < tiles_n; ++jt) {
             feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
             digits(jt, 1);
+            if (!per_tile) continue;
             if (jt == 0) stream_wait(ctx.stream, side);
             prm.jt_only = jt;
+            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+            RNLA_LAUNCH_CHECK();
+        }
+        if (!per_tile) {
+            stream_wait(ctx.stream, side);
+            prm.jt_only = -1;
             kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
             RNLA_LAUNCH_CHECK();
         }
@@ -677,9 +640,19 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
     }
 }
 
-void tc_gemm_tn(Ctx&, const double*, int64_t, int64_t, int64_t, const double*, int64_t, int64_t, int,
-                int, double*, int64_t) {
-    fail(RNLA_ERR_UNSUPPORTED, "two-sided digit-sliced GEMM is not built; use RNLA_PREC_FP64");
+// C = X^T Y on the split-bf16 tensor-core GEMM (gemm_bfx.cu): the level is
+// the larger plane count requested (1 = plain bf16; default 3, which holds
+// FP32 data exactly), at most 3.
+void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y, int64_t NN,
+                int64_t ldy, int dx, int dy, double* C, int64_t ldc) {
+    if (K <= 0 || MM <= 0 || NN <= 0) return;
+    int level = std::max(dx, dy);
+    if (level <= 0) level = 3;
+    if (level > 3) level = 3;
+    BfxPlanes px, py;
+    bfx_planes(ctx, px, X, false, MM, K, ldx, 1, bfx_tile_rows(level, true), level);
+    bfx_planes(ctx, py, Y, false, NN, K, ldy, 1, bfx_tile_rows(level, false), level);
+    bfx_gemm(ctx, level, px, py, C, ldc, false);
 }
 
 }  // namespace rnla

@@ -111,3 +111,27 @@ def test_bf16x_host_and_device_entries_agree(rnla):
     std = rnla.blendenpik_dev(At, bt, xt, 1e-12, 2000, 4.0, o)
     assert sth["iterations"] == std["iterations"]
     np.testing.assert_array_equal(np.ravel(xh), xt.cpu().numpy())
+
+
+@pytest.mark.parametrize("m,n,kappa", [(5000, 1, 1.0), (9000, 77, 1e6), (12000, 200, 1e6), (20000, 511, 1e4),
+                                       (40000, 1024, 1e6)])
+def test_bf16x_lsqr_fp32_storage(rnla, m, n, kappa):
+    """A stored in FP32: the LSQR streams a row-major FP32 copy (4 bytes per
+    element; kernel variants with 1, 2, 4 and 8 column chunks per lane)."""
+    import torch
+    A, b = _problem(m, n, kappa, 1e-6)
+    A32 = A.astype(np.float32)
+    A64 = A32.astype(np.float64)
+    At = torch.from_numpy(A32).cuda().t().contiguous().t()
+    bt = torch.from_numpy(b).cuda()
+    xt = torch.zeros(n, dtype=torch.float64, device="cuda")
+    st = rnla.blendenpik_dev(At, bt, xt, 1e-12, 2000, 4.0, _fast(rnla))
+    x = xt.cpu().numpy()
+    xl = np.linalg.lstsq(A64, b, rcond=None)[0]
+    assert abs(_relres(A64, x, b) - _relres(A64, xl, b)) < 1e-10
+    # backward error against its floor 2^-48 ||b|| / ||r|| for a float-float iterate
+    r = b - A64 @ x
+    be = np.linalg.norm(A64.T @ r) / (np.linalg.norm(A64) * np.linalg.norm(r))
+    assert be <= 1e3 * 2.0 ** -48 * np.linalg.norm(b) / np.linalg.norm(r), be
+    assert st["precision_used"] == int(rnla.Precision.BF16X)
+    assert 0 < st["iterations"] < 500

@@ -113,20 +113,77 @@ def test_rand_svd_randnla_fp64(rnla):
     assert rel.max() < 0.03 and rel[0] < 1e-6
 
 
-def test_tensor_core_precision_is_refused_where_not_built(rnla):
-    """rand_svd's products A^T Q and Q^T A would need a two-sided tensor-core
-    GEMM, which is not built: both the driver and the GEMM entry say so
-    instead of computing something else."""
+def test_rand_svd_randnla_tensor_core_vs_oracle(rnla):
+    """The tensor-core (BF16X) range finder on the oracle's FP64 pipeline with
+    the same Omega: the top-k singular values within 1e-6 relative, the
+    approximation error ||A - U S Vt||_F and U's orthonormality at the level
+    of the split-bf16 products (~1e-7)."""
+    sig = 10.0 ** (-np.arange(1000) / 100.0)
+    A = O.make_lowrank_test_matrix(2000, 1000, sig, 1, 2)
+    o = rnla.options(precision=rnla.Precision.BF16X, mode=rnla.Mode.RandNLA, power_iters=2, seed=42)
+    U, S, Vt, st = rnla.rand_svd(A, 50, 1e-6, 10, o, return_stats=True)
+    Uo, so, Vto = O.rand_svd_randnla(A, 50, 10, 2, seed=42)
+    s = np.diag(S)
+    assert np.max(np.abs(s - so) / so) < 1e-6
+    assert np.allclose(U.T @ U, np.eye(50), atol=1e-6)
+    assert np.allclose(Vt @ Vt.T, np.eye(50), atol=1e-6)
+    err = np.linalg.norm(A - U @ S @ Vt)
+    err_o = np.linalg.norm(A - (Uo * so) @ Vto)
+    assert abs(err - err_o) <= 1e-6 * err_o
+    assert st["precision_used"] == int(rnla.Precision.BF16X)
+
+
+def test_rand_svd_randnla_tensor_core_fp32_storage(rnla):
+    """A stored in FP32 (read by the plane builder directly, no FP64 copy)."""
     import torch
-    A = np.random.default_rng(6).standard_normal((200, 100))
-    o = rnla.options(precision=rnla.Precision.BF16X, mode=rnla.Mode.RandNLA)
-    with pytest.raises(rnla.Unsupported):
-        rnla.rand_svd(A, 10, 1e-6, 5, o)
-    x = torch.randn((64, 16), dtype=torch.float64, device="cuda").t().contiguous().t()
-    y = torch.randn((64, 8), dtype=torch.float64, device="cuda").t().contiguous().t()
-    c = torch.zeros((16, 8), dtype=torch.float64, device="cuda").t().contiguous().t()
-    with pytest.raises(rnla.Unsupported):
-        rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X)
-    rnla.gemm_tn_dev(x, y, c)                       # FP64 is the built path
-    torch.cuda.synchronize()
-    assert torch.allclose(c, x.t() @ y, rtol=1e-12, atol=1e-12)
+    rng = np.random.default_rng(8)
+    m, n, k, p = 3000, 1500, 64, 16
+    sig = np.exp(-np.arange(n) / 16.0)
+    A = O.make_lowrank_test_matrix(m, n, sig, 3, 4).astype(np.float32)
+    A64 = A.astype(np.float64)
+    At = torch.from_numpy(A).cuda().t().contiguous().t()
+    l = k + p
+    U = torch.zeros((l, m), dtype=torch.float64, device="cuda").t()
+    sg = torch.zeros(l, dtype=torch.float64, device="cuda")
+    Vt = torch.zeros((n, l), dtype=torch.float64, device="cuda").t()
+    o = rnla.options(precision=rnla.Precision.BF16X, mode=rnla.Mode.RandNLA, power_iters=2, seed=5)
+    r, _ = rnla.rand_svd_dev(At, k, 1e-6, p, U, sg, Vt, o)
+    assert r == k
+    _, so, _ = O.rand_svd_randnla(A64, k, p, 2, seed=5)
+    s = sg[:k].cpu().numpy()
+    assert np.max(np.abs(s - so) / so) < 1e-6
+    del rng
+
+
+@pytest.mark.parametrize("K,MM,NN", [(5000, 300, 200), (700, 130, 97), (64, 16, 8)])
+def test_gemm_tn_split_bf16_levels(rnla, K, MM, NN):
+    """rnla_gemm_tn_dev on the tensor cores: level 1 (plain bf16), 2 and 3
+    planes (the digits arguments) against the FP64 product."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(K + MM)
+    x = torch.randn((MM, K), generator=g, dtype=torch.float64, device="cuda").t()
+    y = torch.randn((NN, K), generator=g, dtype=torch.float64, device="cuda").t()
+    ref = x.t() @ y
+    scale = (x.abs().t() @ y.abs()).max().item()
+    for level, bound in ((1, 2e-2), (2, 2e-4), (3, 2e-6)):
+        c = torch.full((NN, MM), float("nan"), dtype=torch.float64, device="cuda").t()
+        rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X, digits_x=level, digits_y=level)
+        torch.cuda.synchronize()
+        err = (c - ref).abs().max().item() / scale
+        assert err < bound, (level, err)
+
+
+def test_gemm_tn_split_bf16_exact_on_small_integers(rnla):
+    """Integers |v| <= 16 are exact in bf16 and the sums stay below 2^24, so
+    every level returns the exact product."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(3)
+    K, MM, NN = 3000, 150, 100
+    x = torch.randint(-16, 17, (MM, K), generator=g, device="cuda").double().t()
+    y = torch.randint(-16, 17, (NN, K), generator=g, device="cuda").double().t()
+    ref = x.t() @ y
+    for level in (1, 2, 3):
+        c = torch.zeros((NN, MM), dtype=torch.float64, device="cuda").t()
+        rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X, digits_x=level, digits_y=level)
+        torch.cuda.synchronize()
+        assert torch.equal(c, ref), level

@@ -84,7 +84,8 @@ def test_float32_data_default_digits(rnla):
     C = _tc(Y, d, seed=4)
     ref = _quantized_sketch(d, m, 4) @ Y.double()
     err = (C - ref).abs().max().item() / ref.abs().max().item()
-    assert err < 1e-7, err
+    # FP32 data default to 3 digits: 24 bits below each column's maximum
+    assert err < 1e-6, err
 
 
 @pytest.mark.parametrize("digits,bound", [(1, 2e-2), (2, 4e-4), (3, 4e-6), (4, 1e-9)])
