@@ -69,8 +69,9 @@ SVD_WORKLOADS = {
 # GB written); per row and pass the kernel moves 8 ldf + 16 bytes.
 LSQR_DRAM_BYTES_PER_ROW_PASS = (5.819774e9 + 0.0375055e9) / (36 * 40000)
 LSQR_NCU_ALGO_BYTES_PER_ROW_PASS = 8 * 500 + 16
-# the same ratio for FP32 rows (None until an ncu capture of that layout is recorded)
-LSQR_F32_DRAM_RATIO = None
+# the same ratio for FP32 rows: one ncu capture at 131072 x 1024 (31 passes: 16.9706 GB
+# read + 0.0752 GB written)
+LSQR_F32_DRAM_RATIO = (16.970577e9 + 0.075243e9) / (31 * (4 * 1024 + 16) * 131072)
 
 
 def parse(argv=None):

@@ -341,10 +341,10 @@ static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_
 // the Grams and the triangular products on the split-bf16 tensor-core GEMM
 // at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP64; the
 // FP64 Householder basis when a Cholesky pivot fails.  Returns 1 on fallback.
-static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l) {
+static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int passes = 2) {
     if (m < l) return orthonormalize(ctx, Y, m, l, m, true), 1;
     DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), T((size_t)m * l, ctx.stream);
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass < passes; ++pass) {
         {
             BfxPlanes ya, yb;
             bfx_planes(ctx, ya, Y, false, l, m, m, 1, bfx_tile_rows(3, true), 3);     // columns of Y
@@ -402,17 +402,48 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
             bfx_planes(ctx, zp, Z, false, l, n, n, 1, bfx_tile_rows(LP, false), LP);
             bfx_gemm(ctx, LP, arow, zp, Y, m, false);                                // Y = A Z
         }
-        fallbacks += orthonormalize_bfx(ctx, Y, m, l);
+        if (it + 1 < o.power_iters) fallbacks += orthonormalize_bfx(ctx, Y, m, l);
     }
+    // one split-bf16 CholeskyQR pass brings kappa(Y) to ~1 (the float-float
+    // R below then does not amplify the FP32-level error of Y^T A)
+    if (o.power_iters >= 1) fallbacks += orthonormalize_bfx(ctx, Y, m, l, 1);
     tm.mark();
-    DevBuf<double> B((size_t)l * n, ctx.stream);
+    // Projection.  Y is orthonormal only to the split-bf16 level (its Grams
+    // accumulate in FP32 over K = m); Q = Y R^-1 with R = chol(Y^T Y) formed
+    // in float-float is orthonormal to ~1e-14, and B = Q^T A = R^-T (Y^T A)
+    // needs no explicit Q: Y^T A on the tensor cores at level 3, R^-T applied
+    // in float-float.
+    DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), Bt((size_t)l * n, ctx.stream),
+        B((size_t)l * n, ctx.stream);
+    gram_ff(ctx, Y, m, l, Y, m, l, m, G, l);
+    if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
+        // Y lost rank: the FP64 Householder basis and the plain projection
+        fallbacks += orthonormalize(ctx, Y, m, l, m, true);
+        fill_identity(ctx, l, l, Ri, l);
+    }
     {
-        BfxPlanes qp;
-        bfx_planes(ctx, qp, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
-        bfx_gemm(ctx, 3, acol, qp, B, l, true);                                      // B = Q^T A (as (A^T Q)^T)
+        BfxPlanes yp;
+        bfx_planes(ctx, yp, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
+        bfx_gemm(ctx, 3, acol, yp, Bt, l, true);                                     // Y^T A (l x n)
     }
+    gram_ff(ctx, Ri, l, l, Bt, l, n, l, B, l);                                       // B = R^-T (Y^T A)
     tm.mark();
-    return svd_finish(ctx, RNLA_PREC_FP64, Y, m, l, B, n, k, U, ldu, sig, Vt, ldvt);
+    // small SVD of B; U = Y (R^-1 U_B)
+    const int64_t r = k < l ? k : l;
+    DevBuf<double> UB((size_t)l * l, ctx.stream), sg(l, ctx.stream), VB((size_t)n * l, ctx.stream);
+    if (!small_svd_gram(ctx, B, l, n, l, UB, l, sg, VB, n)) small_svd(ctx, B, l, n, l, UB, l, sg, VB, n);
+    {
+        DevBuf<double> RiT((size_t)l * l, ctx.stream), W2((size_t)l * r, ctx.stream);
+        transpose(ctx, l, l, Ri, l, RiT, l);
+        gram_ff(ctx, RiT, l, l, UB, l, r, l, W2, l);                                 // R^-1 U_B[:, :r]
+        BfxPlanes yr, wp;
+        bfx_planes(ctx, yr, Y, false, m, l, 1, m, bfx_tile_rows(3, true), 3);        // rows of Y
+        bfx_planes(ctx, wp, W2, false, r, l, l, 1, bfx_tile_rows(3, false), 3);      // columns of W2
+        bfx_gemm(ctx, 3, yr, wp, U, ldu, false);
+    }
+    RNLA_CUDA(cudaMemcpyAsync(sig, sg.get(), r * sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
+    transpose(ctx, n, r, VB, n, Vt, ldvt);
+    return r;
 }
 
 static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda,

@@ -473,10 +473,59 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(double* __restrict__ G, 
     }
 }
 
+// The same right-looking Cholesky over a cooperative grid: CTA c owns the
+// columns j = c, c + G, ...; step k updates G[i][j] -= G[k][i] G[k][j] / G[k][k]
+// (k < i <= j) in the owned columns with the unscaled pivot row, which no
+// one writes during the step; a bounded grid barrier ends each step.  The
+// rows are scaled by 1 / sqrt(G[k][k]) at the end.  Every CTA reads the same
+// pivot, so a non-positive one ends all of them at the same step.
+__global__ void __launch_bounds__(256) cholesky_coop_kernel(double* __restrict__ G, int64_t n, int64_t ld,
+                                                            unsigned int* status, GridBarrier bar) {
+    for (int64_t k = 0; k < n; ++k) {
+        const double d = *((volatile double*)&G[k + k * ld]);
+        if (!(d > 0.0)) {
+            if (threadIdx.x == 0) atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);
+            return;
+        }
+        const double inv = 1.0 / d;
+        for (int64_t j = k + 1 + blockIdx.x; j < n; j += gridDim.x) {
+            const double gkj = G[k + j * ld] * inv;
+            for (int64_t i = k + 1 + threadIdx.x; i <= j; i += blockDim.x)
+                G[i + j * ld] = fma(-G[k + i * ld], gkj, G[i + j * ld]);
+        }
+        if (!grid_sync(bar)) return;
+    }
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+    // scale row i by 1 / sqrt(G[i][i]) (diagonal last, in its own pass)
+    for (int64_t e = gt; e < n * n; e += gs) {
+        const int64_t i = e % n, j = e / n;
+        if (i < j) G[i + j * ld] /= sqrt(G[i + i * ld]);
+        else if (i > j) G[i + j * ld] = 0.0;
+    }
+    if (!grid_sync(bar)) return;
+    for (int64_t i = gt; i < n; i += gs) G[i + i * ld] = sqrt(G[i + i * ld]);
+}
+
 bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld) {
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
-    cholesky_kernel<<<1, 1024, 0, ctx.stream>>>(G, n, ld, ctx.status);
-    RNLA_LAUNCH_CHECK();
+    if (n >= 128) {
+        // one barrier per column beats a single CTA's FP64 throughput
+        int nb = 0;
+        RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, cholesky_coop_kernel, 256, 0));
+        int Gs = ctx.sm_count;
+        if (Gs > nb * ctx.sm_count) Gs = nb * ctx.sm_count;
+        if (Gs > n) Gs = (int)n;
+        DevBuf<unsigned int> bw(2, ctx.stream);
+        RNLA_CUDA(cudaMemsetAsync(bw.get(), 0, 2 * sizeof(unsigned int), ctx.stream));
+        GridBarrier bar{bw.get(), bw.get() + 1, ctx.status};
+        void* args[] = {&G, &n, &ld, &ctx.status, &bar};
+        RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_coop_kernel, dim3((unsigned)Gs), dim3(256), args,
+                                              0, ctx.stream));
+        count_launch();
+    } else {
+        cholesky_kernel<<<1, 1024, 0, ctx.stream>>>(G, n, ld, ctx.status);
+        RNLA_LAUNCH_CHECK();
+    }
     unsigned int h = 0;
     RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -670,6 +719,75 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(double* __restrict__ W, do
     }
 }
 
+// The same one-sided Jacobi spread over a cooperative grid: in each round
+// of the circle-method tournament the s/2 disjoint column pairs go one per
+// CTA (256 threads reduce the three dot products over the s rows and apply
+// the rotation to W and V), and a bounded grid barrier separates rounds.
+// Same rotation formulae and tolerance as jacobi_kernel; a sweep without a
+// rotation ends the iteration (all CTAs read the same counter).
+__global__ void __launch_bounds__(256) jacobi_coop_kernel(double* __restrict__ W, double* __restrict__ V, int s,
+                                                          int max_sweeps, unsigned int* __restrict__ rot,
+                                                          GridBarrier bar) {
+    __shared__ double red[3][8];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int sp = (s + 1) & ~1;
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        for (int round = 0; round < sp - 1; ++round) {
+            for (int pr = blockIdx.x; pr < sp / 2; pr += gridDim.x) {
+                int a, b;
+                if (pr == 0) { a = 0; b = 1 + (round % (sp - 1)); }
+                else {
+                    a = 1 + ((round + pr) % (sp - 1));
+                    b = 1 + ((round + sp - 1 - pr) % (sp - 1));
+                }
+                if (a >= s || b >= s) continue;          // the bye of an odd s (uniform over the CTA)
+                if (a > b) { const int t = a; a = b; b = t; }
+                double* wa = W + (int64_t)a * s;
+                double* wb = W + (int64_t)b * s;
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int i = tid; i < s; i += blockDim.x) {
+                    const double x = wa[i], y = wb[i];
+                    al = fma(x, x, al);
+                    be = fma(y, y, be);
+                    ga = fma(x, y, ga);
+                }
+                al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+                if (lane == 0) { red[0][wid] = al; red[1][wid] = be; red[2][wid] = ga; }
+                __syncthreads();
+                al = 0.0; be = 0.0; ga = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { al += red[0][w]; be += red[1][w]; ga += red[2][w]; }
+                __syncthreads();
+                if (ga == 0.0 || fabs(ga) <= tol * sqrt(al * be)) continue;
+                const double zeta = (be - al) / (2.0 * ga);
+                const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
+                const double c = 1.0 / sqrt(fma(t, t, 1.0));
+                const double sn = c * t;
+                for (int i = tid; i < s; i += blockDim.x) {
+                    const double x = wa[i], y = wb[i];
+                    wa[i] = c * x - sn * y;
+                    wb[i] = sn * x + c * y;
+                }
+                double* va = V + (int64_t)a * s;
+                double* vb = V + (int64_t)b * s;
+                for (int i = tid; i < s; i += blockDim.x) {
+                    const double x = va[i], y = vb[i];
+                    va[i] = c * x - sn * y;
+                    vb[i] = sn * x + c * y;
+                }
+                if (tid == 0) atomicAdd(&rot[sweep & 1], 1u);
+            }
+            if (!grid_sync(bar)) return;
+        }
+        // every CTA reads this sweep's count after the last round's barrier;
+        // the other slot is cleared for the next sweep before anyone uses it
+        const unsigned int n_rot = *((volatile unsigned int*)&rot[sweep & 1]);
+        if (blockIdx.x == 0 && tid == 0) rot[(sweep + 1) & 1] = 0u;
+        if (!grid_sync(bar)) return;
+        if (n_rot == 0u) break;
+    }
+}
+
 // sigma_i = ||W_i||, descending order; U_R = W_i / sigma_i (zero columns
 // completed with the first coordinate vectors orthogonal to the others);
 // V columns permuted alike.  One CTA.
@@ -749,6 +867,89 @@ __global__ void triu_copy_kernel(const double* __restrict__ src, int64_t lds, in
     }
 }
 
+// One-sided Jacobi of W (s x s) with the rotations accumulated into V: one
+// CTA for small s, the cooperative grid version from s = 64 on.
+void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s) {
+    if (s < 64) {
+        jacobi_kernel<<<1, 1024, 0, ctx.stream>>>(W, V, (int)s, 60);
+        RNLA_LAUNCH_CHECK();
+        return;
+    }
+    int nb = 0;
+    RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, jacobi_coop_kernel, 256, 0));
+    int G = (int)((s + 1) / 2);
+    if (G > nb * ctx.sm_count) G = nb * ctx.sm_count;
+    if (G > ctx.sm_count) G = ctx.sm_count;
+    DevBuf<unsigned int> words(4, ctx.stream);       // rotation counts [2], barrier count, generation
+    RNLA_CUDA(cudaMemsetAsync(words.get(), 0, 4 * sizeof(unsigned int), ctx.stream));
+    ctx.clear_status();
+    GridBarrier bar{words.get() + 2, words.get() + 3, ctx.status};
+    int si = (int)s, sweeps = 60;
+    unsigned int* rot = words.get();
+    void* args[] = {&W, &V, &si, &sweeps, &rot, &bar};
+    RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel, dim3((unsigned)G), dim3(256), args, 0,
+                                          ctx.stream));
+    count_launch();
+    ctx.check_status("Jacobi SVD");
+}
+
+// V[:, j] /= sigma_j (rows q, columns p)
+__global__ void scale_columns_inv_kernel(int64_t q, int64_t p, double* __restrict__ V, int64_t ldv,
+                                         const double* __restrict__ sigma) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < q * p; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % q, j = e / q;
+        V[i + j * ldv] /= sigma[j];
+    }
+}
+static void scale_columns_inv(Ctx& ctx, int64_t q, int64_t p, double* V, int64_t ldv, const double* sigma) {
+    int g = div_up(q * p, 256);
+    if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
+    scale_columns_inv_kernel<<<g, 256, 0, ctx.stream>>>(q, p, V, ldv, sigma);
+    RNLA_LAUNCH_CHECK();
+}
+
+// SVD of a wide B (p x q, p <= q) from R = chol(B B^T): the Gram is formed
+// in float-float (gram_ff), R's right singular vectors (one-sided Jacobi on
+// R) are B's left ones U_B, the column norms its singular values, and
+// V_B = B^T U_B Sigma^-1 (float-float product).  Squaring B loses accuracy
+// in the small singular values (relative error ~ 2^-48 (sigma_1 / sigma_i)^2),
+// so this returns false -- and writes nothing the caller keeps -- when the
+// Cholesky fails or sigma_p / sigma_1 < 1e-5; the caller then takes
+// small_svd.  Synchronises once (to read the two extreme sigmas).
+bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
+                    double* sigma, double* V, int64_t ldv) {
+    if (p <= 0 || p > q) return false;
+    DevBuf<double> Bt((size_t)q * p, ctx.stream), G((size_t)p * p, ctx.stream);
+    transpose(ctx, p, q, B, ldb, Bt, q);
+    gram_ff(ctx, Bt, q, p, Bt, q, p, q, G, p);                 // B B^T
+    if (!cholesky_upper(ctx, G, p, p)) return false;
+    DevBuf<double> W((size_t)p * p, ctx.stream), VR((size_t)p * p, ctx.stream), UR((size_t)p * p, ctx.stream),
+        VS((size_t)p * p, ctx.stream), sg(p, ctx.stream);
+    DevBuf<int> order(p, ctx.stream);
+    int g = div_up(p * p, 256);
+    if (g > 1024) g = 1024;
+    triu_copy_kernel<<<g, 256, 0, ctx.stream>>>(G, p, p, W);
+    RNLA_LAUNCH_CHECK();
+    fill_identity(ctx, p, p, VR, p);
+    jacobi_sweeps(ctx, W, VR, p);
+    const size_t smem = (size_t)p * sizeof(double);
+    if (smem > 48 * 1024)
+        RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, VR, (int)p, UR, VS, sg, order);
+    RNLA_LAUNCH_CHECK();
+    double ext[2];
+    RNLA_CUDA(cudaMemcpyAsync(&ext[0], sg.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaMemcpyAsync(&ext[1], sg.get() + p - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (!(ext[0] > 0.0) || !(ext[1] >= 1e-5 * ext[0])) return false;
+    // U_B = VS (R = UR Sigma VS^T, B B^T = VS Sigma^2 VS^T); V_B = B^T VS Sigma^-1
+    copy_matrix(ctx, p, p, VS, p, U, ldu);
+    RNLA_CUDA(cudaMemcpyAsync(sigma, sg.get(), p * sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
+    gram_ff(ctx, B, ldb, q, VS, p, p, p, V, ldv);
+    scale_columns_inv(ctx, q, p, V, ldv, sg);
+    return true;
+}
+
 void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
                double* sigma, double* V, int64_t ldv) {
     const int64_t s = p < q ? p : q;
@@ -767,8 +968,7 @@ void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, dou
     RNLA_LAUNCH_CHECK();
     fill_identity(ctx, s, s, VR, s);
     // R VR = W with orthogonal columns -> R = UR diag(sigma) VR^T
-    jacobi_kernel<<<1, 1024, 0, ctx.stream>>>(W, VR, (int)s, 60);
-    RNLA_LAUNCH_CHECK();
+    jacobi_sweeps(ctx, W, VR, s);
     DevBuf<double> UR((size_t)s * s, ctx.stream), VS((size_t)s * s, ctx.stream);
     DevBuf<int> order(s, ctx.stream);
     const size_t smem = (size_t)s * sizeof(double);

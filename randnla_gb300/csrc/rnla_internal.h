@@ -71,6 +71,14 @@ void full_piv_lu_l(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx,
 // Thin SVD of B (p x q): U (p x t), sigma (t), V (q x t), t = min(p, q),
 // singular values descending; exactly-zero singular directions get the
 // first unused coordinate vectors (so SVD(0) = (I, 0, I)).
+// One-sided Jacobi of W (s x s), rotations accumulated into V (one CTA for
+// s < 64, a cooperative grid above).
+void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s);
+// SVD of a wide B (p <= q) through chol(B B^T) with a float-float Gram:
+// U_B (p x p), sigma (p), V_B (q x p).  Returns false (caller uses
+// small_svd) when the Cholesky fails or sigma_p / sigma_1 < 1e-5.
+bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
+                    double* sigma, double* V, int64_t ldv);
 void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U,
                int64_t ldu, double* sigma, double* V, int64_t ldv);
 
@@ -212,6 +220,12 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
                      const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN);
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
+// ---- float-float tall-skinny products (gram_ff.cu) ----
+// C (N1 x N2, FP64, ldc) = X^T Y for column-major FP64 X (K x N1, ldx) and
+// Y (K x N2, ldy), accumulated in float-float (~48 bits) on the FP32 pipe.
+void gram_ff(Ctx& ctx, const double* X, int64_t ldx, int64_t N1, const double* Y, int64_t ldy, int64_t N2,
+             int64_t K, double* C, int64_t ldc);
+
 // ---- split-bf16 tensor-core GEMM (gemm_bfx.cu) ----
 // An operand as bf16 planes (X = X_0 + X_1 + ..., each the bf16 rounding of
 // the remainder) in K-major SWIZZLE_128B tiles of TR rows x 64 K.
