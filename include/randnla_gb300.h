@@ -447,7 +447,10 @@ RNLA_API int rnla_sketch_apply_ex_dev(const void* x_dev, int32_t x_is_f32, int64
  * RNLA_PREC_FP64 on the FP64 CUDA cores; RNLA_PREC_BF16X on the split-bf16
  * tcgen05 GEMM, each operand cut into max(digits_x, digits_y) bf16 planes
  * (1..3, default 3) and the plane pairs p + q < planes accumulated in FP32
- * (3 planes: ~24 significant bits per operand); RNLA_PREC_BF16 = one plane. */
+ * (3 planes: ~24 significant bits per operand); RNLA_PREC_BF16 = one plane;
+ * 4 or more digits select exact integer digit products (X in five 6-bit
+ * digits and Y in four 8-bit digits below each column's maximum, 1024-term
+ * windows exact in FP32 and folded into int64). */
 RNLA_API int rnla_gemm_tn_dev(const double* x_dev, int64_t k, int64_t mm, int64_t ldx, const double* y_dev,
                      int64_t nn, int64_t ldy, int32_t precision, int32_t digits_x,
                      int32_t digits_y, double* c_dev, int64_t ldc, void* stream);

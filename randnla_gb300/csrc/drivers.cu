@@ -339,8 +339,9 @@ static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_
 
 // Orthonormal basis of Y (m x l, ld m, m >= l) in place: CholeskyQR2 with
 // the Grams and the triangular products on the split-bf16 tensor-core GEMM
-// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP64; the
-// FP64 Householder basis when a Cholesky pivot fails.  Returns 1 on fallback.
+// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP32 (FP64
+// if that fails); the FP64 Householder basis when a Cholesky pivot fails.
+// Returns 1 on fallback.
 static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int passes = 2) {
     if (m < l) return orthonormalize(ctx, Y, m, l, m, true), 1;
     DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), T((size_t)m * l, ctx.stream);
@@ -351,7 +352,10 @@ static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int pas
             bfx_planes(ctx, yb, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
             bfx_gemm(ctx, 3, ya, yb, G, l, false);                                    // G = Y^T Y
         }
-        if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
+        // the Gram is FP32-accurate, so R^-1 in FP32 is enough; FP64 when the
+        // FP32 Cholesky fails, Householder when that fails too
+        if (!cholesky_inverse_f32(ctx, G, l, l, Ri, l) &&
+            (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l))) {
             orthonormalize(ctx, Y, m, l, m, true);
             return 1;
         }
@@ -369,10 +373,10 @@ static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int pas
 // The RandNLA-mode range finder and projection on the tensor cores
 // (lora_helpers.rs:17-44 with a Gaussian Omega and q power iterations):
 // Y = A Omega, q times {Z = orth(A^T Y), Y = orth(A Z)}, B = Q^T A, then the
-// FP64 small-SVD finish of lora_drivers.rs:51-68.  A is read as bf16 planes
-// made once: its rows at level 2 for the A Z products and its columns with
-// three planes (A^T Y at level 2, B = Q^T A at level 3, which holds FP32
-// data exactly).  Omega is the FP64 Gaussian of the FP64 path (same key).
+// small-SVD finish of lora_drivers.rs:51-68.  A is read as bf16 planes made
+// once (its rows for the A Z products, its columns for A^T Y, level 2); the
+// projection B = Q^T A is an exact digit product (tc_exact_tn).  Omega is
+// the FP64 Gaussian of the FP64 path (same key).
 static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda, int64_t k,
                             int64_t l, const rnla_options& o, double* U, int64_t ldu, double* sig, double* Vt,
                             int64_t ldvt, int& fallbacks, StageTimer& tm) {
@@ -380,7 +384,7 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     const RngKey key = key_of(&o.rng);
     BfxPlanes arow, acol;
     bfx_planes(ctx, arow, Av, a_f32, m, n, 1, lda, bfx_tile_rows(LP, true), LP);   // A(i, k) = A[i + k lda]
-    bfx_planes(ctx, acol, Av, a_f32, n, m, lda, 1, bfx_tile_rows(3, true), 3);    // A^T(i, k) = A[k + i lda]
+    bfx_planes(ctx, acol, Av, a_f32, n, m, lda, 1, bfx_tile_rows(LP, true), LP);  // A^T(i, k) = A[k + i lda]
     DevBuf<double> Y((size_t)m * l, ctx.stream), Z((size_t)n * l, ctx.stream);
     {
         DevBuf<double> Om((size_t)n * l, ctx.stream);
@@ -421,11 +425,10 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         fallbacks += orthonormalize(ctx, Y, m, l, m, true);
         fill_identity(ctx, l, l, Ri, l);
     }
-    {
-        BfxPlanes yp;
-        bfx_planes(ctx, yp, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
-        bfx_gemm(ctx, 3, acol, yp, Bt, l, true);                                     // Y^T A (l x n)
-    }
+    // Y^T A (l x n) exactly on the tensor cores (integer digits, int64
+    // windows): an FP32-accumulated product would leave B with errors of
+    // ~1e-5 relative to sigma_k at K = 65536
+    tc_exact_tn(ctx, Av, a_f32, m, n, lda, Y, l, m, Bt, l, true, 4);
     gram_ff(ctx, Ri, l, l, Bt, l, n, l, B, l);                                       // B = R^-T (Y^T A)
     tm.mark();
     // small SVD of B; U = Y (R^-1 U_B)

@@ -66,6 +66,7 @@ struct Args {
     const float2* AF;           // row-major copy of A, m rows of rowq 16-byte chunks
     int64_t m, n, ldf, hp;      // hp = ldf / 2 column pairs
     int64_t rowq;               // 16-byte chunks per row: hp (float-float rows) or ldf / 4 (FP32 rows)
+    int nparts;                 // rows of partF: one per CTA, or one per warp (FP32-row passes)
     int R;                      // rows per tile (multiple of 8)
     int ST;                     // ring stages
     int64_t ntiles;
@@ -636,7 +637,7 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
     const int hp = (int)a.hp;
     const int hq = (int)a.rowq;
     const int64_t ntl = rg.ntl;
-    f32x2 yh[KP], nyh[KP], yl[KP];
+    f32x2 yh[KP], yl[KP];
 #pragma unroll
     for (int kk = 0; kk < KC; ++kk) {
         const int c = lane + 32 * kk;
@@ -645,7 +646,6 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
             float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
             if (dot && c < hq) { y0 = a.yF[4 * c + 2 * h]; y1 = a.yF[4 * c + 2 * h + 1]; }
             yh[2 * kk + h] = pk2(y0.x, y1.x);
-            nyh[2 * kk + h] = pk2(-y0.x, -y1.x);
             yl[2 * kk + h] = pk2(y0.y, y1.y);
         }
     }
@@ -706,8 +706,8 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
             for (int kk = 0; kk < KC; ++kk) {
 #pragma unroll
                 for (int w = 0; w < RW; ++w) {
-                    ff2_madd_x(v[w][kk].x, yh[2 * kk], nyh[2 * kk], yl[2 * kk], sh[w][0], sl[w][0]);
-                    ff2_madd_x(v[w][kk].y, yh[2 * kk + 1], nyh[2 * kk + 1], yl[2 * kk + 1], sh[w][1], sl[w][1]);
+                    ff2_madd_xp(v[w][kk].x, yh[2 * kk], yl[2 * kk], sh[w][0], sl[w][0]);
+                    ff2_madd_xp(v[w][kk].y, yh[2 * kk + 1], yl[2 * kk + 1], sh[w][1], sl[w][1]);
                 }
             }
 #pragma unroll
@@ -753,21 +753,20 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
             }
         }
         if (acc_at) {
-            f32x2 uh[RW], nuh[RW], ul[RW];
+            f32x2 uh[RW], ul[RW];
 #pragma unroll
             for (int w = 0; w < RW; ++w) {
                 const float x = __shfl_sync(0xffffffffu, nv.x, w << SHL);
                 const float y = __shfl_sync(0xffffffffu, nv.y, w << SHL);
                 uh[w] = pk2(x, x);
-                nuh[w] = pk2(-x, -x);
                 ul[w] = pk2(y, y);
             }
 #pragma unroll
             for (int kk = 0; kk < KC; ++kk) {
 #pragma unroll
                 for (int w = 0; w < RW; ++w) {
-                    ff2_madd_x(v[w][kk].x, uh[w], nuh[w], ul[w], ah[2 * kk], al[2 * kk]);
-                    ff2_madd_x(v[w][kk].y, uh[w], nuh[w], ul[w], ah[2 * kk + 1], al[2 * kk + 1]);
+                    ff2_madd_xp(v[w][kk].x, uh[w], ul[w], ah[2 * kk], al[2 * kk]);
+                    ff2_madd_xp(v[w][kk].y, uh[w], ul[w], ah[2 * kk + 1], al[2 * kk + 1]);
                 }
             }
         }
@@ -776,6 +775,9 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
     const float2 b2 = ff_warp_sum(b2h, b2l);
     if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
     if (acc_at) {
+        // each warp's column sums go straight to its own row of partF (no
+        // shared-memory scratch: the ring gets that space)
+        float4* P4 = reinterpret_cast<float4*>(a.partF) + ((size_t)blockIdx.x * WF + warp) * hp;
 #pragma unroll
         for (int kk = 0; kk < KC; ++kk) {
             const int c = lane + 32 * kk;
@@ -783,26 +785,13 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const float2 H = upk2(ah[2 * kk + h]), L = upk2(al[2 * kk + h]);
-                    scratch[(size_t)warp * hp + 2 * c + h] = make_float4(H.x, L.x, H.y, L.y);
+                    const float2 c0 = ff_norm(H.x, L.x), c1v = ff_norm(H.y, L.y);
+                    P4[2 * c + h] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
                 }
             }
         }
     }
     __syncthreads();
-    if (acc_at) {
-        float4* P4 = reinterpret_cast<float4*>(a.partF) + (size_t)blockIdx.x * hp;
-        for (int p = tid; p < hp; p += TF) {
-            float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
-#pragma unroll
-            for (int w = 0; w < WF; ++w) {
-                const float4 q = scratch[(size_t)w * hp + p];
-                ff_acc(h0, l0, q.x, q.y);
-                ff_acc(h1, l1, q.z, q.w);
-            }
-            const float2 c0 = ff_norm(h0, l0), c1v = ff_norm(h1, l1);
-            P4[p] = make_float4(c0.x, c0.y, c1v.x, c1v.y);
-        }
-    }
     if (tid == 0) {
         float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
         for (int w = 0; w < WF; ++w) {
@@ -826,12 +815,13 @@ __device__ __forceinline__ float2 sum_slot(const Args& a, int slot, int lane) {
     return ff_warp_sum(h, l);
 }
 
-// g_j = sum over CTAs of partF[c][j]; one warp per column, warps 1..nwc-1.
+// g_j = sum over the nparts rows of partF[c][j] (one per CTA, or per warp);
+// one warp per column, warps 1..nwc-1.
 __device__ void reduce_columns(const Args& a, int warp, int lane, int nwc) {
     const int64_t nw = (int64_t)gridDim.x * (nwc - 1);
     for (int64_t j = (int64_t)blockIdx.x * (nwc - 1) + (warp - 1); j < a.n; j += nw) {
         float h = 0.f, l = 0.f;
-        for (int64_t c = lane; c < gridDim.x; c += 32) {
+        for (int64_t c = lane; c < a.nparts; c += 32) {
             const float2 v = a.partF[c * a.ldf + j];
             ff_acc(h, l, v.x, v.y);
         }
@@ -1381,13 +1371,13 @@ static KernelPick pick_kernel(int64_t hp) {
     return {kernel_kp<16, 1, false>(), WA * 1, T, false};
 }
 // FP32 rows: hq 16-byte chunks (4 columns each) per row, KC = KP / 2 chunks
-// per lane, fused roles throughout (n <= 1024: 8 chunks per lane, one row
+// per lane, fused roles throughout (n <= 1024: 8 chunks per lane, two rows
 // per warp).
 static KernelPick pick_kernel_f32(int64_t hq) {
     if (hq <= 32) return {kernel_kp<2, 8, true, true>(), WF * 8, TF, true};
     if (hq <= 64) return {kernel_kp<4, 4, true, true>(), WF * 4, TF, true};
-    if (hq <= 128) return {kernel_kp<8, 2, true, true>(), WF * 2, TF, true};
-    return {kernel_kp<16, 1, true, true>(), WF * 1, TF, true};
+    if (hq <= 128) return {kernel_kp<8, 4, true, true>(), WF * 4, TF, true};
+    return {kernel_kp<16, 2, true, true>(), WF * 2, TF, true};
 }
 
 }  // namespace lsff
@@ -1452,8 +1442,9 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
     const void* k = kp.fn;
     const int R = kp.R;
     const size_t stage = (size_t)R * rowq * 16;
-    // fused: per-warp column scratch; split: the two u hand-off buffers
-    const size_t extra = kp.fused ? (size_t)WF * hp * 16 : (size_t)2 * R * 16;
+    // fused: per-warp column scratch (none for FP32 rows, whose warps write
+    // partF directly); split: the two u hand-off buffers
+    const size_t extra = a_f32 ? 0 : kp.fused ? (size_t)WF * hp * 16 : (size_t)2 * R * 16;
     int STn = (int)(RING_BYTES / stage);
     STn = STn > MAX_ST ? MAX_ST : STn;
     const size_t smem_cap = 224 * 1024;            // dynamic shared memory per CTA (static use is < 2 KB)
@@ -1486,7 +1477,8 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
     uF.alloc(m, st);
     yF.alloc(ldf, st);
     gF.alloc(n, st); vF.alloc(n, st); wF.alloc(n, st); xF.alloc(n, st); vunF.alloc(n, st); varF.alloc(n, st);
-    partF.alloc((size_t)G * ldf, st);
+    const int nparts = a_f32 ? G * WF : G;
+    partF.alloc((size_t)nparts * ldf, st);
     spF.alloc((size_t)G * 4, st);
     colsq.alloc(n, st);
     out.alloc(8, st);
@@ -1512,7 +1504,7 @@ LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t
         RNLA_LAUNCH_CHECK();
         a.x0F = x0F.get();
     }
-    a.AF = AF; a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.rowq = rowq; a.R = R; a.ST = STn;
+    a.AF = AF; a.m = m; a.n = n; a.ldf = ldf; a.hp = hp; a.rowq = rowq; a.nparts = nparts; a.R = R; a.ST = STn;
     a.ntiles = div_up(m, R);
     a.bF = bF;
     a.uF = uF.get(); a.yF = yF.get(); a.gF = gF.get(); a.vF = vF.get(); a.wF = wF.get(); a.xF = xF.get();

@@ -212,6 +212,20 @@ __device__ __forceinline__ void ff2_madd_x(f32x2 a, f32x2 bh, f32x2 nbh, f32x2 b
     sl = add2(sl, add2(t, c));
 }
 
+// The same with -bh formed on the fly (one integer sign flip instead of a
+// register pair holding -bh).
+__device__ __forceinline__ void ff2_madd_xp(f32x2 a, f32x2 bh, f32x2 bl, f32x2& sh, f32x2& sl) {
+    const f32x2 p = mul2(a, bh);
+    const f32x2 np = neg2(p);
+    const f32x2 e = fma2(a, bh, np);                       // a bh - p, exact
+    const f32x2 c = fma2(a, bl, e);
+    const f32x2 s = add2(sh, p);                           // sh + p
+    const f32x2 bp = sub2(s, sh);
+    const f32x2 t = add2(sub2(sh, sub2(s, bp)), sub2(p, bp));
+    sh = s;
+    sl = add2(sl, add2(t, c));
+}
+
 // (h, l) += (oh, ol) on both lanes (see ff_acc)
 __device__ __forceinline__ void ff2_acc(f32x2& h, f32x2& l, f32x2 oh, f32x2 ol) {
     const f32x2 s = add2(h, oh);

@@ -61,6 +61,9 @@ void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, co
 // Cholesky G = R^T R (upper R written to the upper triangle of G, n x n);
 // returns false if a pivot is not positive (synchronises).
 bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld);
+// Ri = R^-1 for G = R^T R in FP32 arithmetic (one CTA, n <= 320); false on a
+// non-positive pivot or a larger n.  For Grams that are FP32-accurate anyway.
+bool cholesky_inverse_f32(Ctx& ctx, const double* G, int64_t n, int64_t ldg, double* Ri, int64_t ldr);
 // Thin orthonormal basis of Y (m x n, m >= n) in place: CholeskyQR2, with a
 // Householder fallback when a Cholesky pivot fails.  Returns 1 if the
 // fallback was taken.
@@ -244,6 +247,11 @@ void bfx_planes(Ctx& ctx, BfxPlanes& P, const void* src, bool f32, int64_t R, in
 // (2 or 3); trans stores C^T instead (C[j + i ldc]).
 void bfx_gemm(Ctx& ctx, int level, const BfxPlanes& X, const BfxPlanes& Y, double* C, int64_t ldc, bool trans);
 
+// C (MM x NN, FP64; C^T into ldc when trans) = X^T Y with exact tensor-core
+// products: X (K x MM, FP32 or FP64) in xd signed 6-bit digits below each
+// column's maximum, Y (K x NN, FP64) in four 8-bit digits (sketch_tc.cu).
+void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int64_t ldx, const double* Y,
+                 int64_t NN, int64_t ldy, double* C, int64_t ldc, bool trans, int xd = 4);
 // C (MM x NN) = X^T Y, X (K x MM), Y (K x NN), all double.
 void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                 int64_t NN, int64_t ldy, int dx, int dy, double* C, int64_t ldc);

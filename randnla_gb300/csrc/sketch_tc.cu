@@ -32,7 +32,8 @@
 //                      (m tile, n tile, K chunk) u = blockIdx.x, + gridDim.x,
 //                      ...; 192 threads: warp 0 streams the S tile and the P
 //                      digit tiles of each stage with cp.async.bulk into a
-//                      4-stage mbarrier ring that runs on across units;
+//                      4-stage (P = 4) or 5-stage (P <= 3) mbarrier ring that
+//                      runs on across units;
 //                      warp 1 allocates TMEM and issues tcgen05.mma
 //                      (M = 128, N = 64 P, K = 16, bf16 x bf16 -> f32: the
 //                      P digit tiles are one operand, so digit p accumulates
@@ -64,7 +65,9 @@ constexpr int BK = 64;            // K per pipeline stage (one 128-byte bf16 row
 constexpr int WIN = 16;           // stages per exact window (1024 K values)
 constexpr int MAXP = 4;           // digits
 constexpr int ACC_COLS = MAXP * BN;                  // TMEM columns of one accumulator set
-constexpr int STAGES = 4;
+// ring depth: as many 16 KB + P x 8 KB stages as fit in ~200 KB (4 for P = 4,
+// 5 for P <= 3), the operand stream from L2 being latency-bound
+__host__ __device__ constexpr int stages_for(int P) { return P >= 4 ? 4 : 5; }
 constexpr int DRAIN_WARPS = 4;
 constexpr int THREADS = 64 + 32 * DRAIN_WARPS;       // loader warp + MMA warp + drain warps
 constexpr int S_BYTES = BM * BK * 2;                 // 16 KB sketch tile
@@ -161,6 +164,7 @@ __device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
 
 template <int P>
 __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm) {
+    constexpr int STAGES = stages_for(P);
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sS = smem;                                           // STAGES x 16 KB
@@ -492,6 +496,7 @@ __global__ void splitk_sum_kernel(const long long* __restrict__ part, int kc_cou
 
 template <int P>
 static size_t smem_bytes() {
+    constexpr int STAGES = stages_for(P);
     return 1024 + (size_t)STAGES * S_BYTES + (size_t)STAGES * P * YD_BYTES + 512;
 }
 
@@ -615,7 +620,181 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     ctx.check_status("tensor-core sketch");
 }
 
+// ---------------------------------------------------------------------------
+// Exact X^T Y for two data operands on the same MMA kernel: X's columns cut
+// into signed 6-bit digits below each column's exponent play the sketch
+// (integers |t| <= 64, exact in bf16), Y's columns the 8-bit digit planes.
+// ---------------------------------------------------------------------------
+
+// One thread per (column j of X, 8 consecutive k): digit `dig` of ND (most
+// significant first) of T = round(|x| 2^(6 ND - E_j)) as the sketch-tile
+// image row j % 128 of tile [j / 128][stage].
+template <typename T>
+__global__ void sdigit_kernel(const T* __restrict__ X, int64_t K, int64_t N, int64_t ldx, const int* __restrict__ E,
+                              int ND, int dig, int Ks, int tiles, uint8_t* __restrict__ out) {
+    const int64_t chunks_per_col = (int64_t)Ks * 8;
+    const int64_t total = chunks_per_col * (int64_t)tiles * BM;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t j = u / chunks_per_col;
+        const int64_t cc = u % chunks_per_col;
+        const int st = (int)(cc >> 3), c8 = (int)(cc & 7);
+        const int it = (int)(j / BM), r = (int)(j % BM);
+        const int Ej = (j < N) ? E[j] : 0;
+        uint16_t dg[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int64_t k = (int64_t)st * BK + c8 * 8 + t;
+            uint64_t M = 0;
+            int e2 = 0;
+            bool neg = false;
+            if (j < N && k < K) {
+                const T x = X[k + j * ldx];
+                mant_exp(x, M, e2);
+                neg = (sizeof(T) == 8) ? (__double_as_longlong((double)x) < 0) : ((__float_as_uint((float)x) >> 31) != 0);
+            }
+            uint64_t Tq = 0;
+            if (M) {
+                const int sh = Ej - 6 * ND - e2;
+                if (sh <= 0) Tq = M << (-sh);
+                else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
+            }
+            const uint32_t d = (dig == 0) ? (uint32_t)(Tq >> (6 * (ND - 1))) : (uint32_t)((Tq >> (6 * (ND - 1 - dig))) & 63u);
+            dg[t] = digit_bf16(d, neg);
+        }
+        uint4 v;
+        v.x = dg[0] | ((uint32_t)dg[1] << 16);
+        v.y = dg[2] | ((uint32_t)dg[3] << 16);
+        v.z = dg[4] | ((uint32_t)dg[5] << 16);
+        v.w = dg[6] | ((uint32_t)dg[7] << 16);
+        uint8_t* tile = out + ((size_t)it * Ks + st) * S_BYTES;
+        *(uint4*)(tile + r * ROW_BYTES + ((c8 ^ (r & 7)) << 4)) = v;
+    }
+}
+
+// C (+)= 2^(Ex_r + Ey_c - shift) * sum over kc of the partials (row r of the
+// product = column r of X, column c = column c of Y); C^T when trans.
+__global__ void exact_tn_sum_kernel(const long long* __restrict__ part, int kc_count, int tiles_m, int tiles_n,
+                                    int64_t M, int64_t N, const int* __restrict__ Ex, const int* __restrict__ Ey,
+                                    int shift, int exact_sum, int accumulate, int trans, double* __restrict__ C,
+                                    int64_t ldc) {
+    const size_t tile_elems = (size_t)BM * BN;
+    const size_t kc_stride = (size_t)tiles_m * tiles_n * tile_elems;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < M * N; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e % M, j = e / M;
+        const size_t off = (size_t)((i / BM) + (int64_t)tiles_m * (j / BN)) * tile_elems + (size_t)(j % BN) * BM + (i % BM);
+        double sum;
+        if (exact_sum) {
+            long long t = 0;
+            for (int k = 0; k < kc_count; ++k) t += part[k * kc_stride + off];
+            sum = (double)t;
+        } else {
+            sum = 0.0;
+            for (int k = 0; k < kc_count; ++k) sum += (double)part[k * kc_stride + off];
+        }
+        const double v = ldexp(sum, Ex[i] + Ey[j] - shift);
+        double* dst = trans ? &C[j + i * ldc] : &C[i + j * ldc];
+        *dst = accumulate ? *dst + v : v;
+    }
+}
+
 }  // namespace tc
+
+// C (MM x NN, FP64) = X^T Y, X (K x MM, FP32 or FP64) and Y (K x NN, FP64)
+// column-major, with exact tensor-core products: Y is cut into 4 planes of
+// 8-bit digits below each column's maximum (32 bits), X into xd digits of 6
+// bits (24 bits for xd = 4: FP32 data to their own precision below each
+// column's maximum); each X digit is one launch of the sketch MMA kernel
+// whose 1024-K windows are exact in FP32 and folded into int64, so the only
+// roundings are the two digit truncations and the final FP64 sums over the
+// xd launches.  The X digit images are built one digit at a time into one
+// buffer (tiles_m x Ks x 16 KB).
+void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int64_t ldx, const double* Y,
+                 int64_t NN, int64_t ldy, double* C, int64_t ldc, bool trans, int xd) {
+    using namespace tc;
+    constexpr int P = 4;
+    if (K <= 0 || MM <= 0 || NN <= 0) return;
+    if (xd < 1 || xd > 5) fail(RNLA_ERR_INVALID_PARAMETERS, "exact X^T Y: 1..5 digits of X");
+    const int tiles_m = div_up(MM, BM), tiles_n = div_up(NN, BN);
+    const int Ks = div_up(K, BK);
+    const int wins = div_up(Ks, WIN);
+    const int sm = ctx.sm_count;
+    const int64_t tiles = (int64_t)tiles_m * tiles_n;
+    constexpr int WIN_MAX = 32000;
+    int best_kc = div_up(wins, WIN_MAX);
+    double best_cost = 1e300;
+    for (int kcn = div_up(wins, WIN_MAX); kcn <= Ks && kcn <= 64; ++kcn) {
+        const int spk_n = div_up(Ks, kcn);
+        const int kc_eff = div_up(Ks, spk_n);
+        const int64_t units = tiles * kc_eff;
+        const int64_t rounds = (units + sm - 1) / sm;
+        const double cost = (double)rounds * spk_n * (0.09 * P) + (double)units * 0.02;
+        if (cost < best_cost - 1e-9) { best_cost = cost; best_kc = kc_eff; }
+    }
+    const int spk = div_up(Ks, best_kc);
+    const int kc_count = div_up(Ks, spk);
+    const int64_t units = tiles * kc_count;
+    DevBuf<int> Ex((size_t)tiles_m * BM, ctx.stream), Ey((size_t)tiles_n * BN, ctx.stream);
+    exp_init_kernel<<<(unsigned)div_up((int64_t)tiles_m * BM, 256), 256, 0, ctx.stream>>>(Ex, (int64_t)tiles_m * BM);
+    RNLA_LAUNCH_CHECK();
+    exp_init_kernel<<<(unsigned)div_up((int64_t)tiles_n * BN, 256), 256, 0, ctx.stream>>>(Ey, (int64_t)tiles_n * BN);
+    RNLA_LAUNCH_CHECK();
+    const int64_t rpb = 4096;
+    if (x_f32)
+        colexp_kernel<float><<<dim3((unsigned)div_up(K, rpb), (unsigned)MM), 256, 0, ctx.stream>>>(
+            static_cast<const float*>(X), K, MM, ldx, nullptr, Ex, 0, rpb);
+    else
+        colexp_kernel<double><<<dim3((unsigned)div_up(K, rpb), (unsigned)MM), 256, 0, ctx.stream>>>(
+            static_cast<const double*>(X), K, MM, ldx, nullptr, Ex, 0, rpb);
+    RNLA_LAUNCH_CHECK();
+    colexp_kernel<double><<<dim3((unsigned)div_up(K, rpb), (unsigned)NN), 256, 0, ctx.stream>>>(Y, K, NN, ldy, nullptr,
+                                                                                              Ey, 0, rpb);
+    RNLA_LAUNCH_CHECK();
+    DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * (YD_BYTES / 2), ctx.stream);
+    {
+        const int64_t su = (int64_t)Ks * 8 * tiles_n * BN;
+        int g = div_up(su, 256);
+        if (g > 32 * sm) g = 32 * sm;
+        slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>(Y, K, NN, ldy, nullptr, NN, Ey, Ks, 0, tiles_n, dig);
+        RNLA_LAUNCH_CHECK();
+    }
+    DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
+    DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
+    const size_t smem = smem_bytes<P>();
+    auto kfn = sketch_mma_kernel<P>;
+    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    Params prm;
+    prm.M = MM; prm.N = NN; prm.K = K;
+    prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
+    prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units; prm.jt_only = -1;
+    prm.sk = sk; prm.ydig = dig; prm.partial = part; prm.status = ctx.status;
+    ctx.clear_status();
+    const unsigned grid = (unsigned)(units < sm ? units : sm);
+    const int exact_sum = (int64_t)wins + kc_count <= WIN_MAX ? 1 : 0;
+    int gs = div_up(MM * NN, 256);
+    if (gs > 8 * sm) gs = 8 * sm;
+    for (int d = 0; d < xd; ++d) {
+        {
+            const int64_t su = (int64_t)Ks * 8 * tiles_m * BM;
+            int g = div_up(su, 256);
+            if (g > 32 * sm) g = 32 * sm;
+            if (x_f32)
+                sdigit_kernel<float><<<g, 256, 0, ctx.stream>>>(static_cast<const float*>(X), K, MM, ldx, Ex, xd, d, Ks,
+                                                                tiles_m, sk);
+            else
+                sdigit_kernel<double><<<g, 256, 0, ctx.stream>>>(static_cast<const double*>(X), K, MM, ldx, Ex, xd, d,
+                                                                 Ks, tiles_m, sk);
+            RNLA_LAUNCH_CHECK();
+        }
+        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+        RNLA_LAUNCH_CHECK();
+        count_launch();
+        exact_tn_sum_kernel<<<gs, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, MM, NN, Ex, Ey,
+                                                        8 * P + 6 * (d + 1), exact_sum, d > 0 ? 1 : 0, trans ? 1 : 0,
+                                                        C, ldc);
+        RNLA_LAUNCH_CHECK();
+    }
+    ctx.check_status("exact tensor-core X^T Y");
+}
 
 bool tc_available(Ctx& ctx) {
     int major = 0, minor = 0;
@@ -640,15 +819,20 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
     }
 }
 
-// C = X^T Y on the split-bf16 tensor-core GEMM (gemm_bfx.cu): the level is
-// the larger plane count requested (1 = plain bf16; default 3, which holds
-// FP32 data exactly), at most 3.
+// C = X^T Y on the tensor cores: the level is the larger digit count
+// requested -- 1..3 on the split-bf16 GEMM (gemm_bfx.cu; 1 = plain bf16,
+// default 3, which holds FP32 data exactly), 4 or more on the exact integer
+// digit products (tc_exact_tn).
 void tc_gemm_tn(Ctx& ctx, const double* X, int64_t K, int64_t MM, int64_t ldx, const double* Y, int64_t NN,
                 int64_t ldy, int dx, int dy, double* C, int64_t ldc) {
     if (K <= 0 || MM <= 0 || NN <= 0) return;
     int level = std::max(dx, dy);
     if (level <= 0) level = 3;
-    if (level > 3) level = 3;
+    if (level >= 4) {
+        // exact digit products (X in five 6-bit digits, Y in four 8-bit digits)
+        tc_exact_tn(ctx, X, false, K, MM, ldx, Y, NN, ldy, C, ldc, false, 5);
+        return;
+    }
     BfxPlanes px, py;
     bfx_planes(ctx, px, X, false, MM, K, ldx, 1, bfx_tile_rows(level, true), level);
     bfx_planes(ctx, py, Y, false, NN, K, ldy, 1, bfx_tile_rows(level, false), level);

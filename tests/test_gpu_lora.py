@@ -158,14 +158,15 @@ def test_rand_svd_randnla_tensor_core_fp32_storage(rnla):
 @pytest.mark.parametrize("K,MM,NN", [(5000, 300, 200), (700, 130, 97), (64, 16, 8)])
 def test_gemm_tn_split_bf16_levels(rnla, K, MM, NN):
     """rnla_gemm_tn_dev on the tensor cores: level 1 (plain bf16), 2 and 3
-    planes (the digits arguments) against the FP64 product."""
+    planes (the digits arguments) and 4 (exact integer digit products)
+    against the FP64 product."""
     import torch
     g = torch.Generator(device="cuda").manual_seed(K + MM)
     x = torch.randn((MM, K), generator=g, dtype=torch.float64, device="cuda").t()
     y = torch.randn((NN, K), generator=g, dtype=torch.float64, device="cuda").t()
     ref = x.t() @ y
     scale = (x.abs().t() @ y.abs()).max().item()
-    for level, bound in ((1, 2e-2), (2, 2e-4), (3, 2e-6)):
+    for level, bound in ((1, 2e-2), (2, 2e-4), (3, 2e-6), (4, 1e-8)):
         c = torch.full((NN, MM), float("nan"), dtype=torch.float64, device="cuda").t()
         rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X, digits_x=level, digits_y=level)
         torch.cuda.synchronize()
@@ -182,7 +183,7 @@ def test_gemm_tn_split_bf16_exact_on_small_integers(rnla):
     x = torch.randint(-16, 17, (MM, K), generator=g, device="cuda").double().t()
     y = torch.randint(-16, 17, (NN, K), generator=g, device="cuda").double().t()
     ref = x.t() @ y
-    for level in (1, 2, 3):
+    for level in (1, 2, 3, 4):
         c = torch.zeros((NN, MM), dtype=torch.float64, device="cuda").t()
         rnla.gemm_tn_dev(x, y, c, precision=rnla.Precision.BF16X, digits_x=level, digits_y=level)
         torch.cuda.synchronize()
