@@ -339,9 +339,9 @@ static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_
 
 // Orthonormal basis of Y (m x l, ld m, m >= l) in place: CholeskyQR2 with
 // the Grams and the triangular products on the split-bf16 tensor-core GEMM
-// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP32 (FP64
-// if that fails); the FP64 Householder basis when a Cholesky pivot fails.
-// Returns 1 on fallback.
+// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP64; the
+// FP64 Householder basis when a Cholesky pivot fails.  Returns 1 on
+// fallback.
 static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int passes = 2) {
     if (m < l) return orthonormalize(ctx, Y, m, l, m, true), 1;
     DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), T((size_t)m * l, ctx.stream);
@@ -352,10 +352,7 @@ static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int pas
             bfx_planes(ctx, yb, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
             bfx_gemm(ctx, 3, ya, yb, G, l, false);                                    // G = Y^T Y
         }
-        // the Gram is FP32-accurate, so R^-1 in FP32 is enough; FP64 when the
-        // FP32 Cholesky fails, Householder when that fails too
-        if (!cholesky_inverse_f32(ctx, G, l, l, Ri, l) &&
-            (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l))) {
+        if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
             orthonormalize(ctx, Y, m, l, m, true);
             return 1;
         }
@@ -393,24 +390,26 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         bfx_planes(ctx, op, Om, false, l, n, n, 1, bfx_tile_rows(LP, false), LP);
         bfx_gemm(ctx, LP, arow, op, Y, m, false);                                    // Y = A Omega
     }
-    fallbacks += orthonormalize_bfx(ctx, Y, m, l);
+    // between products the basis only has to stay well conditioned (its span
+    // is what the next product uses): one CholeskyQR pass; the projection
+    // below makes the final one orthonormal in float-float
+    fallbacks += orthonormalize_bfx(ctx, Y, m, l, 1);
     for (int it = 0; it < o.power_iters; ++it) {
         {
             BfxPlanes yp;
             bfx_planes(ctx, yp, Y, false, l, m, m, 1, bfx_tile_rows(LP, false), LP);
             bfx_gemm(ctx, LP, acol, yp, Z, n, false);                                // Z = A^T Q
         }
-        fallbacks += orthonormalize_bfx(ctx, Z, n, l);
+        fallbacks += orthonormalize_bfx(ctx, Z, n, l, 1);
         {
             BfxPlanes zp;
             bfx_planes(ctx, zp, Z, false, l, n, n, 1, bfx_tile_rows(LP, false), LP);
             bfx_gemm(ctx, LP, arow, zp, Y, m, false);                                // Y = A Z
         }
-        if (it + 1 < o.power_iters) fallbacks += orthonormalize_bfx(ctx, Y, m, l);
+        // one split-bf16 CholeskyQR pass also before the projection: it brings
+        // kappa(Y) to ~1, so the float-float R below does not amplify errors
+        fallbacks += orthonormalize_bfx(ctx, Y, m, l, 1);
     }
-    // one split-bf16 CholeskyQR pass brings kappa(Y) to ~1 (the float-float
-    // R below then does not amplify the FP32-level error of Y^T A)
-    if (o.power_iters >= 1) fallbacks += orthonormalize_bfx(ctx, Y, m, l, 1);
     tm.mark();
     // Projection.  Y is orthonormal only to the split-bf16 level (its Grams
     // accumulate in FP32 over K = m); Q = Y R^-1 with R = chol(Y^T Y) formed

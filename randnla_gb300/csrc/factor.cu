@@ -473,86 +473,6 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(double* __restrict__ G, 
     }
 }
 
-// R^-1 of the Cholesky factor of G (n x n, upper part read), in FP32, one
-// CTA with the packed upper triangle in shared memory (n <= CHOL_F32_MAX):
-// right-looking Cholesky, then column-by-column inversion in place (column
-// j of R^-1 from the finished columns < j and column j of R).  For the
-// CholeskyQR passes whose Grams are themselves only FP32-accurate (the
-// split-bf16 products); Ri (FP64, ld ldr) gets zeros below the diagonal.
-constexpr int CHOL_F32_MAX = 320;
-__device__ __forceinline__ int pk_idx(int i, int j) { return j * (j + 1) / 2 + i; }   // i <= j
-__global__ void __launch_bounds__(1024) chol_inv_f32_kernel(const double* __restrict__ G, int n, int64_t ldg,
-                                                            double* __restrict__ Ri, int64_t ldr,
-                                                            unsigned int* status) {
-    extern __shared__ float sm_f[];
-    float* P = sm_f;                                  // packed upper, n (n + 1) / 2
-    float* tmp = sm_f + n * (n + 1) / 2;              // n
-    __shared__ float rkk_s;
-    __shared__ int bad_s;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    if (tid == 0) bad_s = 0;
-    for (int e = tid; e < n * n; e += nt) {
-        const int i = e % n, j = e / n;
-        if (i <= j) P[pk_idx(i, j)] = (float)G[i + (int64_t)j * ldg];
-    }
-    for (int k = 0; k < n; ++k) {
-        __syncthreads();
-        if (tid == 0) {
-            const float d = P[pk_idx(k, k)];
-            if (!(d > 0.f)) {
-                bad_s = 1;
-                atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);
-            }
-            rkk_s = sqrtf(d);
-            P[pk_idx(k, k)] = rkk_s;
-        }
-        __syncthreads();
-        if (bad_s) return;
-        const float inv = 1.0f / rkk_s;
-        for (int j = k + 1 + tid; j < n; j += nt) P[pk_idx(k, j)] *= inv;
-        __syncthreads();
-        const int w = n - k - 1;
-        for (int e = tid; e < w * w; e += nt) {
-            const int ii = k + 1 + e % w, jj = k + 1 + e / w;
-            if (ii <= jj) P[pk_idx(ii, jj)] = fmaf(-P[pk_idx(k, ii)], P[pk_idx(k, jj)], P[pk_idx(ii, jj)]);
-        }
-    }
-    // X = R^-1 in place: x_jj = 1 / r_jj, x_ij = -(sum_{i <= q < j} x_iq r_qj) / r_jj
-    for (int j = 0; j < n; ++j) {
-        __syncthreads();
-        const float rjj = P[pk_idx(j, j)];
-        for (int i = tid; i < j; i += nt) {
-            float acc = 0.f;
-            for (int q = i; q < j; ++q) acc = fmaf(P[pk_idx(i, q)], P[pk_idx(q, j)], acc);
-            tmp[i] = -acc / rjj;
-        }
-        __syncthreads();
-        for (int i = tid; i < j; i += nt) P[pk_idx(i, j)] = tmp[i];
-        if (tid == 0) P[pk_idx(j, j)] = 1.0f / rjj;
-    }
-    __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
-        const int i = e % n, j = e / n;
-        Ri[i + (int64_t)j * ldr] = (i <= j) ? (double)P[pk_idx(i, j)] : 0.0;
-    }
-}
-
-// false when a pivot is not positive (or n is too large for the kernel)
-bool cholesky_inverse_f32(Ctx& ctx, const double* G, int64_t n, int64_t ldg, double* Ri, int64_t ldr) {
-    if (n <= 0) return true;
-    if (n > CHOL_F32_MAX) return false;
-    const size_t smem = ((size_t)n * (n + 1) / 2 + n) * sizeof(float);
-    RNLA_CUDA(cudaFuncSetAttribute(chol_inv_f32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
-    chol_inv_f32_kernel<<<1, 1024, smem, ctx.stream>>>(G, (int)n, ldg, Ri, ldr, ctx.status);
-    RNLA_LAUNCH_CHECK();
-    unsigned int h = 0;
-    RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
-    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
-    RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
-    return h == 0;
-}
-
 // The same right-looking Cholesky over a cooperative grid: CTA c owns the
 // columns j = c, c + G, ...; step k updates G[i][j] -= G[k][i] G[k][j] / G[k][k]
 // (k < i <= j) in the owned columns with the unscaled pivot row, which no
@@ -801,63 +721,70 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(double* __restrict__ W, do
 
 // The same one-sided Jacobi spread over a cooperative grid: in each round
 // of the circle-method tournament the s/2 disjoint column pairs go one per
-// warp across the grid (the lanes reduce the three dot products over the s
-// rows and apply the rotation to W and V), and a bounded grid barrier
-// separates rounds.  Same rotation formulae and tolerance as jacobi_kernel;
-// a sweep without a rotation ends the iteration (all CTAs read the same
-// counter).
+// CTA (256 threads reduce the three dot products over the s rows and apply
+// the rotation to W and V; short FP64 dependency chains per thread), and a
+// bounded grid barrier separates rounds.  Same rotation formulae and
+// tolerance as jacobi_kernel; a sweep without a rotation ends the iteration
+// (all CTAs read the same counter).  (A warp per pair measured slower: the
+// 64-cycle FP64 dependent latency over s / 32 rows per lane dominates.)
 __global__ void __launch_bounds__(256) jacobi_coop_kernel(double* __restrict__ W, double* __restrict__ V, int s,
                                                           int max_sweeps, unsigned int* __restrict__ rot,
                                                           GridBarrier bar) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ double red[3][8];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int sp = (s + 1) & ~1;
     const double tol = 1e-15;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         for (int round = 0; round < sp - 1; ++round) {
-            for (int pr = blockIdx.x * nw + wid; pr < sp / 2; pr += gridDim.x * nw) {
+            for (int pr = blockIdx.x; pr < sp / 2; pr += gridDim.x) {
                 int a, b;
                 if (pr == 0) { a = 0; b = 1 + (round % (sp - 1)); }
                 else {
                     a = 1 + ((round + pr) % (sp - 1));
                     b = 1 + ((round + sp - 1 - pr) % (sp - 1));
                 }
-                if (a >= s || b >= s) continue;          // the bye of an odd s (uniform over the warp)
+                if (a >= s || b >= s) continue;          // the bye of an odd s (uniform over the CTA)
                 if (a > b) { const int t = a; a = b; b = t; }
                 double* wa = W + (int64_t)a * s;
                 double* wb = W + (int64_t)b * s;
                 double al = 0.0, be = 0.0, ga = 0.0;
-                for (int i = lane; i < s; i += 32) {
+                for (int i = tid; i < s; i += blockDim.x) {
                     const double x = wa[i], y = wb[i];
                     al = fma(x, x, al);
                     be = fma(y, y, be);
                     ga = fma(x, y, ga);
                 }
                 al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+                if (lane == 0) { red[0][wid] = al; red[1][wid] = be; red[2][wid] = ga; }
+                __syncthreads();
+                al = 0.0; be = 0.0; ga = 0.0;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { al += red[0][w]; be += red[1][w]; ga += red[2][w]; }
+                __syncthreads();
                 if (ga == 0.0 || fabs(ga) <= tol * sqrt(al * be)) continue;
                 const double zeta = (be - al) / (2.0 * ga);
                 const double t = copysign(1.0, zeta) / (fabs(zeta) + sqrt(fma(zeta, zeta, 1.0)));
                 const double c = 1.0 / sqrt(fma(t, t, 1.0));
                 const double sn = c * t;
-                for (int i = lane; i < s; i += 32) {
+                for (int i = tid; i < s; i += blockDim.x) {
                     const double x = wa[i], y = wb[i];
                     wa[i] = c * x - sn * y;
                     wb[i] = sn * x + c * y;
                 }
                 double* va = V + (int64_t)a * s;
                 double* vb = V + (int64_t)b * s;
-                for (int i = lane; i < s; i += 32) {
+                for (int i = tid; i < s; i += blockDim.x) {
                     const double x = va[i], y = vb[i];
                     va[i] = c * x - sn * y;
                     vb[i] = sn * x + c * y;
                 }
-                if (lane == 0) atomicAdd(&rot[sweep & 1], 1u);
+                if (tid == 0) atomicAdd(&rot[sweep & 1], 1u);
             }
             if (!grid_sync(bar)) return;
         }
         // every CTA reads this sweep's count after the last round's barrier;
         // the other slot is cleared for the next sweep before anyone uses it
         const unsigned int n_rot = *((volatile unsigned int*)&rot[sweep & 1]);
-        if (blockIdx.x == 0 && threadIdx.x == 0) rot[(sweep + 1) & 1] = 0u;
+        if (blockIdx.x == 0 && tid == 0) rot[(sweep + 1) & 1] = 0u;
         if (!grid_sync(bar)) return;
         if (n_rot == 0u) break;
     }
@@ -952,7 +879,7 @@ void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s) {
     }
     int nb = 0;
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, jacobi_coop_kernel, 256, 0));
-    int G = div_up((s + 1) / 2, 8);                  // a warp per column pair, 8 warps per CTA
+    int G = (int)((s + 1) / 2);                      // a CTA per column pair
     if (G > nb * ctx.sm_count) G = nb * ctx.sm_count;
     if (G > ctx.sm_count) G = ctx.sm_count;
     DevBuf<unsigned int> words(4, ctx.stream);       // rotation counts [2], barrier count, generation

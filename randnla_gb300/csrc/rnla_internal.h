@@ -61,9 +61,6 @@ void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, co
 // Cholesky G = R^T R (upper R written to the upper triangle of G, n x n);
 // returns false if a pivot is not positive (synchronises).
 bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld);
-// Ri = R^-1 for G = R^T R in FP32 arithmetic (one CTA, n <= 320); false on a
-// non-positive pivot or a larger n.  For Grams that are FP32-accurate anyway.
-bool cholesky_inverse_f32(Ctx& ctx, const double* G, int64_t n, int64_t ldg, double* Ri, int64_t ldr);
 // Thin orthonormal basis of Y (m x n, m >= n) in place: CholeskyQR2, with a
 // Householder fallback when a Cholesky pivot fails.  Returns 1 if the
 // fallback was taken.

@@ -391,7 +391,23 @@ __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int
     const int64_t k0 = (int64_t)blockIdx.x * rows_per_block;
     const int64_t k1 = min(K, k0 + rows_per_block);
     int best = -1074;
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
+    // eight independent loads in flight per thread (the loop is bound by
+    // memory latency, not by the exponent arithmetic)
+    constexpr int U = 8;
+    int64_t k = k0 + threadIdx.x;
+    for (; k + (U - 1) * (int64_t)blockDim.x < k1; k += U * (int64_t)blockDim.x) {
+        uint64_t M[U];
+        int e2[U];
+#pragma unroll
+        for (int q = 0; q < U; ++q) {
+            bool neg;
+            load_elem(Y, ldy, N, extra, k + q * (int64_t)blockDim.x, j, M[q], e2[q], neg);
+        }
+#pragma unroll
+        for (int q = 0; q < U; ++q)
+            if (M[q]) best = max(best, e2[q] + 64 - __clzll((long long)M[q]));
+    }
+    for (; k < k1; k += blockDim.x) {
         uint64_t M;
         int e2;
         bool neg;
@@ -626,12 +642,13 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
 // (integers |t| <= 64, exact in bf16), Y's columns the 8-bit digit planes.
 // ---------------------------------------------------------------------------
 
-// One thread per (column j of X, 8 consecutive k): digit `dig` of ND (most
-// significant first) of T = round(|x| 2^(6 ND - E_j)) as the sketch-tile
-// image row j % 128 of tile [j / 128][stage].
+// One thread per (column j of X, 8 consecutive k): the ND digits (most
+// significant first) of T = round(|x| 2^(6 ND - E_j)) as sketch-tile image
+// rows j % 128 of tiles [digit][j / 128][stage] (X is read once).
 template <typename T>
 __global__ void sdigit_kernel(const T* __restrict__ X, int64_t K, int64_t N, int64_t ldx, const int* __restrict__ E,
-                              int ND, int dig, int Ks, int tiles, uint8_t* __restrict__ out) {
+                              int ND, int Ks, int tiles, uint8_t* __restrict__ out) {
+    const size_t digit_stride = (size_t)tiles * Ks * S_BYTES;
     const int64_t chunks_per_col = (int64_t)Ks * 8;
     const int64_t total = chunks_per_col * (int64_t)tiles * BM;
     for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total; u += (int64_t)gridDim.x * blockDim.x) {
@@ -640,34 +657,43 @@ __global__ void sdigit_kernel(const T* __restrict__ X, int64_t K, int64_t N, int
         const int st = (int)(cc >> 3), c8 = (int)(cc & 7);
         const int it = (int)(j / BM), r = (int)(j % BM);
         const int Ej = (j < N) ? E[j] : 0;
-        uint16_t dg[8];
+        uint64_t Tq[8];
+        bool neg[8];
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             const int64_t k = (int64_t)st * BK + c8 * 8 + t;
             uint64_t M = 0;
             int e2 = 0;
-            bool neg = false;
+            neg[t] = false;
             if (j < N && k < K) {
                 const T x = X[k + j * ldx];
                 mant_exp(x, M, e2);
-                neg = (sizeof(T) == 8) ? (__double_as_longlong((double)x) < 0) : ((__float_as_uint((float)x) >> 31) != 0);
+                neg[t] = (sizeof(T) == 8) ? (__double_as_longlong((double)x) < 0)
+                                          : ((__float_as_uint((float)x) >> 31) != 0);
             }
-            uint64_t Tq = 0;
+            Tq[t] = 0;
             if (M) {
                 const int sh = Ej - 6 * ND - e2;
-                if (sh <= 0) Tq = M << (-sh);
-                else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
+                if (sh <= 0) Tq[t] = M << (-sh);
+                else if (sh < 64) Tq[t] = (M + (1ull << (sh - 1))) >> sh;
             }
-            const uint32_t d = (dig == 0) ? (uint32_t)(Tq >> (6 * (ND - 1))) : (uint32_t)((Tq >> (6 * (ND - 1 - dig))) & 63u);
-            dg[t] = digit_bf16(d, neg);
         }
-        uint4 v;
-        v.x = dg[0] | ((uint32_t)dg[1] << 16);
-        v.y = dg[2] | ((uint32_t)dg[3] << 16);
-        v.z = dg[4] | ((uint32_t)dg[5] << 16);
-        v.w = dg[6] | ((uint32_t)dg[7] << 16);
-        uint8_t* tile = out + ((size_t)it * Ks + st) * S_BYTES;
-        *(uint4*)(tile + r * ROW_BYTES + ((c8 ^ (r & 7)) << 4)) = v;
+        uint8_t* tile = out + ((size_t)it * Ks + st) * S_BYTES + r * ROW_BYTES + ((c8 ^ (r & 7)) << 4);
+        for (int dig = 0; dig < ND; ++dig) {
+            uint16_t dg[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const uint32_t d = (dig == 0) ? (uint32_t)(Tq[t] >> (6 * (ND - 1)))
+                                              : (uint32_t)((Tq[t] >> (6 * (ND - 1 - dig))) & 63u);
+                dg[t] = digit_bf16(d, neg[t]);
+            }
+            uint4 v;
+            v.x = dg[0] | ((uint32_t)dg[1] << 16);
+            v.y = dg[2] | ((uint32_t)dg[3] << 16);
+            v.z = dg[4] | ((uint32_t)dg[5] << 16);
+            v.w = dg[6] | ((uint32_t)dg[7] << 16);
+            *(uint4*)(tile + (size_t)dig * digit_stride) = v;
+        }
     }
 }
 
@@ -706,8 +732,8 @@ __global__ void exact_tn_sum_kernel(const long long* __restrict__ part, int kc_c
 // column's maximum); each X digit is one launch of the sketch MMA kernel
 // whose 1024-K windows are exact in FP32 and folded into int64, so the only
 // roundings are the two digit truncations and the final FP64 sums over the
-// xd launches.  The X digit images are built one digit at a time into one
-// buffer (tiles_m x Ks x 16 KB).
+// xd launches.  All X digit images are built in one pass over X
+// (xd x tiles_m x Ks x 16 KB).
 void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                  int64_t NN, int64_t ldy, double* C, int64_t ldc, bool trans, int xd) {
     using namespace tc;
@@ -757,7 +783,20 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
         slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>(Y, K, NN, ldy, nullptr, NN, Ey, Ks, 0, tiles_n, dig);
         RNLA_LAUNCH_CHECK();
     }
-    DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
+    const size_t digit_bytes = (size_t)tiles_m * Ks * S_BYTES;
+    DevBuf<uint8_t> sk(digit_bytes * xd, ctx.stream);
+    {
+        const int64_t su = (int64_t)Ks * 8 * tiles_m * BM;
+        int g = div_up(su, 256);
+        if (g > 32 * sm) g = 32 * sm;
+        if (x_f32)
+            sdigit_kernel<float><<<g, 256, 0, ctx.stream>>>(static_cast<const float*>(X), K, MM, ldx, Ex, xd, Ks, tiles_m,
+                                                            sk);
+        else
+            sdigit_kernel<double><<<g, 256, 0, ctx.stream>>>(static_cast<const double*>(X), K, MM, ldx, Ex, xd, Ks,
+                                                             tiles_m, sk);
+        RNLA_LAUNCH_CHECK();
+    }
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
     const size_t smem = smem_bytes<P>();
     auto kfn = sketch_mma_kernel<P>;
@@ -773,18 +812,7 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
     int gs = div_up(MM * NN, 256);
     if (gs > 8 * sm) gs = 8 * sm;
     for (int d = 0; d < xd; ++d) {
-        {
-            const int64_t su = (int64_t)Ks * 8 * tiles_m * BM;
-            int g = div_up(su, 256);
-            if (g > 32 * sm) g = 32 * sm;
-            if (x_f32)
-                sdigit_kernel<float><<<g, 256, 0, ctx.stream>>>(static_cast<const float*>(X), K, MM, ldx, Ex, xd, d, Ks,
-                                                                tiles_m, sk);
-            else
-                sdigit_kernel<double><<<g, 256, 0, ctx.stream>>>(static_cast<const double*>(X), K, MM, ldx, Ex, xd, d,
-                                                                 Ks, tiles_m, sk);
-            RNLA_LAUNCH_CHECK();
-        }
+        prm.sk = sk.get() + (size_t)d * digit_bytes;
         kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
         RNLA_LAUNCH_CHECK();
         count_launch();
