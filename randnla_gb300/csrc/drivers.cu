@@ -574,6 +574,57 @@ static void blendenpik_validate(int64_t m, int64_t n, double epsilon, int64_t l,
     if (n <= 0) fail(RNLA_ERR_INVALID_DIMENSIONS, "A must have at least one column");
 }
 
+// max and min of the first n diagonal entries of R (ld), one CTA
+__global__ void diag_range_kernel(const double* __restrict__ R, int64_t n, int64_t ld, double* __restrict__ out) {
+    __shared__ double mx[256], mn[256];
+    double a = 0.0, b = INFINITY;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = fabs(R[i + i * ld]);
+        a = fmax(a, v);
+        b = fmin(b, v);
+    }
+    mx[threadIdx.x] = a;
+    mn[threadIdx.x] = b;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) {
+            mx[threadIdx.x] = fmax(mx[threadIdx.x], mx[threadIdx.x + s]);
+            mn[threadIdx.x] = fmin(mn[threadIdx.x], mn[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = mx[0];
+        out[1] = mn[0];
+    }
+}
+
+// R of the sketch [S a, S b] (d x nc, ld d) without Householder reflections:
+// the float-float Gram of [S a, S b] (gram_ff, ~2^-48 relative) and a blocked
+// FP64 Cholesky of it.  Its last column is R^-T (S a)^T S b = (Q^T S b)[:n],
+// the reference's z_0 (sketch_and_precondition.rs:54), so R and z_0 land in
+// the top n rows of SK exactly where the Householder QR leaves them.  The
+// Gram's rounding perturbs the preconditioned sketch (S a) R^-1 by about
+// 2^-48 kappa(S a)^2; R is kept only when that stays below 2^-5 (kappa
+// estimated by the ratio of R's extreme diagonal entries, a lower bound),
+// so the preconditioner's quality -- and the LSQR iteration count -- is that
+// of the Householder R.  Otherwise SK is left untouched and false returned.
+static bool cholqr_sketch(Ctx& ctx, double* SK, int64_t d, int64_t n, int64_t nc) {
+    DevBuf<double> Gm((size_t)nc * nc, ctx.stream), ext(2, ctx.stream);
+    gram_ff(ctx, SK, d, nc, SK, d, nc, d, Gm, nc);
+    if (!cholesky_upper(ctx, Gm, nc, nc, n)) return false;
+    diag_range_kernel<<<1, 256, 0, ctx.stream>>>(Gm, n, nc, ext);
+    RNLA_LAUNCH_CHECK();
+    double h[2] = {0.0, 0.0};
+    RNLA_CUDA(cudaMemcpyAsync(h, ext.get(), sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (!(h[1] > 0.0)) return false;
+    const double ratio = h[0] / h[1];
+    if (!(ratio * ratio * 0x1p-48 <= 0x1p-5)) return false;
+    copy_matrix(ctx, n, nc, Gm, nc, SK, d);
+    return true;
+}
+
 // With a feed, A is still arriving from the host in column chunks: the
 // tensor-core sketch consumes each column tile as it lands; every other
 // path waits for the whole matrix first.
@@ -627,13 +678,18 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
     DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
     bool inv_ok;
+    int qr_fallbacks = 0;
     if (o.precision != RNLA_PREC_FP64 && qr_ff_supported(ctx, d, n, nc)) {
         // float-float factorization on the FP32 pipe (qr_ff.cu)
         householder_qr_ff(ctx, SK, d, n, nc, d);
         inv_ok = upper_inverse_ff(ctx, SK, n, d, Mi, n);
     } else if (o.precision != RNLA_PREC_FP64 && qr_ff_tsqr_supported(ctx, d, n, nc)) {
-        // taller sketches (d = 4096 at n = 1024): two row halves, then their R blocks
-        householder_qr_ff_tsqr(ctx, SK, d, n, nc, d);
+        // wider sketches (d = 4096 at n = 1024): CholeskyQR where the sketch's
+        // conditioning allows it, else two row halves, then their R blocks
+        if (o.orth != 0 || !cholqr_sketch(ctx, SK, d, n, nc)) {
+            if (o.orth == 0) ++qr_fallbacks;
+            householder_qr_ff_tsqr(ctx, SK, d, n, nc, d);
+        }
         inv_ok = upper_inverse_ff(ctx, SK, n, d, Mi, n);
     } else {
         householder_qr(ctx, SK, d, n, nc, d, tau);
@@ -684,6 +740,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         st->xnorm = lr.xnorm;
         st->sketch_rows = d;
         st->precision_used = o.precision;
+        st->orth_fallbacks = qr_fallbacks;
         st->ms_sketch = tm.ms(0, 1);
         st->ms_factor = tm.ms(1, 2);
         st->ms_solve = tm.ms(2, 3);

@@ -6,6 +6,7 @@
 //   * one-sided Jacobi SVD of a small matrix (lora_drivers.rs:53 `B.svd`)
 // All run on the GPU in FP64.
 #include "rnla_internal.h"
+#include <cooperative_groups.h>
 #include <vector>
 
 namespace rnla {
@@ -473,54 +474,147 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(double* __restrict__ G, 
     }
 }
 
-// The same right-looking Cholesky over a cooperative grid: CTA c owns the
-// columns j = c, c + G, ...; step k updates G[i][j] -= G[k][i] G[k][j] / G[k][k]
-// (k < i <= j) in the owned columns with the unscaled pivot row, which no
-// one writes during the step; a bounded grid barrier ends each step.  The
-// rows are scaled by 1 / sqrt(G[k][k]) at the end.  Every CTA reads the same
-// pivot, so a non-positive one ends all of them at the same step.
-__global__ void __launch_bounds__(256) cholesky_coop_kernel(double* __restrict__ G, int64_t n, int64_t ld,
-                                                            unsigned int* status, GridBarrier bar) {
-    for (int64_t k = 0; k < n; ++k) {
-        const double d = *((volatile double*)&G[k + k * ld]);
-        if (!(d > 0.0)) {
-            if (threadIdx.x == 0) atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);
+// Blocked right-looking Cholesky G = R^T R over a cooperative grid (upper
+// triangle read, R written over it, strict lower triangle zeroed).  Panels
+// of CHB = 32 rows; CTA c owns the columns j = c, c + G, ...  Per panel K:
+//   (1) every CTA loads the panel's diagonal block and factors it in shared
+//       memory (warp 0; the other warps wait): redundant work, but no grid
+//       barrier between the diagonal block and its use;
+//   (2) each CTA forms the panel rows R[K][j] = R_KK^-T G[K][j] of its own
+//       trailing columns (one warp per column, forward substitution with
+//       the pivots' reciprocals); CTA 0 writes R_KK;
+//   grid barrier (the panel rows of every column are now in G);
+//   (3) each CTA subtracts R[K][i]^T R[K][j] from its own columns j, rows
+//       k1 <= i <= j, with 64-row chunks of the panel rows staged in shared
+//       memory;
+//   grid barrier.
+// Two barriers per 32 columns instead of one per column.  Columns at or
+// beyond npd (npd = n or n - 1) need no positive pivot: a bordered Gram
+// [X c]^T [X c] gives R of X and, in column n - 1, R^-T X^T c and the
+// residual norm sqrt(max(0, .)).  Every CTA factors the same diagonal block
+// from the same data, so a non-positive pivot ends all of them at the same
+// panel.
+constexpr int CHB = 32;
+constexpr int CH_THREADS = 256;
+
+__global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __restrict__ G, int64_t n, int64_t npd,
+                                                                      int64_t ld, unsigned int* status,
+                                                                      GridBarrier bar) {
+    __shared__ double Ds[CHB][CHB + 1];           // diagonal block, R_KK after step (1)
+    __shared__ double ris[CHB];                   // 1 / R[t][t]
+    __shared__ double Ps[CHB][64 + 1];            // panel rows of a 64-row chunk
+    __shared__ int bad_s;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int Gc = gridDim.x, c = blockIdx.x;
+    for (int64_t k0 = 0; k0 < npd; k0 += CHB) {
+        const int kb = (int)(npd - k0 < CHB ? npd - k0 : CHB);
+        const int64_t k1 = k0 + kb;
+        // (1) diagonal block
+        for (int e = tid; e < CHB * CHB; e += CH_THREADS) {
+            const int i = e % CHB, j = e / CHB;
+            Ds[i][j] = (i <= j && j < kb) ? G[(k0 + i) + (k0 + j) * ld] : 0.0;
+        }
+        if (tid == 0) bad_s = 0;
+        __syncthreads();
+        if (warp == 0) {
+            for (int t = 0; t < kb; ++t) {
+                const double d = Ds[t][t];
+                if (!(d > 0.0)) {
+                    if (lane == 0) bad_s = 1;
+                    break;
+                }
+                const double ri = rsqrt(d);
+                __syncwarp();
+                if (lane >= t && lane < kb) Ds[t][lane] *= ri;      // row t of R (R[t][t] = d ri)
+                if (lane == 0) ris[t] = ri;
+                __syncwarp();
+                if (lane > t && lane < kb) {
+                    const double rl = Ds[t][lane];
+                    for (int i = t + 1; i <= lane; ++i) Ds[i][lane] = fma(-Ds[t][i], rl, Ds[i][lane]);
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        if (bad_s) {
+            if (tid == 0) atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);
             return;
         }
-        const double inv = 1.0 / d;
-        for (int64_t j = k + 1 + blockIdx.x; j < n; j += gridDim.x) {
-            const double gkj = G[k + j * ld] * inv;
-            for (int64_t i = k + 1 + threadIdx.x; i <= j; i += blockDim.x)
-                G[i + j * ld] = fma(-G[k + i * ld], gkj, G[i + j * ld]);
+        // (2) panel rows of the owned trailing columns: R_KK^T x = g
+        {
+            int64_t j = k1 + ((c - k1 % Gc) % Gc + Gc) % Gc;        // first owned column >= k1
+            j += (int64_t)warp * Gc;
+            for (; j < n; j += (int64_t)(CH_THREADS / 32) * Gc) {
+                double g = lane < kb ? G[(k0 + lane) + j * ld] : 0.0;
+                for (int s = 0; s < kb; ++s) {
+                    const double xs = __shfl_sync(0xffffffffu, g, s) * ris[s];
+                    if (lane == s) g = xs;
+                    else if (lane > s && lane < kb) g = fma(-Ds[s][lane], xs, g);
+                }
+                if (lane < kb) G[(k0 + lane) + j * ld] = g;
+            }
+        }
+        if (!grid_sync(bar)) return;
+        // every CTA has read the diagonal block: R_KK replaces it
+        if (c == 0)
+            for (int e = tid; e < kb * kb; e += CH_THREADS) {
+                const int i = e % kb, j = e / kb;
+                if (i <= j) G[(k0 + i) + (k0 + j) * ld] = Ds[i][j];
+            }
+        // (3) trailing update of the owned columns
+        const int64_t jfirst = k1 + ((c - k1 % Gc) % Gc + Gc) % Gc;
+        if (jfirst < n) {
+            const int64_t jlast = (n - 1) - (((n - 1 - c) % Gc) + Gc) % Gc;   // last owned column
+            const int r = tid & 63, cg = tid >> 6;          // row within the chunk, column group
+            for (int64_t i0 = k1; i0 <= jlast; i0 += 64) {
+                __syncthreads();
+                for (int e = tid; e < CHB * 64; e += CH_THREADS) {
+                    const int t = e % CHB, rr = e / CHB;
+                    Ps[t][rr] = (t < kb && i0 + rr < n) ? G[(k0 + t) + (i0 + rr) * ld] : 0.0;
+                }
+                __syncthreads();
+                const int64_t i = i0 + r;
+                // owned columns j >= max(jfirst, i0), handed to the four column groups in turn
+                int64_t j = jfirst;
+                if (j < i0) j += ((i0 - j + Gc - 1) / Gc) * Gc;
+                j += (int64_t)cg * Gc;
+                for (; j < n; j += 4 * (int64_t)Gc) {
+                    if (i > j) continue;
+                    double acc = 0.0;
+                    const double* gj = G + k0 + j * ld;
+#pragma unroll 8
+                    for (int t = 0; t < kb; ++t) acc = fma(Ps[t][r], gj[t], acc);
+                    G[i + j * ld] -= acc;
+                }
+            }
         }
         if (!grid_sync(bar)) return;
     }
+    // trailing columns beyond npd: the residual norm on the diagonal
     const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
-    // scale row i by 1 / sqrt(G[i][i]) (diagonal last, in its own pass)
     for (int64_t e = gt; e < n * n; e += gs) {
         const int64_t i = e % n, j = e / n;
-        if (i < j) G[i + j * ld] /= sqrt(G[i + i * ld]);
-        else if (i > j) G[i + j * ld] = 0.0;
+        if (i > j) G[i + j * ld] = 0.0;
+        else if (i == j && i >= npd) G[i + j * ld] = sqrt(fmax(G[i + j * ld], 0.0));
     }
-    if (!grid_sync(bar)) return;
-    for (int64_t i = gt; i < n; i += gs) G[i + i * ld] = sqrt(G[i + i * ld]);
 }
 
-bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld) {
+bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd) {
+    if (npd < 0) npd = n;
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
-    if (n >= 128) {
-        // one barrier per column beats a single CTA's FP64 throughput
+    if (n >= 128 || npd < n) {
         int nb = 0;
-        RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, cholesky_coop_kernel, 256, 0));
+        RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, cholesky_blocked_kernel, CH_THREADS, 0));
         int Gs = ctx.sm_count;
         if (Gs > nb * ctx.sm_count) Gs = nb * ctx.sm_count;
         if (Gs > n) Gs = (int)n;
+        if (Gs < 1) Gs = 1;
         DevBuf<unsigned int> bw(2, ctx.stream);
         RNLA_CUDA(cudaMemsetAsync(bw.get(), 0, 2 * sizeof(unsigned int), ctx.stream));
         GridBarrier bar{bw.get(), bw.get() + 1, ctx.status};
-        void* args[] = {&G, &n, &ld, &ctx.status, &bar};
-        RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_coop_kernel, dim3((unsigned)Gs), dim3(256), args,
-                                              0, ctx.stream));
+        void* args[] = {&G, &n, &npd, &ld, &ctx.status, &bar};
+        RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)cholesky_blocked_kernel, dim3((unsigned)Gs),
+                                              dim3(CH_THREADS), args, 0, ctx.stream));
         count_launch();
     } else {
         cholesky_kernel<<<1, 1024, 0, ctx.stream>>>(G, n, ld, ctx.status);
@@ -770,12 +864,14 @@ __global__ void __launch_bounds__(256) jacobi_coop_kernel(double* __restrict__ W
                     wa[i] = c * x - sn * y;
                     wb[i] = sn * x + c * y;
                 }
-                double* va = V + (int64_t)a * s;
-                double* vb = V + (int64_t)b * s;
-                for (int i = tid; i < s; i += blockDim.x) {
-                    const double x = va[i], y = vb[i];
-                    va[i] = c * x - sn * y;
-                    vb[i] = sn * x + c * y;
+                if (V) {
+                    double* va = V + (int64_t)a * s;
+                    double* vb = V + (int64_t)b * s;
+                    for (int i = tid; i < s; i += blockDim.x) {
+                        const double x = va[i], y = vb[i];
+                        va[i] = c * x - sn * y;
+                        vb[i] = sn * x + c * y;
+                    }
                 }
                 if (tid == 0) atomicAdd(&rot[sweep & 1], 1u);
             }
@@ -821,7 +917,7 @@ __global__ void __launch_bounds__(256) jacobi_finish_kernel(const double* __rest
         if (threadIdx.x == 0) sigma[r] = sg;
         for (int i = threadIdx.x; i < s; i += blockDim.x) {
             UR[i + (int64_t)r * s] = (sg > 0.0) ? W[i + (int64_t)c * s] / sg : 0.0;
-            VS[i + (int64_t)r * s] = V[i + (int64_t)c * s];
+            if (V) VS[i + (int64_t)r * s] = V[i + (int64_t)c * s];
         }
     }
     __syncthreads();
@@ -869,12 +965,144 @@ __global__ void triu_copy_kernel(const double* __restrict__ src, int64_t lds, in
     }
 }
 
-// One-sided Jacobi of W (s x s) with the rotations accumulated into V: one
-// CTA for small s, the cooperative grid version from s = 64 on.
+// The same one-sided Jacobi on one thread-block cluster of JC CTAs whose
+// shared memories hold W (and V) between them: column c lives in CTA c % JC
+// at slot c / JC; each warp of the cluster owns one position of the
+// round-robin pairing (jacobi_coop_kernel's), reads its two columns through
+// distributed shared memory into registers (JE elements per lane), reduces
+// alpha, beta, gamma with shuffles, rotates and writes them back.  A round
+// ends with a cluster barrier -- hardware, a few hundred cycles -- where the
+// grid version pays a global-memory barrier (~2 us) and L2 round trips for
+// the columns.  The rotation count of a sweep is summed over the cluster's
+// shared counters, so every CTA leaves after the same sweep.  s <= JC * 40.
+namespace jcl {
+constexpr int JC = 8;
+constexpr int JE = 10;
+constexpr int SMAX = 32 * JE;
+}  // namespace jcl
+
+__global__ void __cluster_dims__(jcl::JC, 1, 1) __launch_bounds__(640, 1)
+    jacobi_cluster_kernel(double* __restrict__ W, double* __restrict__ V, int s, int max_sweeps) {
+    using namespace jcl;
+    namespace cg = cooperative_groups;
+    extern __shared__ double jsm[];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    const int cw = (s + JC - 1) / JC;
+    double* Ws = jsm;
+    double* Vs = jsm + (size_t)cw * s;
+    unsigned int* cnt = (unsigned int*)(jsm + (size_t)cw * s * (V ? 2 : 1));
+    for (int e = threadIdx.x; e < cw * s; e += blockDim.x) {
+        const int slot = e / s, i = e % s, c = slot * JC + rank;
+        Ws[e] = c < s ? W[i + (int64_t)c * s] : 0.0;
+        if (V) Vs[e] = c < s ? V[i + (int64_t)c * s] : 0.0;
+    }
+    if (threadIdx.x < 2) cnt[threadIdx.x] = 0u;
+    cl.sync();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int sp = (s + 1) & ~1, npairs = sp / 2;
+    const int pr = rank * nwarps + warp;
+    const double tol = 1e-15;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        for (int round = 0; round < sp - 1; ++round) {
+            int a = s, b = s;
+            if (pr < npairs) {
+                if (pr == 0) { a = 0; b = 1 + (round % (sp - 1)); }
+                else {
+                    a = 1 + ((round + pr) % (sp - 1));
+                    b = 1 + ((round + sp - 1 - pr) % (sp - 1));
+                }
+                if (a > b) { const int t = a; a = b; b = t; }
+            }
+            if (a < s && b < s) {                        // uniform over the warp
+                double* wa = cl.map_shared_rank(Ws + (size_t)(a / JC) * s, (unsigned)(a % JC));
+                double* wb = cl.map_shared_rank(Ws + (size_t)(b / JC) * s, (unsigned)(b % JC));
+                double x[JE], y[JE];
+                double al = 0.0, be = 0.0, ga = 0.0;
+#pragma unroll
+                for (int e = 0; e < JE; ++e) {
+                    const int i = lane + 32 * e;
+                    x[e] = i < s ? wa[i] : 0.0;
+                    y[e] = i < s ? wb[i] : 0.0;
+                    al = fma(x[e], x[e], al);
+                    be = fma(y[e], y[e], be);
+                    ga = fma(x[e], y[e], ga);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    al += __shfl_xor_sync(0xffffffffu, al, o);
+                    be += __shfl_xor_sync(0xffffffffu, be, o);
+                    ga += __shfl_xor_sync(0xffffffffu, ga, o);
+                }
+                if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
+                    // t = tan of the rotation angle, the root of t^2 + 2 zeta t - 1 with |t| <= 1,
+                    // zeta = (beta - alpha) / (2 gamma)
+                    const double tau = be - al;
+                    const double h = sqrt(fma(tau, tau, 4.0 * ga * ga));
+                    const double t = 2.0 * ga / (tau >= 0.0 ? tau + h : tau - h);
+                    const double c = rsqrt(fma(t, t, 1.0));
+                    const double sn = c * t;
+#pragma unroll
+                    for (int e = 0; e < JE; ++e) {
+                        const int i = lane + 32 * e;
+                        if (i < s) {
+                            wa[i] = c * x[e] - sn * y[e];
+                            wb[i] = sn * x[e] + c * y[e];
+                        }
+                    }
+                    if (V) {
+                        double* va = cl.map_shared_rank(Vs + (size_t)(a / JC) * s, (unsigned)(a % JC));
+                        double* vb = cl.map_shared_rank(Vs + (size_t)(b / JC) * s, (unsigned)(b % JC));
+#pragma unroll
+                        for (int e = 0; e < JE; ++e) {
+                            const int i = lane + 32 * e;
+                            if (i < s) {
+                                const double p = va[i], q = vb[i];
+                                va[i] = c * p - sn * q;
+                                vb[i] = sn * p + c * q;
+                            }
+                        }
+                    }
+                    if (lane == 0) atomicAdd(&cnt[sweep & 1], 1u);
+                }
+            }
+            cl.sync();
+        }
+        unsigned int tot = 0u;
+        for (int r = 0; r < JC; ++r) tot += *((volatile unsigned int*)cl.map_shared_rank(&cnt[sweep & 1], (unsigned)r));
+        cl.sync();
+        if (threadIdx.x == 0) cnt[sweep & 1] = 0u;
+        if (tot == 0u) break;
+    }
+    cl.sync();
+    for (int e = threadIdx.x; e < cw * s; e += blockDim.x) {
+        const int slot = e / s, i = e % s, c = slot * JC + rank;
+        if (c < s) {
+            W[i + (int64_t)c * s] = Ws[e];
+            if (V) V[i + (int64_t)c * s] = Vs[e];
+        }
+    }
+}
+
+// One-sided Jacobi of W (s x s) with the rotations accumulated into V (V may
+// be null): one CTA for small s, one cluster up to s = 320, the cooperative
+// grid version beyond.
 void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s) {
     if (s < 64) {
+        if (!V) fail(RNLA_ERR_COMPUTATION, "single-CTA Jacobi needs V");
         jacobi_kernel<<<1, 1024, 0, ctx.stream>>>(W, V, (int)s, 60);
         RNLA_LAUNCH_CHECK();
+        return;
+    }
+    if (s <= jcl::SMAX) {
+        const int cw = (int)((s + jcl::JC - 1) / jcl::JC);
+        const size_t smem = (size_t)cw * s * sizeof(double) * (V ? 2 : 1) + 16;
+        const int npairs = (int)((s + 1) / 2);
+        const int nwarps = (npairs + jcl::JC - 1) / jcl::JC;
+        RNLA_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        jacobi_cluster_kernel<<<jcl::JC, 32 * nwarps, smem, ctx.stream>>>(W, V, (int)s, 60);
+        RNLA_LAUNCH_CHECK();
+        count_launch();
         return;
     }
     int nb = 0;
@@ -925,19 +1153,27 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     transpose(ctx, p, q, B, ldb, Bt, q);
     gram_ff(ctx, Bt, q, p, Bt, q, p, q, G, p);                 // B B^T
     if (!cholesky_upper(ctx, G, p, p)) return false;
-    DevBuf<double> W((size_t)p * p, ctx.stream), VR((size_t)p * p, ctx.stream), UR((size_t)p * p, ctx.stream),
-        VS((size_t)p * p, ctx.stream), sg(p, ctx.stream);
+    DevBuf<double> W((size_t)p * p, ctx.stream), UR((size_t)p * p, ctx.stream), sg(p, ctx.stream);
     DevBuf<int> order(p, ctx.stream);
     int g = div_up(p * p, 256);
     if (g > 1024) g = 1024;
-    triu_copy_kernel<<<g, 256, 0, ctx.stream>>>(G, p, p, W);
+    // Jacobi on R^T (the rows of R): R^T V' = W' with orthogonal columns, so
+    // B B^T = R^T R = (W' Sigma^-1) Sigma^2 (W' Sigma^-1)^T and U_B is W' with
+    // normalised columns -- no rotation accumulation
+    triu_copy_kernel<<<g, 256, 0, ctx.stream>>>(G, p, p, UR);
     RNLA_LAUNCH_CHECK();
-    fill_identity(ctx, p, p, VR, p);
-    jacobi_sweeps(ctx, W, VR, p);
+    transpose(ctx, p, p, UR, p, W, p);
+    DevBuf<double> VR;
+    if (p < 64) {                                    // the single-CTA Jacobi accumulates V regardless
+        VR.alloc((size_t)p * p, ctx.stream);
+        fill_identity(ctx, p, p, VR, p);
+    }
+    jacobi_sweeps(ctx, W, p < 64 ? VR.get() : nullptr, p);
     const size_t smem = (size_t)p * sizeof(double);
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, VR, (int)p, UR, VS, sg, order);
+    DevBuf<double> VS((size_t)p * p, ctx.stream);
+    jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, nullptr, (int)p, VS, nullptr, sg, order);
     RNLA_LAUNCH_CHECK();
     double ext[2];
     RNLA_CUDA(cudaMemcpyAsync(&ext[0], sg.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));

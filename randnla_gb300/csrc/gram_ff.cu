@@ -25,14 +25,30 @@ constexpr int TM = 64;          // tile rows / columns
 constexpr int KC = 32;          // K rows per shared-memory slice
 constexpr int THREADS = 256;
 
+// Tile (t1, t2) of C for a linear tile index: column-major over all tiles,
+// or for a symmetric product X^T X over the upper triangle t1 <= t2 only.
+__host__ __device__ __forceinline__ void tile_coords(int tile, int tiles1, int sym, int& t1, int& t2) {
+    if (!sym) {
+        t1 = tile % tiles1;
+        t2 = tile / tiles1;
+        return;
+    }
+    int c = (int)((sqrt(8.0 * tile + 1.0) - 1.0) * 0.5);
+    while ((c + 1) * (c + 2) / 2 <= tile) ++c;
+    while (c * (c + 1) / 2 > tile) --c;
+    t2 = c;
+    t1 = tile - c * (c + 1) / 2;
+}
+
 __global__ void __launch_bounds__(THREADS) gram_ff_kernel(const double* __restrict__ X, int64_t ldx, int64_t N1,
                                                           const double* __restrict__ Y, int64_t ldy, int64_t N2,
-                                                          int64_t K, int64_t rows_per_chunk, int tiles1,
+                                                          int64_t K, int64_t rows_per_chunk, int tiles1, int sym,
                                                           float4* __restrict__ part) {
     __shared__ float2 xs[KC][TM + 1];
     __shared__ float2 ys[KC][TM + 1];
     const int tile = blockIdx.x, chunk = blockIdx.y;
-    const int t1 = tile % tiles1, t2 = tile / tiles1;
+    int t1, t2;
+    tile_coords(tile, tiles1, sym, t1, t2);
     const int64_t i0 = (int64_t)t1 * TM, j0 = (int64_t)t2 * TM;
     const int64_t k0 = (int64_t)chunk * rows_per_chunk;
     const int64_t k1 = min(K, k0 + rows_per_chunk);
@@ -86,11 +102,20 @@ __global__ void __launch_bounds__(THREADS) gram_ff_kernel(const double* __restri
 }
 
 // C[i + j ldc] = sum over chunks (fixed order, float-float) of the partials.
-__global__ void gram_sum_kernel(const float4* __restrict__ part, int chunks, int tiles1, int tiles, int64_t N1,
-                                int64_t N2, double* __restrict__ C, int64_t ldc) {
+// (for a symmetric product the lower tiles are read from their mirror)
+__global__ void gram_sum_kernel(const float4* __restrict__ part, int chunks, int tiles1, int tiles, int sym,
+                                int64_t N1, int64_t N2, double* __restrict__ C, int64_t ldc) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < N1 * N2; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = e % N1, j = e / N1;
-        const int tile = (int)(i / TM) + tiles1 * (int)(j / TM);
+        int64_t i = e % N1, j = e / N1;
+        const int64_t io = i, jo = j;
+        int tile;
+        if (sym) {
+            if (i / TM > j / TM) { const int64_t t = i; i = j; j = t; }
+            const int a = (int)(i / TM), b = (int)(j / TM);
+            tile = b * (b + 1) / 2 + a;
+        } else {
+            tile = (int)(i / TM) + tiles1 * (int)(j / TM);
+        }
         const int r = (int)(i % TM), c = (int)(j % TM);
         float h = 0.f, l = 0.f;
         for (int ch = 0; ch < chunks; ++ch) {
@@ -99,7 +124,7 @@ __global__ void gram_sum_kernel(const float4* __restrict__ part, int chunks, int
             else ff_acc(h, l, v.x, v.y);
         }
         const float2 s = ff_norm(h, l);
-        C[i + j * ldc] = (double)s.x + (double)s.y;
+        C[io + jo * ldc] = (double)s.x + (double)s.y;
     }
 }
 
@@ -113,8 +138,10 @@ void gram_ff(Ctx& ctx, const double* X, int64_t ldx, int64_t N1, const double* Y
         fill_zero(ctx, N1, N2, C, ldc);
         return;
     }
+    // X^T X: the upper tiles only, mirrored in the sum
+    const int sym = (X == Y && ldx == ldy && N1 == N2) ? 1 : 0;
     const int tiles1 = div_up(N1, TM), tiles2 = div_up(N2, TM);
-    const int tiles = tiles1 * tiles2;
+    const int tiles = sym ? tiles1 * (tiles1 + 1) / 2 : tiles1 * tiles2;
     // about two CTAs per SM over (tile, K chunk), chunks a multiple of 32 rows
     int chunks = div_up(2 * ctx.sm_count, tiles);
     const int64_t max_chunks = div_up(K, KC);
@@ -124,12 +151,12 @@ void gram_ff(Ctx& ctx, const double* X, int64_t ldx, int64_t N1, const double* Y
     chunks = div_up(K, rpc);
     DevBuf<float4> part((size_t)chunks * tiles * (TM * TM / 2), ctx.stream);
     gram_ff_kernel<<<dim3((unsigned)tiles, (unsigned)chunks), THREADS, 0, ctx.stream>>>(X, ldx, N1, Y, ldy, N2, K, rpc,
-                                                                                   tiles1, part);
+                                                                                   tiles1, sym, part);
     RNLA_LAUNCH_CHECK();
     count_launch();
     int g = div_up(N1 * N2, 256);
     if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
-    gram_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, chunks, tiles1, tiles, N1, N2, C, ldc);
+    gram_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, chunks, tiles1, tiles, sym, N1, N2, C, ldc);
     RNLA_LAUNCH_CHECK();
 }
 

@@ -60,7 +60,7 @@ void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, co
                            double* x);
 // Cholesky G = R^T R (upper R written to the upper triangle of G, n x n);
 // returns false if a pivot is not positive (synchronises).
-bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld);
+bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd = -1);
 // Thin orthonormal basis of Y (m x n, m >= n) in place: CholeskyQR2, with a
 // Householder fallback when a Cholesky pivot fails.  Returns 1 if the
 // fallback was taken.
