@@ -565,7 +565,7 @@ def run_svd(args, rank, local, ws):
         ev[i][0].record(stream)
         _, st = R.rand_svd_dev(A, k, 1e-6, p, U, sg, Vt, o)
         ev[i][1].record(stream)
-        stages.append((st["ms_sketch"], st["ms_factor"], st["ms_solve"]))
+        stages.append((st["ms_sketch"], st["ms_factor"], st["ms_solve"], st["svd_sweeps"]))
     torch.cuda.synchronize()
     launches = lib.rnla_kernel_launches() - launches0
     clk = clocks.stop()
@@ -606,7 +606,8 @@ def run_svd(args, rank, local, ws):
         "config": workload_config(args, wl, ws),
         "path": "BF16X rand_svd (RandNLA mode): split-bf16 tensor-core range finder, CholeskyQR2, FP64 SVD finish",
         "accuracy": acc,
-        "stages": {"range_finder_ms": rf, "projection_ms": pr, "svd_finish_ms": fin, "passes_over_A": passes},
+        "stages": {"range_finder_ms": rf, "projection_ms": pr, "svd_finish_ms": fin, "passes_over_A": passes,
+                   "jacobi_sweeps": stages[-1][3]},
         "fp64_path": fp64,
         "speedup_vs_fp64_path": (value / ws) / fp64["value"] if fp64 else None,
         "e2e": None,

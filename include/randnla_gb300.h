@@ -169,6 +169,7 @@ typedef struct {
     int32_t precision_used;
     double ms_sketch, ms_factor, ms_solve, ms_total;  /* device-timed stages */
     double ms_kernel;         /* the inner solver's persistent kernel alone (device-timed; LSQR) */
+    int64_t svd_sweeps;       /* rand_svd (tensor-core RandNLA mode): one-sided Jacobi sweeps of the small SVD */
 } rnla_stats;
 
 /* Defaults: FP64, reference mode, CGLS, power_iters 2, Philox4x32 key 0,

@@ -31,7 +31,7 @@ class Stats(ctypes.Structure):
                 ("anorm", c_dbl), ("acond", c_dbl), ("arnorm", c_dbl), ("xnorm", c_dbl),
                 ("sketch_rows", c_i64), ("rank", c_i64), ("orth_fallbacks", c_i32),
                 ("precision_used", c_i32), ("ms_sketch", c_dbl), ("ms_factor", c_dbl),
-                ("ms_solve", c_dbl), ("ms_total", c_dbl), ("ms_kernel", c_dbl)]
+                ("ms_solve", c_dbl), ("ms_total", c_dbl), ("ms_kernel", c_dbl), ("svd_sweeps", c_i64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -376,7 +376,7 @@ static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int pas
 // the FP64 Gaussian of the FP64 path (same key).
 static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int64_t n, int64_t lda, int64_t k,
                             int64_t l, const rnla_options& o, double* U, int64_t ldu, double* sig, double* Vt,
-                            int64_t ldvt, int& fallbacks, StageTimer& tm) {
+                            int64_t ldvt, int& fallbacks, int& sweeps, StageTimer& tm) {
     const int LP = (o.digits_a >= 1 && o.digits_a <= 3) ? o.digits_a : 2;   // power-iteration level
     const RngKey key = key_of(&o.rng);
     BfxPlanes arow, acol;
@@ -433,7 +433,7 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     // small SVD of B; U = Y (R^-1 U_B)
     const int64_t r = k < l ? k : l;
     DevBuf<double> UB((size_t)l * l, ctx.stream), sg(l, ctx.stream), VB((size_t)n * l, ctx.stream);
-    if (!small_svd_gram(ctx, B, l, n, l, UB, l, sg, VB, n)) small_svd(ctx, B, l, n, l, UB, l, sg, VB, n);
+    if (!small_svd_gram(ctx, B, l, n, l, UB, l, sg, VB, n, &sweeps)) small_svd(ctx, B, l, n, l, UB, l, sg, VB, n);
     {
         DevBuf<double> RiT((size_t)l * l, ctx.stream), W2((size_t)l * r, ctx.stream);
         transpose(ctx, l, l, Ri, l, RiT, l);
@@ -483,14 +483,14 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
         ld = m;
     }
     int64_t r = 0;
-    int fallbacks = 0;
+    int fallbacks = 0, sweeps = 0;
     if (o.mode == RNLA_MODE_RANDNLA && o.precision != RNLA_PREC_FP64) {
         if (!tc_available(ctx))
             fail(RNLA_ERR_UNSUPPORTED, "tensor-core precision requested but sm_103a kernels unavailable");
         int64_t l = k + s;
         const int64_t mn = m < n ? m : n;
         if (l > mn) l = mn;
-        r = rand_svd_bfx(ctx, Av, a_f32, m, n, lda, k, l, o, U, ldu, sig, Vt, ldvt, fallbacks, tm);
+        r = rand_svd_bfx(ctx, Av, a_f32, m, n, lda, k, l, o, U, ldu, sig, Vt, ldvt, fallbacks, sweeps, tm);
     } else if (o.mode == RNLA_MODE_REFERENCE) {
         if (o.precision != RNLA_PREC_FP64)
             fail(RNLA_ERR_UNSUPPORTED, "reference mode runs in FP64 only");
@@ -534,6 +534,7 @@ static int64_t rand_svd_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, in
     if (st) {
         st->rank = r;
         st->orth_fallbacks = fallbacks;
+        st->svd_sweeps = sweeps;
         st->precision_used = o.precision;
         st->ms_sketch = tm.ms(0, 1);
         st->ms_factor = tm.ms(1, 2);

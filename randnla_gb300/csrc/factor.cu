@@ -6,7 +6,6 @@
 //   * one-sided Jacobi SVD of a small matrix (lora_drivers.rs:53 `B.svd`)
 // All run on the GPU in FP64.
 #include "rnla_internal.h"
-#include <cooperative_groups.h>
 #include <vector>
 
 namespace rnla {
@@ -496,6 +495,7 @@ __global__ void __launch_bounds__(1024) cholesky_kernel(double* __restrict__ G, 
 // panel.
 constexpr int CHB = 32;
 constexpr int CH_THREADS = 256;
+constexpr int CH_MAXQ = 32;                 // owned columns per CTA: n <= CH_MAXQ x grid
 
 __global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __restrict__ G, int64_t n, int64_t npd,
                                                                       int64_t ld, unsigned int* status,
@@ -503,6 +503,7 @@ __global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __
     __shared__ double Ds[CHB][CHB + 1];           // diagonal block, R_KK after step (1)
     __shared__ double ris[CHB];                   // 1 / R[t][t]
     __shared__ double Ps[CHB][64 + 1];            // panel rows of a 64-row chunk
+    __shared__ double Rjs[CH_MAXQ][CHB];          // panel rows of the owned trailing columns
     __shared__ int bad_s;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int Gc = gridDim.x, c = blockIdx.x;
@@ -517,23 +518,35 @@ __global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __
         if (tid == 0) bad_s = 0;
         __syncthreads();
         if (warp == 0) {
-            for (int t = 0; t < kb; ++t) {
-                const double d = Ds[t][t];
-                if (!(d > 0.0)) {
-                    if (lane == 0) bad_s = 1;
-                    break;
+            // lane c holds column c of the block in registers; step t scales
+            // row t by 1 / sqrt(pivot) and subtracts R[t][i] R[t][c] from rows
+            // t < i <= c, R[t][i] arriving from lane i by shuffle
+            double col[CHB];
+#pragma unroll
+            for (int i = 0; i < CHB; ++i) col[i] = Ds[i][lane];
+            bool bad = false;
+#pragma unroll
+            for (int t = 0; t < CHB; ++t) {
+                if (t < kb && !bad) {
+                    const double d = __shfl_sync(0xffffffffu, col[t], t);
+                    if (!(d > 0.0)) {
+                        bad = true;
+                    } else {
+                        const double ri = rsqrt(d);
+                        const double rt = col[t] * ri;               // R[t][lane] (R[t][t] = d ri)
+                        col[t] = rt;
+                        if (lane == 0) ris[t] = ri;
+#pragma unroll
+                        for (int i = t + 1; i < CHB; ++i) {
+                            const double rti = __shfl_sync(0xffffffffu, rt, i);
+                            if (i <= lane) col[i] = fma(-rti, rt, col[i]);
+                        }
+                    }
                 }
-                const double ri = rsqrt(d);
-                __syncwarp();
-                if (lane >= t && lane < kb) Ds[t][lane] *= ri;      // row t of R (R[t][t] = d ri)
-                if (lane == 0) ris[t] = ri;
-                __syncwarp();
-                if (lane > t && lane < kb) {
-                    const double rl = Ds[t][lane];
-                    for (int i = t + 1; i <= lane; ++i) Ds[i][lane] = fma(-Ds[t][i], rl, Ds[i][lane]);
-                }
-                __syncwarp();
             }
+#pragma unroll
+            for (int i = 0; i < CHB; ++i) Ds[i][lane] = col[i];
+            if (bad && lane == 0) bad_s = 1;
         }
         __syncthreads();
         if (bad_s) {
@@ -561,10 +574,16 @@ __global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __
                 const int i = e % kb, j = e / kb;
                 if (i <= j) G[(k0 + i) + (k0 + j) * ld] = Ds[i][j];
             }
-        // (3) trailing update of the owned columns
+        // (3) trailing update of the owned columns q = 0, 1, ... (j = jfirst + q Gc),
+        // their panel rows staged in shared memory
         const int64_t jfirst = k1 + ((c - k1 % Gc) % Gc + Gc) % Gc;
         if (jfirst < n) {
-            const int64_t jlast = (n - 1) - (((n - 1 - c) % Gc) + Gc) % Gc;   // last owned column
+            const int nq = (int)((n - 1 - jfirst) / Gc) + 1;
+            const int64_t jlast = jfirst + (int64_t)(nq - 1) * Gc;
+            for (int e = tid; e < nq * CHB; e += CH_THREADS) {
+                const int q = e / CHB, t = e % CHB;
+                Rjs[q][t] = t < kb ? G[(k0 + t) + (jfirst + (int64_t)q * Gc) * ld] : 0.0;
+            }
             const int r = tid & 63, cg = tid >> 6;          // row within the chunk, column group
             for (int64_t i0 = k1; i0 <= jlast; i0 += 64) {
                 __syncthreads();
@@ -574,17 +593,20 @@ __global__ void __launch_bounds__(CH_THREADS) cholesky_blocked_kernel(double* __
                 }
                 __syncthreads();
                 const int64_t i = i0 + r;
-                // owned columns j >= max(jfirst, i0), handed to the four column groups in turn
-                int64_t j = jfirst;
-                if (j < i0) j += ((i0 - j + Gc - 1) / Gc) * Gc;
-                j += (int64_t)cg * Gc;
-                for (; j < n; j += 4 * (int64_t)Gc) {
+                // owned columns j >= i0, handed to the four column groups in turn
+                const int q0 = i0 > jfirst ? (int)((i0 - jfirst + Gc - 1) / Gc) : 0;
+                for (int q = q0 + cg; q < nq; q += 4) {
+                    const int64_t j = jfirst + (int64_t)q * Gc;
                     if (i > j) continue;
-                    double acc = 0.0;
-                    const double* gj = G + k0 + j * ld;
-#pragma unroll 8
-                    for (int t = 0; t < kb; ++t) acc = fma(Ps[t][r], gj[t], acc);
-                    G[i + j * ld] -= acc;
+                    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;     // four independent chains
+#pragma unroll
+                    for (int t = 0; t < CHB; t += 4) {
+                        a0 = fma(Ps[t][r], Rjs[q][t], a0);
+                        a1 = fma(Ps[t + 1][r], Rjs[q][t + 1], a1);
+                        a2 = fma(Ps[t + 2][r], Rjs[q][t + 2], a2);
+                        a3 = fma(Ps[t + 3][r], Rjs[q][t + 3], a3);
+                    }
+                    G[i + j * ld] -= (a0 + a1) + (a2 + a3);
                 }
             }
         }
@@ -609,6 +631,7 @@ bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd) {
         if (Gs > nb * ctx.sm_count) Gs = nb * ctx.sm_count;
         if (Gs > n) Gs = (int)n;
         if (Gs < 1) Gs = 1;
+        if (n > (int64_t)CH_MAXQ * Gs) fail(RNLA_ERR_INVALID_DIMENSIONS, "Cholesky: n above the blocked kernel's limit");
         DevBuf<unsigned int> bw(2, ctx.stream);
         RNLA_CUDA(cudaMemsetAsync(bw.get(), 0, 2 * sizeof(unsigned int), ctx.stream));
         GridBarrier bar{bw.get(), bw.get() + 1, ctx.status};
@@ -823,11 +846,13 @@ __global__ void __launch_bounds__(1024) jacobi_kernel(double* __restrict__ W, do
 // 64-cycle FP64 dependent latency over s / 32 rows per lane dominates.)
 __global__ void __launch_bounds__(256) jacobi_coop_kernel(double* __restrict__ W, double* __restrict__ V, int s,
                                                           int max_sweeps, unsigned int* __restrict__ rot,
-                                                          GridBarrier bar) {
+                                                          unsigned int* __restrict__ sweeps_out, GridBarrier bar) {
     __shared__ double red[3][8];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int sp = (s + 1) & ~1;
-    const double tol = 1e-15;
+    // rotations stop at |gamma| <= s 2^-53 sqrt(alpha beta): below that, gamma is
+    // the rounding of its own s-term dot product
+    const double tol = fmax(1e-15, (double)s * 0x1p-53);
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
         for (int round = 0; round < sp - 1; ++round) {
             for (int pr = blockIdx.x; pr < sp / 2; pr += gridDim.x) {
@@ -880,7 +905,10 @@ __global__ void __launch_bounds__(256) jacobi_coop_kernel(double* __restrict__ W
         // every CTA reads this sweep's count after the last round's barrier;
         // the other slot is cleared for the next sweep before anyone uses it
         const unsigned int n_rot = *((volatile unsigned int*)&rot[sweep & 1]);
-        if (blockIdx.x == 0 && tid == 0) rot[(sweep + 1) & 1] = 0u;
+        if (blockIdx.x == 0 && tid == 0) {
+            rot[(sweep + 1) & 1] = 0u;
+            if (sweeps_out) *sweeps_out = (unsigned int)(sweep + 1);
+        }
         if (!grid_sync(bar)) return;
         if (n_rot == 0u) break;
     }
@@ -965,144 +993,14 @@ __global__ void triu_copy_kernel(const double* __restrict__ src, int64_t lds, in
     }
 }
 
-// The same one-sided Jacobi on one thread-block cluster of JC CTAs whose
-// shared memories hold W (and V) between them: column c lives in CTA c % JC
-// at slot c / JC; each warp of the cluster owns one position of the
-// round-robin pairing (jacobi_coop_kernel's), reads its two columns through
-// distributed shared memory into registers (JE elements per lane), reduces
-// alpha, beta, gamma with shuffles, rotates and writes them back.  A round
-// ends with a cluster barrier -- hardware, a few hundred cycles -- where the
-// grid version pays a global-memory barrier (~2 us) and L2 round trips for
-// the columns.  The rotation count of a sweep is summed over the cluster's
-// shared counters, so every CTA leaves after the same sweep.  s <= JC * 40.
-namespace jcl {
-constexpr int JC = 8;
-constexpr int JE = 10;
-constexpr int SMAX = 32 * JE;
-}  // namespace jcl
-
-__global__ void __cluster_dims__(jcl::JC, 1, 1) __launch_bounds__(640, 1)
-    jacobi_cluster_kernel(double* __restrict__ W, double* __restrict__ V, int s, int max_sweeps) {
-    using namespace jcl;
-    namespace cg = cooperative_groups;
-    extern __shared__ double jsm[];
-    cg::cluster_group cl = cg::this_cluster();
-    const int rank = (int)cl.block_rank();
-    const int cw = (s + JC - 1) / JC;
-    double* Ws = jsm;
-    double* Vs = jsm + (size_t)cw * s;
-    unsigned int* cnt = (unsigned int*)(jsm + (size_t)cw * s * (V ? 2 : 1));
-    for (int e = threadIdx.x; e < cw * s; e += blockDim.x) {
-        const int slot = e / s, i = e % s, c = slot * JC + rank;
-        Ws[e] = c < s ? W[i + (int64_t)c * s] : 0.0;
-        if (V) Vs[e] = c < s ? V[i + (int64_t)c * s] : 0.0;
-    }
-    if (threadIdx.x < 2) cnt[threadIdx.x] = 0u;
-    cl.sync();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int sp = (s + 1) & ~1, npairs = sp / 2;
-    const int pr = rank * nwarps + warp;
-    const double tol = 1e-15;
-    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
-        for (int round = 0; round < sp - 1; ++round) {
-            int a = s, b = s;
-            if (pr < npairs) {
-                if (pr == 0) { a = 0; b = 1 + (round % (sp - 1)); }
-                else {
-                    a = 1 + ((round + pr) % (sp - 1));
-                    b = 1 + ((round + sp - 1 - pr) % (sp - 1));
-                }
-                if (a > b) { const int t = a; a = b; b = t; }
-            }
-            if (a < s && b < s) {                        // uniform over the warp
-                double* wa = cl.map_shared_rank(Ws + (size_t)(a / JC) * s, (unsigned)(a % JC));
-                double* wb = cl.map_shared_rank(Ws + (size_t)(b / JC) * s, (unsigned)(b % JC));
-                double x[JE], y[JE];
-                double al = 0.0, be = 0.0, ga = 0.0;
-#pragma unroll
-                for (int e = 0; e < JE; ++e) {
-                    const int i = lane + 32 * e;
-                    x[e] = i < s ? wa[i] : 0.0;
-                    y[e] = i < s ? wb[i] : 0.0;
-                    al = fma(x[e], x[e], al);
-                    be = fma(y[e], y[e], be);
-                    ga = fma(x[e], y[e], ga);
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    al += __shfl_xor_sync(0xffffffffu, al, o);
-                    be += __shfl_xor_sync(0xffffffffu, be, o);
-                    ga += __shfl_xor_sync(0xffffffffu, ga, o);
-                }
-                if (ga != 0.0 && fabs(ga) > tol * sqrt(al * be)) {
-                    // t = tan of the rotation angle, the root of t^2 + 2 zeta t - 1 with |t| <= 1,
-                    // zeta = (beta - alpha) / (2 gamma)
-                    const double tau = be - al;
-                    const double h = sqrt(fma(tau, tau, 4.0 * ga * ga));
-                    const double t = 2.0 * ga / (tau >= 0.0 ? tau + h : tau - h);
-                    const double c = rsqrt(fma(t, t, 1.0));
-                    const double sn = c * t;
-#pragma unroll
-                    for (int e = 0; e < JE; ++e) {
-                        const int i = lane + 32 * e;
-                        if (i < s) {
-                            wa[i] = c * x[e] - sn * y[e];
-                            wb[i] = sn * x[e] + c * y[e];
-                        }
-                    }
-                    if (V) {
-                        double* va = cl.map_shared_rank(Vs + (size_t)(a / JC) * s, (unsigned)(a % JC));
-                        double* vb = cl.map_shared_rank(Vs + (size_t)(b / JC) * s, (unsigned)(b % JC));
-#pragma unroll
-                        for (int e = 0; e < JE; ++e) {
-                            const int i = lane + 32 * e;
-                            if (i < s) {
-                                const double p = va[i], q = vb[i];
-                                va[i] = c * p - sn * q;
-                                vb[i] = sn * p + c * q;
-                            }
-                        }
-                    }
-                    if (lane == 0) atomicAdd(&cnt[sweep & 1], 1u);
-                }
-            }
-            cl.sync();
-        }
-        unsigned int tot = 0u;
-        for (int r = 0; r < JC; ++r) tot += *((volatile unsigned int*)cl.map_shared_rank(&cnt[sweep & 1], (unsigned)r));
-        cl.sync();
-        if (threadIdx.x == 0) cnt[sweep & 1] = 0u;
-        if (tot == 0u) break;
-    }
-    cl.sync();
-    for (int e = threadIdx.x; e < cw * s; e += blockDim.x) {
-        const int slot = e / s, i = e % s, c = slot * JC + rank;
-        if (c < s) {
-            W[i + (int64_t)c * s] = Ws[e];
-            if (V) V[i + (int64_t)c * s] = Vs[e];
-        }
-    }
-}
-
 // One-sided Jacobi of W (s x s) with the rotations accumulated into V (V may
-// be null): one CTA for small s, one cluster up to s = 320, the cooperative
-// grid version beyond.
-void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s) {
+// be null from s = 64 on): one CTA for small s, the cooperative grid version
+// from s = 64 on.
+void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s, unsigned int* sweeps_dev) {
     if (s < 64) {
         if (!V) fail(RNLA_ERR_COMPUTATION, "single-CTA Jacobi needs V");
         jacobi_kernel<<<1, 1024, 0, ctx.stream>>>(W, V, (int)s, 60);
         RNLA_LAUNCH_CHECK();
-        return;
-    }
-    if (s <= jcl::SMAX) {
-        const int cw = (int)((s + jcl::JC - 1) / jcl::JC);
-        const size_t smem = (size_t)cw * s * sizeof(double) * (V ? 2 : 1) + 16;
-        const int npairs = (int)((s + 1) / 2);
-        const int nwarps = (npairs + jcl::JC - 1) / jcl::JC;
-        RNLA_CUDA(cudaFuncSetAttribute(jacobi_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        jacobi_cluster_kernel<<<jcl::JC, 32 * nwarps, smem, ctx.stream>>>(W, V, (int)s, 60);
-        RNLA_LAUNCH_CHECK();
-        count_launch();
         return;
     }
     int nb = 0;
@@ -1116,7 +1014,7 @@ void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s) {
     GridBarrier bar{words.get() + 2, words.get() + 3, ctx.status};
     int si = (int)s, sweeps = 60;
     unsigned int* rot = words.get();
-    void* args[] = {&W, &V, &si, &sweeps, &rot, &bar};
+    void* args[] = {&W, &V, &si, &sweeps, &rot, &sweeps_dev, &bar};
     RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)jacobi_coop_kernel, dim3((unsigned)G), dim3(256), args, 0,
                                           ctx.stream));
     count_launch();
@@ -1147,7 +1045,7 @@ static void scale_columns_inv(Ctx& ctx, int64_t q, int64_t p, double* V, int64_t
 // Cholesky fails or sigma_p / sigma_1 < 1e-5; the caller then takes
 // small_svd.  Synchronises once (to read the two extreme sigmas).
 bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
-                    double* sigma, double* V, int64_t ldv) {
+                    double* sigma, double* V, int64_t ldv, int* sweeps) {
     if (p <= 0 || p > q) return false;
     DevBuf<double> Bt((size_t)q * p, ctx.stream), G((size_t)p * p, ctx.stream);
     transpose(ctx, p, q, B, ldb, Bt, q);
@@ -1168,7 +1066,9 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
         VR.alloc((size_t)p * p, ctx.stream);
         fill_identity(ctx, p, p, VR, p);
     }
-    jacobi_sweeps(ctx, W, p < 64 ? VR.get() : nullptr, p);
+    DevBuf<unsigned int> nsw(1, ctx.stream);
+    RNLA_CUDA(cudaMemsetAsync(nsw.get(), 0, sizeof(unsigned int), ctx.stream));
+    jacobi_sweeps(ctx, W, p < 64 ? VR.get() : nullptr, p, nsw);
     const size_t smem = (size_t)p * sizeof(double);
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1176,9 +1076,12 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, nullptr, (int)p, VS, nullptr, sg, order);
     RNLA_LAUNCH_CHECK();
     double ext[2];
+    unsigned int hsw = 0;
     RNLA_CUDA(cudaMemcpyAsync(&ext[0], sg.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaMemcpyAsync(&ext[1], sg.get() + p - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaMemcpyAsync(&hsw, nsw.get(), sizeof hsw, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (sweeps) *sweeps = (int)hsw;
     if (!(ext[0] > 0.0) || !(ext[1] >= 1e-5 * ext[0])) return false;
     // U_B = VS (R = UR Sigma VS^T, B B^T = VS Sigma^2 VS^T); V_B = B^T VS Sigma^-1
     copy_matrix(ctx, p, p, VS, p, U, ldu);

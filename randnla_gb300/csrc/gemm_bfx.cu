@@ -33,6 +33,7 @@
 #include "rnla_internal.h"
 #include "rnla_async.cuh"
 #include "rnla_tc.cuh"
+#include "rnla_ff.cuh"
 #include <cuda_bf16.h>
 #include <algorithm>
 
@@ -256,52 +257,55 @@ __global__ void __launch_bounds__(THREADS, 1) bfx_gemm_kernel(const Params prm) 
 // ---------------------------------------------------------------------------
 // Operand images
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint16_t bf16_bits(double v) {
-    return __bfloat16_as_ushort(__float2bfloat16_rn((float)v));
-}
-__device__ __forceinline__ double bf16_value(uint16_t b) {
-    return (double)__uint_as_float((uint32_t)b << 16);
-}
-
 // Plane split of one value: p-th plane = bf16 rounding of what the earlier
-// planes leave.  FP32 data split in FP32 (each remainder v - bf16(v) is exact
-// in FP32), FP64 data in FP64.
+// planes leave, in FP32 (each remainder v - bf16(v) is exact in FP32).  FP64
+// data is first rounded to 24 bits with integer operations (ff_split), which
+// the three planes of the widest level hold exactly.
 __device__ __forceinline__ uint16_t split_step(float& rem) {
     const __nv_bfloat16 h = __float2bfloat16_rn(rem);
     rem -= __bfloat162float(h);
     return __bfloat16_as_ushort(h);
 }
-__device__ __forceinline__ uint16_t split_step(double& rem) {
-    const uint16_t h = bf16_bits(rem);
-    rem -= bf16_value(h);
-    return h;
-}
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(double v) { return ff_split(v).x; }
 
 // Block = one (row tile, K stage): TR x 64 elements staged through shared
-// memory in the source type (coalesced reads along whichever index is
-// contiguous), then each thread writes one 16-byte chunk (8 K values) of one
-// row for every plane.
+// memory as FP32 (coalesced reads along whichever index is contiguous, eight
+// loads in flight per thread), then each thread writes one 16-byte chunk (8 K
+// values) of one row for every plane.  TR x 64 is a multiple of 8 x 256.
 template <typename T>
 __global__ void __launch_bounds__(256) planes_kernel(const T* __restrict__ src, int64_t R, int64_t K, int64_t sr,
                                                      int64_t sk, int TR, int Ks, int PL, uint8_t* __restrict__ out) {
     extern __shared__ __align__(16) unsigned char st_raw[];
-    T* st = reinterpret_cast<T*>(st_raw);                 // TR x (64 + 1)
+    float* st = reinterpret_cast<float*>(st_raw);         // TR x (64 + 1)
     const int rt = blockIdx.x / Ks, s = blockIdx.x % Ks;
     const int64_t r0 = (int64_t)rt * TR, k0 = (int64_t)s * BK;
     const int n = TR * BK;
     const bool kfast = (sk == 1);
-    for (int e = threadIdx.x; e < n; e += blockDim.x) {
-        const int r = kfast ? e / BK : e % TR;
-        const int k = kfast ? e % BK : e / TR;
-        const int64_t rg = r0 + r, kg = k0 + k;
-        st[r * (BK + 1) + k] = (rg < R && kg < K) ? src[rg * sr + kg * sk] : (T)0;
+    for (int e0 = threadIdx.x; e0 < n; e0 += 8 * blockDim.x) {
+        T v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int e = e0 + q * blockDim.x;
+            const int r = kfast ? e / BK : e % TR;
+            const int k = kfast ? e % BK : e / TR;
+            const int64_t rg = r0 + r, kg = k0 + k;
+            v[q] = (e < n && rg < R && kg < K) ? src[rg * sr + kg * sk] : (T)0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int e = e0 + q * blockDim.x;
+            const int r = kfast ? e / BK : e % TR;
+            const int k = kfast ? e % BK : e / TR;
+            if (e < n) st[r * (BK + 1) + k] = to_f32(v[q]);
+        }
     }
     __syncthreads();
     const size_t tile_bytes = (size_t)TR * BK * 2;
     uint8_t* base = out + ((size_t)rt * Ks + s) * PL * tile_bytes;
     for (int t = threadIdx.x; t < TR * 8; t += blockDim.x) {
         const int r = t >> 3, c8 = t & 7;
-        T rem[8];
+        float rem[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) rem[j] = st[r * (BK + 1) + c8 * 8 + j];
         for (int p = 0; p < PL; ++p) {
@@ -352,7 +356,7 @@ void bfx_planes(Ctx& ctx, BfxPlanes& P, const void* src, bool f32, int64_t R, in
     P.tiles = div_up(R, TR);
     P.Ks = div_up(K, BK);
     P.buf.alloc((size_t)P.tiles * P.Ks * planes * TR * BK * 2, ctx.stream);
-    const size_t smem = (size_t)TR * (BK + 1) * (f32 ? sizeof(float) : sizeof(double));
+    const size_t smem = (size_t)TR * (BK + 1) * sizeof(float);
     const unsigned blocks = (unsigned)((int64_t)P.tiles * P.Ks);
     if (f32) {
         auto k = planes_kernel<float>;

@@ -73,12 +73,12 @@ void full_piv_lu_l(Ctx& ctx, const double* X, int64_t m, int64_t n, int64_t ldx,
 // first unused coordinate vectors (so SVD(0) = (I, 0, I)).
 // One-sided Jacobi of W (s x s), rotations accumulated into V (one CTA for
 // s < 64, a cooperative grid above).
-void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s);
+void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s, unsigned int* sweeps_dev = nullptr);
 // SVD of a wide B (p <= q) through chol(B B^T) with a float-float Gram:
 // U_B (p x p), sigma (p), V_B (q x p).  Returns false (caller uses
 // small_svd) when the Cholesky fails or sigma_p / sigma_1 < 1e-5.
 bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
-                    double* sigma, double* V, int64_t ldv);
+                    double* sigma, double* V, int64_t ldv, int* sweeps = nullptr);
 void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U,
                int64_t ldu, double* sigma, double* V, int64_t ldv);
 

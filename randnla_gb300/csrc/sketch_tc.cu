@@ -88,6 +88,7 @@ struct Params {
     int jt_only;              // >= 0: only column tile jt_only (units = tiles_m * kc_count)
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
     const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
+    int ypl;                  // planes stored per stage in ydig (>= P; the first P are used)
     long long* partial;       // [kc][tile][BN][BM] exact integer sums (row fastest)
     unsigned int* status;
 };
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
             for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
                 const Unit w = unit_of(prm, u);
                 const uint8_t* sk = prm.sk + ((size_t)w.it * prm.Ks + w.s_begin) * S_BYTES;
-                const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)w.jt * prm.Ks + w.s_begin) * (size_t)(P * YD_BYTES);
+                const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)w.jt * prm.Ks + w.s_begin) * (size_t)(prm.ypl * YD_BYTES);
                 for (int i = 0; i < w.nst; ++i) {
                     const int slot = g % STAGES;
                     if (g >= STAGES && !mbar_wait(&empty[slot], (uint32_t)((g / STAGES) - 1) & 1u, err)) {
@@ -223,7 +224,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                     bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
 #pragma unroll
                     for (int p = 0; p < P; ++p)
-                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * P + p) * YD_BYTES, YD_BYTES,
+                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * prm.ypl + p) * YD_BYTES, YD_BYTES,
                                  &full[slot]);
                     ++g;
                 }
@@ -383,6 +384,39 @@ __global__ void exp_init_kernel(int* __restrict__ E, int64_t n) {
 
 // Block (x, y): rows [x * rows_per_block, ...) of column j0 + y; the block
 // maximum goes into E[j] with atomicMax (the maximum is order independent).
+// The largest |y| is the largest bit pattern with the sign cleared (IEEE
+// order), so the loop is a load, a mask and an unsigned max per element, with
+// eight loads in flight per thread; the exponent is formed once per thread.
+__device__ __forceinline__ int exp_of_bits(uint32_t b) {          // FP32 |y| bits -> E with |y| < 2^E
+    const int e = (int)(b >> 23);
+    return e ? e - 126 : -149 + (32 - __clz((int)(b & 0x7FFFFFu)));
+}
+__device__ __forceinline__ int exp_of_bits(uint64_t b) {          // FP64
+    const int e = (int)(b >> 52);
+    return e ? e - 1022 : -1074 + (64 - __clzll((long long)(b & 0xFFFFFFFFFFFFFull)));
+}
+__device__ __forceinline__ uint32_t abs_bits(float y) { return __float_as_uint(y) & 0x7FFFFFFFu; }
+__device__ __forceinline__ uint64_t abs_bits(double y) {
+    return (uint64_t)__double_as_longlong(y) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+template <typename T>
+__device__ __forceinline__ int column_max_exp(const T* __restrict__ col, int64_t k0, int64_t k1) {
+    using U = decltype(abs_bits(T(0)));
+    U best = 0;
+    constexpr int Q = 8;
+    int64_t k = k0 + threadIdx.x;
+    for (; k + (Q - 1) * (int64_t)blockDim.x < k1; k += Q * (int64_t)blockDim.x) {
+        T v[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) v[q] = col[k + q * (int64_t)blockDim.x];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) best = max(best, abs_bits(v[q]));
+    }
+    for (; k < k1; k += blockDim.x) best = max(best, abs_bits(col[k]));
+    return best ? exp_of_bits(best) : -1074;
+}
+
 template <typename T>
 __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
                               const double* __restrict__ extra, int* __restrict__ E, int64_t j0,
@@ -390,30 +424,7 @@ __global__ void colexp_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int
     const int64_t j = j0 + blockIdx.y;
     const int64_t k0 = (int64_t)blockIdx.x * rows_per_block;
     const int64_t k1 = min(K, k0 + rows_per_block);
-    int best = -1074;
-    // eight independent loads in flight per thread (the loop is bound by
-    // memory latency, not by the exponent arithmetic)
-    constexpr int U = 8;
-    int64_t k = k0 + threadIdx.x;
-    for (; k + (U - 1) * (int64_t)blockDim.x < k1; k += U * (int64_t)blockDim.x) {
-        uint64_t M[U];
-        int e2[U];
-#pragma unroll
-        for (int q = 0; q < U; ++q) {
-            bool neg;
-            load_elem(Y, ldy, N, extra, k + q * (int64_t)blockDim.x, j, M[q], e2[q], neg);
-        }
-#pragma unroll
-        for (int q = 0; q < U; ++q)
-            if (M[q]) best = max(best, e2[q] + 64 - __clzll((long long)M[q]));
-    }
-    for (; k < k1; k += blockDim.x) {
-        uint64_t M;
-        int e2;
-        bool neg;
-        load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
-        if (M) best = max(best, e2 + 64 - __clzll((long long)M));
-    }
+    int best = (j < N) ? column_max_exp(Y + j * ldy, k0, k1) : column_max_exp(extra, k0, k1);
     __shared__ int red[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
@@ -573,7 +584,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
-    prm.sk = sk; prm.ydig = dig; prm.partial = part; prm.status = ctx.status;
+    prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
     auto kfn = sketch_mma_kernel<P>;
     RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -734,6 +745,17 @@ __global__ void exact_tn_sum_kernel(const long long* __restrict__ part, int kc_c
 // roundings are the two digit truncations and the final FP64 sums over the
 // xd launches.  All X digit images are built in one pass over X
 // (xd x tiles_m x Ks x 16 KB).
+template <int P>
+static void launch_mma(Ctx& ctx, const tc::Params& prm, unsigned grid) {
+    using namespace tc;
+    const size_t smem = smem_bytes<P>();
+    auto kfn = sketch_mma_kernel<P>;
+    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+    RNLA_LAUNCH_CHECK();
+    count_launch();
+}
+
 void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int64_t ldx, const double* Y,
                  int64_t NN, int64_t ldy, double* C, int64_t ldc, bool trans, int xd) {
     using namespace tc;
@@ -798,26 +820,30 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
         RNLA_LAUNCH_CHECK();
     }
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
-    const size_t smem = smem_bytes<P>();
-    auto kfn = sketch_mma_kernel<P>;
-    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     Params prm;
     prm.M = MM; prm.N = NN; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units; prm.jt_only = -1;
-    prm.sk = sk; prm.ydig = dig; prm.partial = part; prm.status = ctx.status;
+    prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
     const unsigned grid = (unsigned)(units < sm ? units : sm);
     const int exact_sum = (int64_t)wins + kc_count <= WIN_MAX ? 1 : 0;
     int gs = div_up(MM * NN, 256);
     if (gs > 8 * sm) gs = 8 * sm;
     for (int d = 0; d < xd; ++d) {
+        // digit pair (d, p) weighs 2^-(6 d + 8 p) against the leading pair; X's
+        // truncation after xd digits is 2^-6 xd, so pairs below 2^-(6 xd + 4)
+        // are left out: the first Pd planes of Y for X digit d
+        const int Pd = std::min(P, (6 * xd + 4 - 6 * d) / 8 + 1);
         prm.sk = sk.get() + (size_t)d * digit_bytes;
-        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
-        RNLA_LAUNCH_CHECK();
-        count_launch();
+        switch (Pd) {
+            case 1: launch_mma<1>(ctx, prm, grid); break;
+            case 2: launch_mma<2>(ctx, prm, grid); break;
+            case 3: launch_mma<3>(ctx, prm, grid); break;
+            default: launch_mma<4>(ctx, prm, grid); break;
+        }
         exact_tn_sum_kernel<<<gs, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, MM, NN, Ex, Ey,
-                                                        8 * P + 6 * (d + 1), exact_sum, d > 0 ? 1 : 0, trans ? 1 : 0,
+                                                        8 * Pd + 6 * (d + 1), exact_sum, d > 0 ? 1 : 0, trans ? 1 : 0,
                                                         C, ldc);
         RNLA_LAUNCH_CHECK();
     }
