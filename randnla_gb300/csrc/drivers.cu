@@ -339,7 +339,7 @@ static int64_t svd_finish(Ctx& ctx, int prec, const double* Q, int64_t m, int64_
 
 // Orthonormal basis of Y (m x l, ld m, m >= l) in place: CholeskyQR2 with
 // the Grams and the triangular products on the split-bf16 tensor-core GEMM
-// at level 3 (FP32 accumulation over K = m), Cholesky and R^-1 in FP64; the
+// at level 3 (FP32 accumulation over K = m), Cholesky in float-float, R^-1 in FP64; the
 // FP64 Householder basis when a Cholesky pivot fails.  Returns 1 on
 // fallback.
 static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int passes = 2) {
@@ -352,7 +352,7 @@ static int orthonormalize_bfx(Ctx& ctx, double* Y, int64_t m, int64_t l, int pas
             bfx_planes(ctx, yb, Y, false, l, m, m, 1, bfx_tile_rows(3, false), 3);
             bfx_gemm(ctx, 3, ya, yb, G, l, false);                                    // G = Y^T Y
         }
-        if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
+        if (!cholesky_upper_ff(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
             orthonormalize(ctx, Y, m, l, m, true);
             return 1;
         }
@@ -419,7 +419,7 @@ static int64_t rand_svd_bfx(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     DevBuf<double> G((size_t)l * l, ctx.stream), Ri((size_t)l * l, ctx.stream), Bt((size_t)l * n, ctx.stream),
         B((size_t)l * n, ctx.stream);
     gram_ff(ctx, Y, m, l, Y, m, l, m, G, l);
-    if (!cholesky_upper(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
+    if (!cholesky_upper_ff(ctx, G, l, l) || !upper_inverse(ctx, G, l, l, Ri, l)) {
         // Y lost rank: the FP64 Householder basis and the plain projection
         fallbacks += orthonormalize(ctx, Y, m, l, m, true);
         fill_identity(ctx, l, l, Ri, l);
@@ -602,7 +602,7 @@ __global__ void diag_range_kernel(const double* __restrict__ R, int64_t n, int64
 
 // R of the sketch [S a, S b] (d x nc, ld d) without Householder reflections:
 // the float-float Gram of [S a, S b] (gram_ff, ~2^-48 relative) and a blocked
-// FP64 Cholesky of it.  Its last column is R^-T (S a)^T S b = (Q^T S b)[:n],
+// float-float Cholesky of it.  Its last column is R^-T (S a)^T S b = (Q^T S b)[:n],
 // the reference's z_0 (sketch_and_precondition.rs:54), so R and z_0 land in
 // the top n rows of SK exactly where the Householder QR leaves them.  The
 // Gram's rounding perturbs the preconditioned sketch (S a) R^-1 by about
@@ -613,7 +613,7 @@ __global__ void diag_range_kernel(const double* __restrict__ R, int64_t n, int64
 static bool cholqr_sketch(Ctx& ctx, double* SK, int64_t d, int64_t n, int64_t nc) {
     DevBuf<double> Gm((size_t)nc * nc, ctx.stream), ext(2, ctx.stream);
     gram_ff(ctx, SK, d, nc, SK, d, nc, d, Gm, nc);
-    if (!cholesky_upper(ctx, Gm, nc, nc, n)) return false;
+    if (!cholesky_upper_ff(ctx, Gm, nc, nc, n)) return false;
     diag_range_kernel<<<1, 256, 0, ctx.stream>>>(Gm, n, nc, ext);
     RNLA_LAUNCH_CHECK();
     double h[2] = {0.0, 0.0};
@@ -643,6 +643,7 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
     tm.mark();
     const RngKey key = key_of(&o.rng);
     const int64_t nc = n + 1;
+    LsqrFFInput lsqr_in;
     DevBuf<double> SK((size_t)d * nc, ctx.stream);
     if (o.precision == RNLA_PREC_FP64) {
         if (feed) feed->wait_all(ctx.stream);
@@ -666,14 +667,17 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // the whole BF16X solve is enqueued without intermediate host
         // synchronisation; the device status is checked once at the end
         ctx.deferred = true;
+        // device-resident A: the solver's row-major copy may start right away
+        // (after the sketch generator on the side stream, beside the sketch)
+        if (!feed && o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n))
+            lsqr_ff_reserve(ctx, a_f32, m, n, lsqr_in);
         // S [a b] in one pass: b rides along as column n of the digit planes
         tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed);
         if (feed) feed->wait_all(ctx.stream);
     }
     tm.mark();
-    // BF16X + LSQR: the float-float copies of A and b for the solver are built
-    // on the side stream while the QR runs
-    LsqrFFInput lsqr_in;
+    // BF16X + LSQR: the float-float (or FP32 row-major) copies of A and b for
+    // the solver, on the side stream
     if (o.precision != RNLA_PREC_FP64 && o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n))
         lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)

@@ -647,7 +647,9 @@ bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd) {
     RNLA_CUDA(cudaMemcpyAsync(&h, ctx.status, sizeof h, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
-    return h == 0;
+    if (h == KSTATUS_NOT_PD) return false;
+    if (h != KSTATUS_OK) throw Error(RNLA_ERR_TIMEOUT, "Cholesky: a grid barrier exceeded its limit");
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -1050,7 +1052,7 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     DevBuf<double> Bt((size_t)q * p, ctx.stream), G((size_t)p * p, ctx.stream);
     transpose(ctx, p, q, B, ldb, Bt, q);
     gram_ff(ctx, Bt, q, p, Bt, q, p, q, G, p);                 // B B^T
-    if (!cholesky_upper(ctx, G, p, p)) return false;
+    if (!cholesky_upper_ff(ctx, G, p, p)) return false;
     DevBuf<double> W((size_t)p * p, ctx.stream), UR((size_t)p * p, ctx.stream), sg(p, ctx.stream);
     DevBuf<int> order(p, ctx.stream);
     int g = div_up(p * p, 256);

@@ -59,32 +59,16 @@ __global__ void __launch_bounds__(THREADS) gram_ff_kernel(const double* __restri
     for (int a = 0; a < 4; ++a)
 #pragma unroll
         for (int b = 0; b < 2; ++b) { ah[a][b] = 0ull; al[a][b] = 0ull; }
-    // element (k, c) of each 32 x 64 slice, consecutive threads on consecutive k;
-    // the next slice's values are loaded into registers while this one is used
-    constexpr int PER = KC * TM / THREADS;           // 8 elements of X and of Y per thread
-    double px[PER], py[PER];
-    auto fetch = [&](int64_t kb) {
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int e = tid + q * THREADS;
+    for (int64_t kb = k0; kb < k1; kb += KC) {
+        // stage: element (k, c) of each 32 x 64 slice; consecutive threads take consecutive k
+        for (int e = tid; e < KC * TM; e += THREADS) {
             const int k = e % KC, c = e / KC;
             const int64_t kg = kb + k;
             const bool kin = kg < k1;
-            px[q] = (kin && i0 + c < N1) ? X[kg + (i0 + c) * ldx] : 0.0;
-            py[q] = (kin && j0 + c < N2) ? Y[kg + (j0 + c) * ldy] : 0.0;
-        }
-    };
-    if (k0 < k1) fetch(k0);
-    for (int64_t kb = k0; kb < k1; kb += KC) {
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int e = tid + q * THREADS;
-            const int k = e % KC, c = e / KC;
-            xs[k][c] = ff_split(px[q]);
-            ys[k][c] = ff_split(py[q]);
+            xs[k][c] = (kin && i0 + c < N1) ? ff_split(X[kg + (i0 + c) * ldx]) : make_float2(0.f, 0.f);
+            ys[k][c] = (kin && j0 + c < N2) ? ff_split(Y[kg + (j0 + c) * ldy]) : make_float2(0.f, 0.f);
         }
         __syncthreads();
-        if (kb + KC < k1) fetch(kb + KC);
 #pragma unroll 4
         for (int k = 0; k < KC; ++k) {
             f32x2 bh[2], nbh[2], bl[2];

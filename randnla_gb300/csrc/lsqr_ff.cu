@@ -1410,18 +1410,31 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     RNLA_LAUNCH_CHECK();
 }
 
-void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
-                     LsqrFFInput& in) {
+void lsqr_ff_reserve(Ctx& ctx, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in) {
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
-    in.A = A; in.m = m; in.n = n;
+    in.m = m; in.n = n;
     in.f32 = a_f32;
     // FP32 data: a row-major FP32 copy (ldf = n rounded up to 4 floats);
     // FP64 data: the float-float copy (ldf = n rounded up to 2 pairs)
     in.ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
     in.AF.alloc(a_f32 ? (size_t)m * in.ldf / 2 : (size_t)m * in.ldf, ctx.stream);
     in.bF.alloc(m, ctx.stream);
+    RNLA_CUDA(cudaEventCreateWithFlags(&in.start, cudaEventDisableTiming));
+    RNLA_CUDA(cudaEventRecord(in.start, ctx.stream));
+}
+
+void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
+                     LsqrFFInput& in) {
+    if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
     const cudaStream_t side = side_stream(ctx.device);
-    stream_wait(side, ctx.stream);                 // buffers allocated, A and b written
+    if (in.start && in.m == m && in.n == n && in.f32 == a_f32) {
+        // buffers reserved earlier: build from that point on
+        RNLA_CUDA(cudaStreamWaitEvent(side, in.start, 0));
+    } else {
+        lsqr_ff_reserve(ctx, a_f32, m, n, in);
+        stream_wait(side, ctx.stream);             // buffers allocated, A and b written
+    }
+    in.A = A;
     build_ff_input(ctx, side, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
     RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     in.owner = ctx.stream;

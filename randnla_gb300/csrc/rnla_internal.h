@@ -61,6 +61,9 @@ void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, co
 // Cholesky G = R^T R (upper R written to the upper triangle of G, n x n);
 // returns false if a pivot is not positive (synchronises).
 bool cholesky_upper(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd = -1);
+// The same factorization in float-float (chol_ff.cu) for the tensor-core
+// paths, whose Grams carry ~2^-48 themselves.
+bool cholesky_upper_ff(Ctx& ctx, double* G, int64_t n, int64_t ld, int64_t npd = -1);
 // Thin orthonormal basis of Y (m x n, m >= n) in place: CholeskyQR2, with a
 // Householder fallback when a Cholesky pivot fails.  Returns 1 if the
 // fallback was taken.
@@ -142,6 +145,7 @@ struct LsqrFFInput {
     bool f32 = false;               // AF holds FP32 rows (A stored in FP32)
     int64_t m = 0, n = 0, ldf = 0;
     cudaEvent_t ready = nullptr;
+    cudaEvent_t start = nullptr;    // set by lsqr_ff_reserve: the point the build may start from
     cudaStream_t owner = nullptr;   // stream the buffers are freed on
     LsqrFFInput() = default;
     LsqrFFInput(const LsqrFFInput&) = delete;
@@ -153,12 +157,17 @@ struct LsqrFFInput {
             cudaStreamWaitEvent(owner, ready, 0);
             cudaEventDestroy(ready);
         }
+        if (start) cudaEventDestroy(start);
     }
 };
 bool lsqr_ff_supported(int64_t n);
 // M (n x n upper) <- the FP64 value of its float-float split, so that the
 // float-float LSQR operator A M and a later FP64 product M z use the same M.
 void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm);
+// lsqr_ff_reserve allocates the copies on ctx.stream and records that point:
+// a later lsqr_ff_prepare then starts the build from there (A and b must
+// already be in place), so it can overlap work enqueued in between.
+void lsqr_ff_reserve(Ctx& ctx, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in);
 void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
                      LsqrFFInput& in);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,

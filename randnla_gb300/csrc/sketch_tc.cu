@@ -86,6 +86,7 @@ struct Params {
     int tiles_m, tiles_n, Ks, kc_count, stages_per_kc;
     int units;                // work units of this launch
     int jt_only;              // >= 0: only column tile jt_only (units = tiles_m * kc_count)
+    int it0, it_count;        // the row tiles [it0, it0 + it_count) of this launch
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
     const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
     int ypl;                  // planes stored per stage in ydig (>= P; the first P are used)
@@ -112,11 +113,11 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // rows of the image, so stores are coalesced.  Entry (i, k) is word
 // i + k * round_up(M, 4) of the stream (block (i >> 2) + k * M4 / 4).
 __global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int dist, int64_t M, int64_t K, int Ks,
-                                                         uint8_t* __restrict__ S) {
+                                                         int it0, uint8_t* __restrict__ S) {
     __shared__ uint32_t qtab[128];
     if (threadIdx.x < 128) qtab[threadIdx.x] = k_qgauss_table[threadIdx.x];
     __syncthreads();
-    const int it = blockIdx.y;
+    const int it = it0 + blockIdx.y;
     const uint64_t gstride = (uint64_t)(((M + 3) & ~3LL) >> 2);
     const int64_t units = (int64_t)Ks * 1024;            // 32 row groups x 32 K pairs per stage
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < units;
@@ -156,8 +157,8 @@ __device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
         w.jt = u % prm.tiles_n;
         rest = u / prm.tiles_n;
     }
-    w.it = rest % prm.tiles_m;
-    w.kc = rest / prm.tiles_m;
+    w.it = prm.it0 + rest % prm.it_count;
+    w.kc = rest / prm.it_count;
     w.s_begin = w.kc * prm.stages_per_kc;
     w.nst = min(prm.Ks, w.s_begin + prm.stages_per_kc) - w.s_begin;
     return w;
@@ -546,7 +547,10 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     // with a feed and a small S, each column tile is its own launch as its
     // columns arrive (below)
     const bool per_tile = feed && (double)tiles_m * Ks * S_BYTES * tiles_n <= 4.0e9;
-    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : tiles;
+    // without a feed and with a large S, S is generated in two halves of its
+    // rows and the MMA runs once per half (below)
+    const bool halves = !feed && tiles_m >= 2 && (double)tiles_m * Ks * S_BYTES >= 1.0e9;
+    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : halves ? (int64_t)(tiles_m / 2) * tiles_n : tiles;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -570,19 +574,31 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
     // the sketch generator (integer ALU bound) runs on the side stream while
-    // the main stream makes the digit planes (HBM bound)
+    // the main stream makes the digit planes (HBM bound).  Without a feed and
+    // with a large S the rows of S come in two halves: the MMA over the first
+    // half starts once it is written and the generator's second half runs
+    // beside it (the MMA CTAs leave the CUDA cores mostly idle)
     const cudaStream_t side = side_stream(ctx.device);
     stream_wait(side, ctx.stream);                 // the S buffer exists
-    {
+    const int h = halves ? tiles_m / 2 : tiles_m;
+    cudaEvent_t first_half = nullptr;
+    auto gen = [&](int it0, int cnt) {
         int gx = div_up((int64_t)Ks * 1024, 256);
-        const int cap = 16 * sm / (tiles_m < 16 ? tiles_m : 16) + 1;
+        const int cap = 16 * sm / (cnt < 16 ? cnt : 16) + 1;
         if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, sk);
+        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)cnt), 256, 0, side>>>(key, dist, M, K, Ks, it0, sk);
         RNLA_LAUNCH_CHECK();
+    };
+    gen(0, h);
+    if (halves) {
+        RNLA_CUDA(cudaEventCreateWithFlags(&first_half, cudaEventDisableTiming));
+        RNLA_CUDA(cudaEventRecord(first_half, side));
+        gen(h, tiles_m - h);
     }
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
+    prm.it0 = 0; prm.it_count = tiles_m;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
@@ -612,10 +628,24 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     };
     if (!feed) {
         digits(0, tiles_n);
-        stream_wait(ctx.stream, side);             // S is written
         prm.jt_only = -1;
-        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
-        RNLA_LAUNCH_CHECK();
+        if (halves) {
+            for (int part = 0; part < 2; ++part) {
+                if (part == 0) RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, first_half, 0));
+                else stream_wait(ctx.stream, side);         // all of S is written
+                prm.it0 = part == 0 ? 0 : h;
+                prm.it_count = part == 0 ? h : tiles_m - h;
+                prm.units = (int)((int64_t)prm.it_count * tiles_n * kc_count);
+                const unsigned gp = (unsigned)(prm.units < sm ? prm.units : sm);
+                kfn<<<gp, THREADS, smem, ctx.stream>>>(prm);
+                RNLA_LAUNCH_CHECK();
+            }
+            RNLA_CUDA(cudaEventDestroy(first_half));
+        } else {
+            stream_wait(ctx.stream, side);             // S is written
+            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+            RNLA_LAUNCH_CHECK();
+        }
     } else {
         // Each column tile's digit planes are made as soon as its columns
         // have landed.  The MMA runs per column tile too (overlapping the
@@ -824,6 +854,7 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
     prm.M = MM; prm.N = NN; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units; prm.jt_only = -1;
+    prm.it0 = 0; prm.it_count = tiles_m;
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
     const unsigned grid = (unsigned)(units < sm ? units : sm);
