@@ -1038,6 +1038,23 @@ static void scale_columns_inv(Ctx& ctx, int64_t q, int64_t p, double* V, int64_t
     RNLA_LAUNCH_CHECK();
 }
 
+// U_B = VS (eigenvectors of B B^T, descending sigma), sigma, V_B = B^T VS
+// Sigma^-1 (float-float product); false -- nothing the caller keeps written
+// -- when sigma_p / sigma_1 < 1e-5 (the Gram route loses the small ones)
+static bool finish_gram_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, const double* VS,
+                            const double* sg, double* U, int64_t ldu, double* sigma, double* V, int64_t ldv) {
+    double ext[2];
+    RNLA_CUDA(cudaMemcpyAsync(&ext[0], sg, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaMemcpyAsync(&ext[1], sg + p - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (!(ext[0] > 0.0) || !(ext[1] >= 1e-5 * ext[0])) return false;
+    copy_matrix(ctx, p, p, VS, p, U, ldu);
+    RNLA_CUDA(cudaMemcpyAsync(sigma, sg, p * sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
+    gram_ff(ctx, B, ldb, q, VS, p, p, p, V, ldv);
+    scale_columns_inv(ctx, q, p, V, ldv, sg);
+    return true;
+}
+
 // SVD of a wide B (p x q, p <= q) from R = chol(B B^T): the Gram is formed
 // in float-float (gram_ff), R's right singular vectors (one-sided Jacobi on
 // R) are B's left ones U_B, the column norms its singular values, and
@@ -1052,9 +1069,15 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     DevBuf<double> Bt((size_t)q * p, ctx.stream), G((size_t)p * p, ctx.stream);
     transpose(ctx, p, q, B, ldb, Bt, q);
     gram_ff(ctx, Bt, q, p, Bt, q, p, q, G, p);                 // B B^T
+    DevBuf<double> G0((size_t)p * p, ctx.stream);
+    copy_matrix(ctx, p, p, G, p, G0, p);
     if (!cholesky_upper_ff(ctx, G, p, p)) return false;
     DevBuf<double> W((size_t)p * p, ctx.stream), UR((size_t)p * p, ctx.stream), sg(p, ctx.stream);
+    DevBuf<double> VS((size_t)p * p, ctx.stream);
     DevBuf<int> order(p, ctx.stream);
+    // FP32 cluster Jacobi + float-float Rayleigh-Ritz (eig_refine.cu), else
+    // the FP64 grid Jacobi below
+    if (eig_gram_refined(ctx, G0, G, p, VS, p, sg, sweeps)) return finish_gram_svd(ctx, B, p, q, ldb, VS, sg, U, ldu, sigma, V, ldv);
     int g = div_up(p * p, 256);
     if (g > 1024) g = 1024;
     // Jacobi on R^T (the rows of R): R^T V' = W' with orthogonal columns, so
@@ -1074,23 +1097,13 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     const size_t smem = (size_t)p * sizeof(double);
     if (smem > 48 * 1024)
         RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    DevBuf<double> VS((size_t)p * p, ctx.stream);
     jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, nullptr, (int)p, VS, nullptr, sg, order);
     RNLA_LAUNCH_CHECK();
-    double ext[2];
     unsigned int hsw = 0;
-    RNLA_CUDA(cudaMemcpyAsync(&ext[0], sg.get(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
-    RNLA_CUDA(cudaMemcpyAsync(&ext[1], sg.get() + p - 1, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaMemcpyAsync(&hsw, nsw.get(), sizeof hsw, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));
     if (sweeps) *sweeps = (int)hsw;
-    if (!(ext[0] > 0.0) || !(ext[1] >= 1e-5 * ext[0])) return false;
-    // U_B = VS (R = UR Sigma VS^T, B B^T = VS Sigma^2 VS^T); V_B = B^T VS Sigma^-1
-    copy_matrix(ctx, p, p, VS, p, U, ldu);
-    RNLA_CUDA(cudaMemcpyAsync(sigma, sg.get(), p * sizeof(double), cudaMemcpyDeviceToDevice, ctx.stream));
-    gram_ff(ctx, B, ldb, q, VS, p, p, p, V, ldv);
-    scale_columns_inv(ctx, q, p, V, ldv, sg);
-    return true;
+    return finish_gram_svd(ctx, B, p, q, ldb, VS, sg, U, ldu, sigma, V, ldv);
 }
 
 void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,

@@ -1306,18 +1306,32 @@ __global__ void rowmajor_split_kernel(const TA* __restrict__ A, int64_t m, int64
 // Row-major FP32 copy: row i is ldq floats (n rounded up to a multiple of 4,
 // zero beyond n), so a 16-byte chunk holds 4 consecutive columns.  32 x 32
 // tiles through shared memory.
-__global__ void rowmajor_f32_kernel(const float* __restrict__ A, int64_t m, int64_t n, int64_t lda,
-                                    float* __restrict__ AQ, int64_t ldq) {
-    __shared__ float tile[32][33];
-    const int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
-    for (int k = threadIdx.y; k < 32; k += 8) {
-        const int64_t i = i0 + threadIdx.x, j = j0 + k;
-        tile[k][threadIdx.x] = (i < m && j < n) ? A[i + j * lda] : 0.f;
-    }
-    __syncthreads();
-    for (int k = threadIdx.y; k < 32; k += 8) {
-        const int64_t i = i0 + k, j = j0 + threadIdx.x;
-        if (i < m && j < ldq) AQ[i * ldq + j] = tile[threadIdx.x][k];
+// Row-major FP32 copy of a column-major FP32 A, 64 x 64 tiles through shared
+// memory (256-byte column segments in, 256-byte row segments out), one
+// persistent block per SM walking the tiles: it runs beside the sketch's
+// tensor-core kernel (whose CTAs leave room for one such block per SM).
+__global__ void __launch_bounds__(256) rowmajor_f32_kernel(const float* __restrict__ A, int64_t m, int64_t n,
+                                                           int64_t lda, float* __restrict__ AQ, int64_t ldq) {
+    __shared__ float tile[64][65];
+    const int64_t tm = (m + 63) / 64, tn = (ldq + 63) / 64;
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;       // 64 x 4
+    for (int64_t t = blockIdx.x; t < tm * tn; t += gridDim.x) {
+        const int64_t i0 = (t % tm) * 64, j0 = (t / tm) * 64;
+        float v[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int64_t i = i0 + tx, j = j0 + ty + 4 * q;
+            v[q] = (i < m && j < n) ? A[i + j * lda] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) tile[ty + 4 * q][tx] = v[q];
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int64_t i = i0 + ty + 4 * q, j = j0 + tx;
+            if (i < m && j < ldq) AQ[i * ldq + j] = tile[tx][ty + 4 * q];
+        }
+        __syncthreads();
     }
 }
 
@@ -1398,7 +1412,7 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
     if (a_f32)
-        rowmajor_f32_kernel<<<grid, dim3(32, 8), 0, st>>>(static_cast<const float*>(A), m, n, lda,
+        rowmajor_f32_kernel<<<ctx.sm_count, 256, 0, st>>>(static_cast<const float*>(A), m, n, lda,
                                                           reinterpret_cast<float*>(AF), ldf);
     else
         rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,

@@ -582,18 +582,20 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     stream_wait(side, ctx.stream);                 // the S buffer exists
     const int h = halves ? tiles_m / 2 : tiles_m;
     cudaEvent_t first_half = nullptr;
-    auto gen = [&](int it0, int cnt) {
+    // (the second half runs beside the first MMA: about one block per SM, so
+    // that the MMA's CTAs find room next to it)
+    auto gen = [&](int it0, int cnt, bool beside) {
         int gx = div_up((int64_t)Ks * 1024, 256);
-        const int cap = 16 * sm / (cnt < 16 ? cnt : 16) + 1;
+        const int cap = beside ? std::max(1, sm / cnt) : 16 * sm / (cnt < 16 ? cnt : 16) + 1;
         if (gx > cap) gx = cap;
         sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)cnt), 256, 0, side>>>(key, dist, M, K, Ks, it0, sk);
         RNLA_LAUNCH_CHECK();
     };
-    gen(0, h);
+    gen(0, h, false);
     if (halves) {
         RNLA_CUDA(cudaEventCreateWithFlags(&first_half, cudaEventDisableTiming));
         RNLA_CUDA(cudaEventRecord(first_half, side));
-        gen(h, tiles_m - h);
+        gen(h, tiles_m - h, true);
     }
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
