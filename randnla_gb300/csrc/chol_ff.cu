@@ -4,11 +4,11 @@
 // Gram-based small SVD, the CholeskyQR R of wide least-squares sketches.
 //
 // Same data flow as cholesky_blocked_kernel (factor.cu) -- panels of 32
-// rows, every CTA factors the panel's diagonal block redundantly (one warp,
-// the block's columns in registers), forms the panel rows of its own
-// columns by forward substitution, grid barrier, subtracts R[K][i]^T R[K][j]
-// from its own columns, grid barrier -- with every operation a float-float
-// one (exact products through FMA, TwoSum accumulation): on GB300 a
+// rows, every CTA factors the panel's diagonal block redundantly (all of its
+// threads, in shared memory, one __syncthreads per pivot), forms the panel
+// rows of its own columns by forward substitution, grid barrier, subtracts
+// R[K][i]^T R[K][j] from its own columns, grid barrier -- with every
+// operation a float-float one (exact products through FMA, TwoSum accumulation): on GB300 a
 // dependent FP64 operation costs ~64 cycles and a warp's FP64 FMA occupies a
 // sub-partition's FP64 unit for 64 cycles, so the FP64 kernel spends ~30 us
 // per panel in the diagonal block alone.  The matrix lives as (hi, lo)
@@ -54,41 +54,38 @@ __global__ void __launch_bounds__(CT) chol_ff_kernel(float2* __restrict__ F, int
     for (int64_t k0 = 0; k0 < npd; k0 += CB) {
         const int kb = (int)(npd - k0 < CB ? npd - k0 : CB);
         const int64_t k1 = k0 + kb;
-        // (1) diagonal block, factored by warp 0 with the columns in registers
+        // (1) diagonal block
         for (int e = tid; e < CB * CB; e += CT) {
             const int i = e % CB, j = e / CB;
             Ds[i][j] = (i <= j && j < kb) ? F[(k0 + i) + (k0 + j) * n] : z2;
         }
         if (tid == 0) bad_s = 0;
         __syncthreads();
-        if (warp == 0) {
-            float2 col[CB];
-#pragma unroll
-            for (int i = 0; i < CB; ++i) col[i] = Ds[i][lane];
-            bool bad = false;
-#pragma unroll
-            for (int t = 0; t < CB; ++t) {
-                if (t < kb && !bad) {
-                    const float2 d = ff_shfl(col[t], t);
-                    if (!(d.x > 0.f)) {
-                        bad = true;
-                    } else {
-                        const float2 ri = ff_rsqrt(d);
-                        const float2 rt = ff_mul(col[t], ri);           // R[t][lane]
-                        col[t] = rt;
-                        if (lane == 0) ris[t] = ri;
-#pragma unroll
-                        for (int i = t + 1; i < CB; ++i) {
-                            const float2 rti = ff_shfl(rt, i);
-                            if (i <= lane) col[i] = ff_fms(col[i], rti, rt);
-                        }
-                    }
-                }
+        // every thread takes up to two entries (i, c), t < i <= c, of the block
+        // per step and subtracts (G[t][i] / sqrt(d)) (G[t][c] / sqrt(d)) with the
+        // unscaled pivot row (no one writes row t during step t); row t is
+        // scaled once the pivots are known.  One __syncthreads per pivot.
+        for (int t = 0; t < kb; ++t) {
+            const float2 d = Ds[t][t];
+            if (!(d.x > 0.f)) {
+                if (tid == 0) bad_s = 1;
+                break;
             }
-#pragma unroll
-            for (int i = 0; i < CB; ++i) Ds[i][lane] = col[i];
-            if (bad && lane == 0) bad_s = 1;
+            const float2 ri = ff_rsqrt(d);
+            if (tid == 0) ris[t] = ri;
+            const int w = kb - t - 1;                     // trailing block size
+            for (int e = tid; e < w * w; e += CT) {
+                const int i = t + 1 + e % w, cc = t + 1 + e / w;
+                if (i <= cc) Ds[i][cc] = ff_fms(Ds[i][cc], ff_mul(Ds[t][i], ri), ff_mul(Ds[t][cc], ri));
+            }
+            __syncthreads();
         }
+        __syncthreads();
+        if (!bad_s)
+            for (int e = tid; e < kb * kb; e += CT) {
+                const int t = e % kb, cc = e / kb;
+                if (t <= cc) Ds[t][cc] = ff_mul(Ds[t][cc], ris[t]);     // R[t][c]; R[t][t] = d / sqrt(d)
+            }
         __syncthreads();
         if (bad_s) {
             if (tid == 0) atomicCAS(status, 0u, (unsigned int)KSTATUS_NOT_PD);

@@ -667,19 +667,20 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // the whole BF16X solve is enqueued without intermediate host
         // synchronisation; the device status is checked once at the end
         ctx.deferred = true;
-        // device-resident A: the solver's row-major copy may start right away
-        // (after the sketch generator on the side stream, beside the sketch)
-        if (!feed && o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n))
-            lsqr_ff_reserve(ctx, a_f32, m, n, lsqr_in);
+        // BF16X + LSQR: the solver's row-major (FP32 or float-float) copies of
+        // A and b.  With A on the device they are built on the main stream
+        // while the sketch generator (side stream) is still running, ahead
+        // of the MMA that waits for it; with a feed, on the side stream after
+        // the sketch
+        const bool ffp = o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n);
+        std::function<void()> before_mma;
+        if (ffp && !feed) before_mma = [&]() { lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in, true); };
         // S [a b] in one pass: b rides along as column n of the digit planes
-        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed);
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed, DIST_GAUSSIAN, before_mma);
         if (feed) feed->wait_all(ctx.stream);
+        if (ffp && feed) lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     }
     tm.mark();
-    // BF16X + LSQR: the float-float (or FP32 row-major) copies of A and b for
-    // the solver, on the side stream
-    if (o.precision != RNLA_PREC_FP64 && o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n))
-        lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)
     DevBuf<double> tau(n, ctx.stream), Mi((size_t)n * n, ctx.stream);
     bool inv_ok;

@@ -699,19 +699,26 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
 #pragma unroll
         for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
         if (dot) {
-            f32x2 sh[RW][2], sl[RW][2];
+            // four independent accumulators per row (chunk halves x even/odd
+            // chunks) keep the TwoSum chains of one row interleaved
+            f32x2 sh[RW][4], sl[RW][4];
 #pragma unroll
-            for (int w = 0; w < RW; ++w) { sh[w][0] = sh[w][1] = sl[w][0] = sl[w][1] = 0ull; }
+            for (int w = 0; w < RW; ++w)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) { sh[w][q] = 0ull; sl[w][q] = 0ull; }
 #pragma unroll
             for (int kk = 0; kk < KC; ++kk) {
 #pragma unroll
                 for (int w = 0; w < RW; ++w) {
-                    ff2_madd_xp(v[w][kk].x, yh[2 * kk], yl[2 * kk], sh[w][0], sl[w][0]);
-                    ff2_madd_xp(v[w][kk].y, yh[2 * kk + 1], yl[2 * kk + 1], sh[w][1], sl[w][1]);
+                    const int q = 2 * (kk & 1);
+                    ff2_madd_xp(v[w][kk].x, yh[2 * kk], yl[2 * kk], sh[w][q], sl[w][q]);
+                    ff2_madd_xp(v[w][kk].y, yh[2 * kk + 1], yl[2 * kk + 1], sh[w][q + 1], sl[w][q + 1]);
                 }
             }
 #pragma unroll
             for (int w = 0; w < RW; ++w) {
+                ff2_acc(sh[w][0], sl[w][0], sh[w][2], sl[w][2]);
+                ff2_acc(sh[w][1], sl[w][1], sh[w][3], sl[w][3]);
                 ff2_acc(sh[w][0], sl[w][0], sh[w][1], sl[w][1]);
                 const float2 H = upk2(sh[w][0]), L = upk2(sl[w][0]);
                 float h = H.x, l = L.x;
@@ -1307,9 +1314,8 @@ __global__ void rowmajor_split_kernel(const TA* __restrict__ A, int64_t m, int64
 // zero beyond n), so a 16-byte chunk holds 4 consecutive columns.  32 x 32
 // tiles through shared memory.
 // Row-major FP32 copy of a column-major FP32 A, 64 x 64 tiles through shared
-// memory (256-byte column segments in, 256-byte row segments out), one
-// persistent block per SM walking the tiles: it runs beside the sketch's
-// tensor-core kernel (whose CTAs leave room for one such block per SM).
+// memory (256-byte column segments in, 256-byte row segments out), eight
+// persistent blocks per SM walking the tiles.
 __global__ void __launch_bounds__(256) rowmajor_f32_kernel(const float* __restrict__ A, int64_t m, int64_t n,
                                                            int64_t lda, float* __restrict__ AQ, int64_t ldq) {
     __shared__ float tile[64][65];
@@ -1412,8 +1418,8 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
     if (a_f32)
-        rowmajor_f32_kernel<<<ctx.sm_count, 256, 0, st>>>(static_cast<const float*>(A), m, n, lda,
-                                                          reinterpret_cast<float*>(AF), ldf);
+        rowmajor_f32_kernel<<<(unsigned)std::min<int64_t>(div_up(m, 64) * div_up(ldf, 64), 8 * ctx.sm_count), 256, 0,
+                              st>>>(static_cast<const float*>(A), m, n, lda, reinterpret_cast<float*>(AF), ldf);
     else
         rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,
                                                                     reinterpret_cast<float*>(AF), ldf);
@@ -1424,35 +1430,22 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     RNLA_LAUNCH_CHECK();
 }
 
-void lsqr_ff_reserve(Ctx& ctx, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in) {
+void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
+                     LsqrFFInput& in, bool on_main) {
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
-    in.m = m; in.n = n;
+    in.A = A; in.m = m; in.n = n;
     in.f32 = a_f32;
     // FP32 data: a row-major FP32 copy (ldf = n rounded up to 4 floats);
     // FP64 data: the float-float copy (ldf = n rounded up to 2 pairs)
     in.ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
     in.AF.alloc(a_f32 ? (size_t)m * in.ldf / 2 : (size_t)m * in.ldf, ctx.stream);
     in.bF.alloc(m, ctx.stream);
-    RNLA_CUDA(cudaEventCreateWithFlags(&in.start, cudaEventDisableTiming));
-    RNLA_CUDA(cudaEventRecord(in.start, ctx.stream));
-}
-
-void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
-                     LsqrFFInput& in) {
-    if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
-    const cudaStream_t side = side_stream(ctx.device);
-    if (in.start && in.m == m && in.n == n && in.f32 == a_f32) {
-        // buffers reserved earlier: build from that point on
-        RNLA_CUDA(cudaStreamWaitEvent(side, in.start, 0));
-    } else {
-        lsqr_ff_reserve(ctx, a_f32, m, n, in);
-        stream_wait(side, ctx.stream);             // buffers allocated, A and b written
-    }
-    in.A = A;
-    build_ff_input(ctx, side, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
+    const cudaStream_t st = on_main ? ctx.stream : side_stream(ctx.device);
+    if (!on_main) stream_wait(st, ctx.stream);     // buffers allocated, A and b written
+    build_ff_input(ctx, st, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
     RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     in.owner = ctx.stream;
-    RNLA_CUDA(cudaEventRecord(in.ready, side));
+    RNLA_CUDA(cudaEventRecord(in.ready, st));
 }
 
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,

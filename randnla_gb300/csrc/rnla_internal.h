@@ -2,6 +2,7 @@
 // Everything here works on device pointers, column-major storage, and is
 // enqueued on ctx.stream.
 #pragma once
+#include <functional>
 #include <vector>
 #include "rnla_common.cuh"
 #include "rnla_rng.cuh"
@@ -151,7 +152,6 @@ struct LsqrFFInput {
     bool f32 = false;               // AF holds FP32 rows (A stored in FP32)
     int64_t m = 0, n = 0, ldf = 0;
     cudaEvent_t ready = nullptr;
-    cudaEvent_t start = nullptr;    // set by lsqr_ff_reserve: the point the build may start from
     cudaStream_t owner = nullptr;   // stream the buffers are freed on
     LsqrFFInput() = default;
     LsqrFFInput(const LsqrFFInput&) = delete;
@@ -163,19 +163,16 @@ struct LsqrFFInput {
             cudaStreamWaitEvent(owner, ready, 0);
             cudaEventDestroy(ready);
         }
-        if (start) cudaEventDestroy(start);
     }
 };
 bool lsqr_ff_supported(int64_t n);
 // M (n x n upper) <- the FP64 value of its float-float split, so that the
 // float-float LSQR operator A M and a later FP64 product M z use the same M.
 void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm);
-// lsqr_ff_reserve allocates the copies on ctx.stream and records that point:
-// a later lsqr_ff_prepare then starts the build from there (A and b must
-// already be in place), so it can overlap work enqueued in between.
-void lsqr_ff_reserve(Ctx& ctx, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in);
+// on_main: build on ctx.stream itself (filling a wait of the main stream)
+// instead of the side stream.
 void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
-                     LsqrFFInput& in);
+                     LsqrFFInput& in, bool on_main = false);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
                          double* arnorms_dev, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
@@ -232,7 +229,7 @@ bool tc_available(Ctx& ctx);
 // of the product is started as soon as its columns are on the device.
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN);
+                     const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN, const std::function<void()>& before_mma = {});
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
 // ---- float-float tall-skinny products (gram_ff.cu) ----

@@ -54,6 +54,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstring>
+#include <functional>
 
 namespace rnla {
 
@@ -530,7 +531,8 @@ static size_t smem_bytes() {
 
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32, int64_t K, int64_t N0,
-                int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed) {
+                int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed,
+                const std::function<void()>& before_mma) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
     const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
     const size_t smem = smem_bytes<P>();
@@ -547,10 +549,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     // with a feed and a small S, each column tile is its own launch as its
     // columns arrive (below)
     const bool per_tile = feed && (double)tiles_m * Ks * S_BYTES * tiles_n <= 4.0e9;
-    // without a feed and with a large S, S is generated in two halves of its
-    // rows and the MMA runs once per half (below)
-    const bool halves = !feed && tiles_m >= 2 && (double)tiles_m * Ks * S_BYTES >= 1.0e9;
-    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : halves ? (int64_t)(tiles_m / 2) * tiles_n : tiles;
+    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : tiles;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -574,28 +573,15 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
     // the sketch generator (integer ALU bound) runs on the side stream while
-    // the main stream makes the digit planes (HBM bound).  Without a feed and
-    // with a large S the rows of S come in two halves: the MMA over the first
-    // half starts once it is written and the generator's second half runs
-    // beside it (the MMA CTAs leave the CUDA cores mostly idle)
+    // the main stream makes the digit planes (HBM bound)
     const cudaStream_t side = side_stream(ctx.device);
     stream_wait(side, ctx.stream);                 // the S buffer exists
-    const int h = halves ? tiles_m / 2 : tiles_m;
-    cudaEvent_t first_half = nullptr;
-    // (the second half runs beside the first MMA: about one block per SM, so
-    // that the MMA's CTAs find room next to it)
-    auto gen = [&](int it0, int cnt, bool beside) {
+    {
         int gx = div_up((int64_t)Ks * 1024, 256);
-        const int cap = beside ? std::max(1, sm / cnt) : 16 * sm / (cnt < 16 ? cnt : 16) + 1;
+        const int cap = 16 * sm / (tiles_m < 16 ? tiles_m : 16) + 1;
         if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)cnt), 256, 0, side>>>(key, dist, M, K, Ks, it0, sk);
+        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, 0, sk);
         RNLA_LAUNCH_CHECK();
-    };
-    gen(0, h, false);
-    if (halves) {
-        RNLA_CUDA(cudaEventCreateWithFlags(&first_half, cudaEventDisableTiming));
-        RNLA_CUDA(cudaEventRecord(first_half, side));
-        gen(h, tiles_m - h, true);
     }
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
@@ -630,24 +616,13 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     };
     if (!feed) {
         digits(0, tiles_n);
+        // the caller's main-stream work that only needs the inputs (the
+        // solver's row-major copy) fills the wait for the generator
+        if (before_mma) before_mma();
         prm.jt_only = -1;
-        if (halves) {
-            for (int part = 0; part < 2; ++part) {
-                if (part == 0) RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, first_half, 0));
-                else stream_wait(ctx.stream, side);         // all of S is written
-                prm.it0 = part == 0 ? 0 : h;
-                prm.it_count = part == 0 ? h : tiles_m - h;
-                prm.units = (int)((int64_t)prm.it_count * tiles_n * kc_count);
-                const unsigned gp = (unsigned)(prm.units < sm ? prm.units : sm);
-                kfn<<<gp, THREADS, smem, ctx.stream>>>(prm);
-                RNLA_LAUNCH_CHECK();
-            }
-            RNLA_CUDA(cudaEventDestroy(first_half));
-        } else {
-            stream_wait(ctx.stream, side);             // S is written
-            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
-            RNLA_LAUNCH_CHECK();
-        }
+        stream_wait(ctx.stream, side);                 // S is written
+        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+        RNLA_LAUNCH_CHECK();
     } else {
         // Each column tile's digit planes are made as soon as its columns
         // have landed.  The MMA runs per column tile too (overlapping the
@@ -892,16 +867,16 @@ bool tc_available(Ctx& ctx) {
 
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed, int dist) {
+                     const ColumnFeed* feed, int dist, const std::function<void()>& before_mma) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
     // default digits: 4 for FP64 data (32 bits below each column's maximum),
     // 3 for FP32 data (its 24-bit significands)
     if (digits <= 0) digits = x_f32 ? 3 : 4;
     switch (digits) {
-        case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 3: tc::run<3>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
-        case 4: tc::run<4>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed); break;
+        case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
+        case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
+        case 3: tc::run<3>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
+        case 4: tc::run<4>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
         default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..4");
     }
 }
