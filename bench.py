@@ -87,7 +87,7 @@ def parse(argv=None):
     p.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison path")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) leg")
-    p.add_argument("--problems", type=int, default=512, help="problems in the batched workload")
+    p.add_argument("--problems", type=int, default=2048, help="problems in the batched workload")
     p.add_argument("--cpu-leg", choices=["port", "lapack"], default=None, help=argparse.SUPPRESS)
     return p.parse_args(argv)
 

@@ -384,13 +384,18 @@ typedef struct {
 /* Many independent blendenpik_overdetermined solves
  * (sketch_and_precondition.rs:26-59 per problem; the reference has no
  * batched entry, callers loop) with shared epsilon, l, sampling_factor and
- * options, queued on one stream.  Each problem's x is exactly what
- * rnla_blendenpik_overdetermined_dev gives for it alone (same sketch seed,
- * same kernels).  status_out (count entries, required) receives each
- * problem's status, stats_out (nullable, count entries) its facts.  Returns
- * RNLA_OK when every problem succeeded, else the first failing problem's
- * status (its message in rnla_last_error_message); a CUDA error stops the
- * batch and marks the problems not yet run RNLA_ERR_CUDA.  Synchronises. */
+ * options.  The problems' data must be in place in `stream` order; the
+ * batch runs on four workers (host threads, each with its own streams and
+ * grids sized for a quarter of the SMs) that take problems in index order,
+ * so small problems run side by side.  Each x matches what
+ * rnla_blendenpik_overdetermined_dev gives for the problem alone to the
+ * solver's accuracy (same sketch seed and kernels; the smaller grids group
+ * partial sums differently).  status_out (count entries, required) receives
+ * each problem's status, stats_out (nullable, count entries) its facts.
+ * Returns RNLA_OK when every problem succeeded, else the lowest-index
+ * failing problem's status (its message in rnla_last_error_message); a
+ * CUDA error stops the batch and marks the problems not yet run
+ * RNLA_ERR_CUDA.  Synchronises. */
 RNLA_API int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsilon, int64_t l,
                                 double sampling_factor, const rnla_options* opt, int32_t* status_out,
                                 rnla_stats* stats_out, void* stream);

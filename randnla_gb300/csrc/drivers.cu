@@ -1,9 +1,13 @@
 // C entry points of the hot path: solvers.rs, cg.rs, lora_helpers.rs,
 // lora_drivers.rs and sketch_and_precondition.rs, orchestrated on the GPU.
 #include "rnla_abi.h"
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace rnla {
@@ -1224,41 +1228,88 @@ int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsil
         return abi_error(RNLA_ERR_INVALID_PARAMETERS, "probs and status_out are required");
     if (count == 0) return abi_ok();
     rnla_options o;
+    int dev = 0, sms = 0;
     try {
         o = opts_or_default(opt);
+        RNLA_CUDA(cudaGetDevice(&dev));
+        RNLA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     } catch (const Error& e) {
         return abi_error(e.code, e.what());
     }
+    // Small problems leave most of the GPU idle (their QR and LSQR are chains
+    // of grid barriers and cross-SM hand-offs), so the batch runs as W
+    // workers, each a host thread with its own main and side streams and grids
+    // sized for sms / W SMs, taking the next problem from a shared counter.
+    const int W = (int)std::min<int64_t>(count, batched_workers());
+    std::vector<cudaStream_t> main_s(W), side_s(W);
+    cudaEvent_t inputs = nullptr;
+    try {
+        for (int w = 0; w < W; ++w) {
+            main_s[w] = worker_stream(dev, 2 * w);
+            side_s[w] = worker_stream(dev, 2 * w + 1);
+        }
+        // the problems' data were written on the caller's stream
+        RNLA_CUDA(cudaEventCreateWithFlags(&inputs, cudaEventDisableTiming));
+        RNLA_CUDA(cudaEventRecord(inputs, (cudaStream_t)stream));
+        for (int w = 0; w < W; ++w) RNLA_CUDA(cudaStreamWaitEvent(main_s[w], inputs, 0));
+        RNLA_CUDA(cudaEventDestroy(inputs));
+    } catch (const Error& e) {
+        return abi_error(e.code, e.what());
+    }
+    std::atomic<int64_t> next{0};
+    std::atomic<bool> dead{false};
+    std::mutex mu;
     int first = RNLA_OK;
+    int64_t first_p = -1;
     std::string first_msg;
-    for (int64_t p = 0; p < count; ++p) {
-        const rnla_ls_problem& q = probs[p];
-        rnla_stats* st = stats_out ? stats_out + p : nullptr;
-        if (st) memset(st, 0, sizeof *st);
-        int rc = RNLA_OK;
-        std::string msg;
-        try {
-            check_mat(q.m, q.n, q.lda);
-            if (!q.a || !q.b || !q.x) fail(RNLA_ERR_INVALID_PARAMETERS, "problem with a null pointer");
-            Ctx ctx((cudaStream_t)stream);
-            blendenpik_impl(ctx, q.a, q.a_is_f32 != 0, q.m, q.n, q.lda, q.b, epsilon, l, sampling_factor, o,
-                            q.x, st);
-        } catch (const Error& e) {
-            rc = e.code;
-            msg = e.what();
-        } catch (const std::bad_alloc&) {
-            rc = RNLA_ERR_COMPUTATION;
-            msg = "host allocation failed";
+    auto work = [&](int w) {
+        cudaSetDevice(dev);
+        for (;;) {
+            const int64_t p = next.fetch_add(1);
+            if (p >= count) break;
+            if (dead.load()) {
+                status_out[p] = RNLA_ERR_CUDA;
+                continue;
+            }
+            const rnla_ls_problem& q = probs[p];
+            rnla_stats* st = stats_out ? stats_out + p : nullptr;
+            if (st) memset(st, 0, sizeof *st);
+            int rc = RNLA_OK;
+            std::string msg;
+            try {
+                check_mat(q.m, q.n, q.lda);
+                if (!q.a || !q.b || !q.x) fail(RNLA_ERR_INVALID_PARAMETERS, "problem with a null pointer");
+                Ctx ctx(main_s[w]);
+                ctx.side = side_s[w];
+                ctx.sm_count = std::max(1, sms / W);
+                blendenpik_impl(ctx, q.a, q.a_is_f32 != 0, q.m, q.n, q.lda, q.b, epsilon, l, sampling_factor, o,
+                                q.x, st);
+            } catch (const Error& e) {
+                rc = e.code;
+                msg = e.what();
+            } catch (const std::bad_alloc&) {
+                rc = RNLA_ERR_COMPUTATION;
+                msg = "host allocation failed";
+            }
+            status_out[p] = rc;
+            if (rc != RNLA_OK) {
+                std::lock_guard<std::mutex> g(mu);
+                if (first_p < 0 || p < first_p) {
+                    first = rc;
+                    first_p = p;
+                    first_msg = "problem " + std::to_string(p) + ": " + msg;
+                }
+                if (rc == RNLA_ERR_CUDA) dead.store(true);
+            }
         }
-        status_out[p] = rc;
-        if (rc != RNLA_OK && first == RNLA_OK) {
-            first = rc;
-            first_msg = "problem " + std::to_string(p) + ": " + msg;
-        }
-        if (rc == RNLA_ERR_CUDA) {
-            for (int64_t r = p + 1; r < count; ++r) status_out[r] = RNLA_ERR_CUDA;
-            return abi_error(first, first_msg.c_str());
-        }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < W; ++w) pool.emplace_back(work, w);
+    work(0);
+    for (auto& t : pool) t.join();
+    for (int w = 0; w < W; ++w) {
+        const cudaError_t e = cudaStreamSynchronize(main_s[w]);
+        if (e != cudaSuccess) return abi_error(RNLA_ERR_CUDA, cudaGetErrorString(e));
     }
     const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
     if (e != cudaSuccess) return abi_error(RNLA_ERR_CUDA, cudaGetErrorString(e));

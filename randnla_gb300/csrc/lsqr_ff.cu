@@ -1440,7 +1440,7 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
     in.ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
     in.AF.alloc(a_f32 ? (size_t)m * in.ldf / 2 : (size_t)m * in.ldf, ctx.stream);
     in.bF.alloc(m, ctx.stream);
-    const cudaStream_t st = on_main ? ctx.stream : side_stream(ctx.device);
+    const cudaStream_t st = on_main ? ctx.stream : (ctx.side ? ctx.side : side_stream(ctx.device));
     if (!on_main) stream_wait(st, ctx.stream);     // buffers allocated, A and b written
     build_ff_input(ctx, st, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
     RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));

@@ -41,8 +41,9 @@ void count_launch();
 // Per-call context: stream plus device facts used for grid sizing.
 struct Ctx {
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;      // side stream of this context (null: the device's shared one)
     int device = 0;
-    int sm_count = 0;
+    int sm_count = 0;                 // SMs the grids are sized for (a batched worker takes a share)
     unsigned int* status = nullptr;   // device word: nonzero = kernel-side failure code
     // Deferred mode: the status word is not cleared between kernels (the
     // first failure code sticks, and later kernels that poll it stop early)
@@ -92,6 +93,8 @@ struct DevBuf {
 
 // Second stream of a device, and an event-based dependency `to` -> `from`.
 cudaStream_t side_stream(int device);
+cudaStream_t worker_stream(int device, int idx);
+int batched_workers();
 cudaStream_t copy_stream(int device);
 void stream_wait(cudaStream_t to, cudaStream_t from);
 

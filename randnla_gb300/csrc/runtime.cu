@@ -90,6 +90,22 @@ cudaStream_t side_stream(int dev) {
     return device_stream(cache, mu, dev);
 }
 
+// Streams of the batched solver's workers: index 2 w (main) and 2 w + 1
+// (side) of worker w, created on first use and kept.
+cudaStream_t worker_stream(int dev, int idx) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, cudaStream_t> cache;
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find({dev, idx});
+    if (it != cache.end()) return it->second;
+    cudaStream_t st = nullptr;
+    RNLA_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cache[{dev, idx}] = st;
+    return st;
+}
+
+int batched_workers() { return 4; }
+
 cudaStream_t copy_stream(int dev) {
     static std::mutex mu;
     static std::map<int, cudaStream_t> cache;

@@ -574,7 +574,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
     // the sketch generator (integer ALU bound) runs on the side stream while
     // the main stream makes the digit planes (HBM bound)
-    const cudaStream_t side = side_stream(ctx.device);
+    const cudaStream_t side = (ctx.side ? ctx.side : side_stream(ctx.device));
     stream_wait(side, ctx.stream);                 // the S buffer exists
     {
         int gx = div_up((int64_t)Ks * 1024, 256);
