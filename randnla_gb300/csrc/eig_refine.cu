@@ -1,4 +1,4 @@
-// Eigenvectors of a small SPD Gram G = B B^T (p x p, 64 <= p <= 320) for the
+// Eigenvectors of a small SPD Gram G = B B^T (p x p, 2 <= p <= 320) for the
 // Gram-based small SVD of the tensor-core rand_svd, in two stages:
 //
 //  1. one-sided Jacobi in FP32 on W = R^T (R = chol(G)) on one thread-block
@@ -222,7 +222,7 @@ __global__ void order_kernel(const double* __restrict__ H, const double* __restr
 bool eig_gram_refined(Ctx& ctx, const double* G, const double* R, int64_t p, double* UB, int64_t ldu, double* sigma,
                       int* sweeps) {
     using namespace eigr;
-    if (p < 64 || p > PMAX) return false;
+    if (p < 2 || p > PMAX) return false;
     DevBuf<float> W32((size_t)p * p, ctx.stream);
     int g = div_up(p * p, 256);
     if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
@@ -235,11 +235,9 @@ bool eig_gram_refined(Ctx& ctx, const double* G, const double* R, int64_t p, dou
         const size_t smem = (size_t)cw * p * sizeof(float) + 16;
         const int npairs = (int)((p + 1) / 2);
         const int nwarps = (npairs + JC - 1) / JC;
-        RNLA_CUDA(cudaFuncSetAttribute(jacobi_f32_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+        set_smem_limit((const void*)jacobi_f32_cluster_kernel, smem);
         jacobi_f32_cluster_kernel<<<JC, 32 * nwarps, smem, ctx.stream>>>(W32, (int)p, 40, nsw);
         RNLA_LAUNCH_CHECK();
-        count_launch();
     }
     const size_t pp = (size_t)p * p;
     DevBuf<double> U(pp, ctx.stream), Ut(pp, ctx.stream), S(pp, ctx.stream), T(pp, ctx.stream), H(pp, ctx.stream),

@@ -283,7 +283,7 @@ void householder_qr(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, int64
                           : own == 2 ? (const void*)hh_qr_flag_kernel<2>
                           : own == 3 ? (const void*)hh_qr_flag_kernel<3>
                                      : (const void*)hh_qr_flag_kernel<4>;
-            RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            set_smem_limit((const void*)k, smem);
             int nb = 0;
             RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, smem));
             if ((int64_t)nb * ctx.sm_count >= G) {
@@ -387,8 +387,7 @@ bool upper_inverse(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double* Ri
     RNLA_CUDA(cudaMemsetAsync(ctx.status, 0, sizeof(unsigned int), ctx.stream));
     const size_t smem = (size_t)n * sizeof(double);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(upper_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+        set_smem_limit((const void*)upper_inverse_kernel, smem);
     upper_inverse_kernel<<<(unsigned)n, 256, smem, ctx.stream>>>(R, n, ldr, Rinv, ldi, ctx.status);
     RNLA_LAUNCH_CHECK();
     unsigned int h = 0;
@@ -428,8 +427,7 @@ void upper_solve_skip_zero(Ctx& ctx, const double* U, int64_t n, int64_t ldu, co
     if (n <= 0) return;
     const size_t smem = (size_t)n * sizeof(double);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(upper_solve_skip_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)upper_solve_skip_kernel, smem);
     upper_solve_skip_kernel<<<1, 256, smem, ctx.stream>>>(U, n, ldu, y, x);
     RNLA_LAUNCH_CHECK();
 }
@@ -1096,7 +1094,7 @@ bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb
     jacobi_sweeps(ctx, W, p < 64 ? VR.get() : nullptr, p, nsw);
     const size_t smem = (size_t)p * sizeof(double);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)jacobi_finish_kernel, smem);
     jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, nullptr, (int)p, VS, nullptr, sg, order);
     RNLA_LAUNCH_CHECK();
     unsigned int hsw = 0;
@@ -1129,8 +1127,7 @@ void small_svd(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, dou
     DevBuf<int> order(s, ctx.stream);
     const size_t smem = (size_t)s * sizeof(double);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(jacobi_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
+        set_smem_limit((const void*)jacobi_finish_kernel, smem);
     jacobi_finish_kernel<<<1, 256, smem, ctx.stream>>>(W, VR, (int)s, UR, VS, sigma, order);
     RNLA_LAUNCH_CHECK();
     // G = QG R = (QG UR) diag(sigma) VS^T

@@ -360,11 +360,11 @@ void bfx_planes(Ctx& ctx, BfxPlanes& P, const void* src, bool f32, int64_t R, in
     const unsigned blocks = (unsigned)((int64_t)P.tiles * P.Ks);
     if (f32) {
         auto k = planes_kernel<float>;
-        RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)k, smem);
         k<<<blocks, 256, smem, ctx.stream>>>(static_cast<const float*>(src), R, K, sr, sk, TR, P.Ks, planes, P.buf);
     } else {
         auto k = planes_kernel<double>;
-        RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)k, smem);
         k<<<blocks, 256, smem, ctx.stream>>>(static_cast<const double*>(src), R, K, sr, sk, TR, P.Ks, planes, P.buf);
     }
     RNLA_LAUNCH_CHECK();
@@ -403,11 +403,10 @@ static void run(Ctx& ctx, const BfxPlanes& X, const BfxPlanes& Y, double* C, int
     prm.xp = X.buf; prm.yp = Y.buf; prm.partial = part; prm.status = ctx.status;
     const size_t smem = 1024 + (size_t)STAGES * (L * XT_BYTES + L * BN * BK * 2) + 256;
     auto kfn = bfx_gemm_kernel<L>;
-    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set_smem_limit((const void*)kfn, smem);
     ctx.clear_status();
     kfn<<<(unsigned)std::min<int64_t>(units, sm), THREADS, smem, ctx.stream>>>(prm);
     RNLA_LAUNCH_CHECK();
-    count_launch();
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
     bfx_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, BN, M, N, trans ? 1 : 0, C, ldc);

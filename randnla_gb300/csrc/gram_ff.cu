@@ -153,7 +153,6 @@ void gram_ff(Ctx& ctx, const double* X, int64_t ldx, int64_t N1, const double* Y
     gram_ff_kernel<<<dim3((unsigned)tiles, (unsigned)chunks), THREADS, 0, ctx.stream>>>(X, ldx, N1, Y, ldy, N2, K, rpc,
                                                                                    tiles1, sym, part);
     RNLA_LAUNCH_CHECK();
-    count_launch();
     int g = div_up(N1 * N2, 256);
     if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
     gram_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, chunks, tiles1, tiles, sym, N1, N2, C, ldc);

@@ -912,7 +912,7 @@ struct IterBufs {
 
 static int coop_grid(Ctx& ctx, const void* kernel, size_t smem) {
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)kernel, smem);
     int nb = 0;
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, IT_THREADS, smem));
     if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "iterative kernel does not fit on an SM");
@@ -1067,7 +1067,7 @@ size_t lsqr_workspace_bytes(int64_t m, int64_t n, int sm_count, int* grid, size_
     int64_t red_off = 0;
     const size_t smem = iter_smem(mode, n, pick_R(n), red_off);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)k, smem);
     int nb = 0;
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, IT_THREADS, smem));
     if (nb < 1) fail(RNLA_ERR_UNSUPPORTED, "iterative kernel does not fit on an SM");

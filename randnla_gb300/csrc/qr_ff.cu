@@ -500,7 +500,7 @@ void householder_qr_ff(Ctx& ctx, double* X, int64_t m, int64_t n, int64_t nc, in
     const int64_t G = nblk < ctx.sm_count ? nblk : ctx.sm_count;
     const size_t smem = qr_ff_smem(ownb, m);
     const void* k = ownb == 1 ? qr_kernel<1>() : ownb == 2 ? qr_kernel<2>() : ownb == 3 ? qr_kernel<3>() : qr_kernel<4>();
-    RNLA_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set_smem_limit((const void*)k, smem);
     int nb = 0;
     RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, T, smem));
     if ((int64_t)nb * ctx.sm_count < G) fail(RNLA_ERR_UNSUPPORTED, "float-float QR: grid not co-resident");
@@ -572,7 +572,7 @@ bool upper_inverse_ff(Ctx& ctx, const double* R, int64_t n, int64_t ldr, double*
     if (n > TI * 8) fail(RNLA_ERR_UNSUPPORTED, "float-float R^-1: n > 1024");
     const size_t smem = (size_t)2 * n * sizeof(float2);
     if (smem > 48 * 1024)
-        RNLA_CUDA(cudaFuncSetAttribute(rinv_ff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        set_smem_limit((const void*)rinv_ff_kernel, smem);
     // a zero pivot is reported through the status word (KSTATUS_SINGULAR):
     // at once, or at the pending check in deferred mode
     ctx.clear_status();

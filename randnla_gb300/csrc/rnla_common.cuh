@@ -95,6 +95,7 @@ struct DevBuf {
 cudaStream_t side_stream(int device);
 cudaStream_t worker_stream(int device, int idx);
 int batched_workers();
+void set_smem_limit(const void* fn, size_t bytes);
 cudaStream_t copy_stream(int device);
 void stream_wait(cudaStream_t to, cudaStream_t from);
 

@@ -83,7 +83,7 @@ void jacobi_sweeps(Ctx& ctx, double* W, double* V, int64_t s, unsigned int* swee
 // small_svd) when the Cholesky fails or sigma_p / sigma_1 < 1e-5.
 bool small_svd_gram(Ctx& ctx, const double* B, int64_t p, int64_t q, int64_t ldb, double* U, int64_t ldu,
                     double* sigma, double* V, int64_t ldv, int* sweeps = nullptr);
-// Eigenvectors of the p x p SPD G (64 <= p <= 320) with R = chol(G): FP32
+// Eigenvectors of the p x p SPD G (2 <= p <= 320) with R = chol(G): FP32
 // cluster Jacobi on R^T, float-float Rayleigh-Ritz refinement (eig_refine.cu).
 // UB (ld ldu) and sigma = sqrt(eigenvalues) in descending order; false when
 // the refinement does not converge (nothing kept).

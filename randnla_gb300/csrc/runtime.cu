@@ -106,6 +106,20 @@ cudaStream_t worker_stream(int dev, int idx) {
 
 int batched_workers() { return 4; }
 
+// The dynamic shared-memory limit of a kernel only ever grows: concurrent
+// callers (the batched solver's workers) launching one kernel with different
+// sizes must never see the limit lowered under them between their own
+// setting and their launch.
+void set_smem_limit(const void* fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<const void*, size_t> cur;
+    std::lock_guard<std::mutex> g(mu);
+    size_t& c = cur[fn];
+    if (bytes <= c) return;
+    RNLA_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    c = bytes;
+}
+
 cudaStream_t copy_stream(int dev) {
     static std::mutex mu;
     static std::map<int, cudaStream_t> cache;

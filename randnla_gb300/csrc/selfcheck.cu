@@ -62,11 +62,11 @@ extern "C" int rnla_check_bounded_wait(int32_t which, int64_t limit_us, void* st
         void* args[] = {&bar, (void*)&limit_ns, &arrived};
         RNLA_CUDA(cudaLaunchCooperativeKernel((const void*)barrier_expiry_kernel, dim3(ctx.sm_count), dim3(128),
                                               args, 0, ctx.stream));
+        count_launch();
     } else {
         mbar_expiry_kernel<<<1, 32, 0, ctx.stream>>>(limit_ns, ctx.status);
         RNLA_LAUNCH_CHECK();
     }
-    count_launch();
     unsigned int passed = 0;
     RNLA_CUDA(cudaMemcpyAsync(&passed, words.get() + 2, sizeof passed, cudaMemcpyDeviceToHost, ctx.stream));
     RNLA_CUDA(cudaStreamSynchronize(ctx.stream));

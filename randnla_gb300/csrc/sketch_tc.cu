@@ -591,7 +591,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
     auto kfn = sketch_mma_kernel<P>;
-    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set_smem_limit((const void*)kfn, smem);
     const unsigned grid = (unsigned)(units < sm ? units : sm);
     // exponents and digit planes of column tiles [jt0, jt0 + cnt)
     auto digits = [&](int jt0, int cnt) {
@@ -757,10 +757,9 @@ static void launch_mma(Ctx& ctx, const tc::Params& prm, unsigned grid) {
     using namespace tc;
     const size_t smem = smem_bytes<P>();
     auto kfn = sketch_mma_kernel<P>;
-    RNLA_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set_smem_limit((const void*)kfn, smem);
     kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
     RNLA_LAUNCH_CHECK();
-    count_launch();
 }
 
 void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int64_t ldx, const double* Y,
