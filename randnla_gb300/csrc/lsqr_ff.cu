@@ -627,29 +627,21 @@ __device__ bool ff_pass_fused(const Args& a, Ring& rg, float4* scratch, float2 c
 // a * y_hi (one multiply-add fewer than a float-float element).  Everything
 // else -- ring, row ownership, u, the per-warp column sums -- is as in
 // ff_pass_fused.
-template <int KC, int RW, int HV>
+template <int KC, int RW>
 __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, float2 c1, float2 c2, float2 c3,
                                   bool dot, const float2* oldv, const float2* bvec, float2* dst, bool want_b2,
                                   bool acc_at, volatile int* err) {
     constexpr int R = WF * RW;
     constexpr int KP = 2 * KC;
     __shared__ float2 wred[WF][2];
-    // HV = 2: sixteen warps, the two of pair pw = warp & 7 sharing its rows,
-    // half hh = warp >> 3 taking chunks [hh 32 KC, (hh + 1) 32 KC) of each
-    // row; their partial row dots meet in shared memory (one named barrier of
-    // the pair per tile, double-buffered slots)
-    __shared__ float2 pdot[2][2][WF][RW];
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int warp = (HV == 2) ? ((tid >> 5) & (WF - 1)) : (tid >> 5);
-    const int hh = (HV == 2) ? (tid >> 8) : 0;
-    const int cb = hh * 32 * KC;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int hp = (int)a.hp;
     const int hq = (int)a.rowq;
     const int64_t ntl = rg.ntl;
     f32x2 yh[KP], yl[KP];
 #pragma unroll
     for (int kk = 0; kk < KC; ++kk) {
-        const int c = cb + lane + 32 * kk;
+        const int c = lane + 32 * kk;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             float2 y0 = make_float2(0.f, 0.f), y1 = make_float2(0.f, 0.f);
@@ -699,11 +691,11 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
             const bool rv = ok && r < rows;
 #pragma unroll
             for (int kk = 0; kk < KC; ++kk) {
-                const int c = cb + lane + 32 * kk;
+                const int c = lane + 32 * kk;
                 v[w][kk] = (rv && c < hq) ? tile[(size_t)r * hq + c] : make_ulonglong2(0ull, 0ull);
             }
         }
-        ring_release(a, rg, st, lane, err, WF * HV);
+        ring_release(a, rg, st, lane, err);
         float tvh[RW], tvl[RW];
 #pragma unroll
         for (int w = 0; w < RW; ++w) { tvh[w] = 0.f; tvl[w] = 0.f; }
@@ -749,26 +741,13 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
                 const float ol = __shfl_xor_sync(0xffffffffu, tvl[0], off);
                 ff_acc(tvh[0], tvl[0], oh, ol);
             }
-            if constexpr (HV == 2) {
-                // the two halves of each row, added in half order by both warps
-                const int buf = (int)(k & 1);
-                if (owner) pdot[buf][hh][warp][rw] = make_float2(tvh[0], tvl[0]);
-                asm volatile("bar.sync %0, 64;" ::"r"(1 + warp) : "memory");
-                if (owner) {
-                    const float2 p0 = pdot[buf][0][warp][rw], p1 = pdot[buf][1][warp][rw];
-                    float h = p0.x, l = p0.y;
-                    ff_acc(h, l, p1.x, p1.y);
-                    tvh[0] = h;
-                    tvl[0] = l;
-                }
-            }
         }
         float2 nv = make_float2(0.f, 0.f);
         if (owner) {
             const float2 tv = ff_norm(tvh[0], tvl[0]);
             nv = ff_add(ff_add(ff_mul(c1, tv), ff_mul(c2, uo)), ff_mul(c3, bb));
             const int r = warp + WF * rw;
-            if (ok && r < rows && hh == 0) {
+            if (ok && r < rows) {
                 dst[r0 + r] = nv;
                 ff_madd(nv.x, nv.y, nv.x, nv.y, sqh, sql);
                 if (want_b2) ff_madd(bb.x, bb.y, bb.x, bb.y, b2h, b2l);
@@ -795,15 +774,14 @@ __device__ bool ff_pass_fused_f32(const Args& a, Ring& rg, float4* scratch, floa
     }
     const float2 sq = ff_warp_sum(sqh, sql);
     const float2 b2 = ff_warp_sum(b2h, b2l);
-    if (lane == 0 && hh == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
+    if (lane == 0) { wred[warp][0] = sq; wred[warp][1] = b2; }
     if (acc_at) {
         // each warp's column sums go straight to its own row of partF (no
-        // shared-memory scratch: the ring gets that space); the two warps of
-        // a pair fill the two halves of one row
+        // shared-memory scratch: the ring gets that space)
         float4* P4 = reinterpret_cast<float4*>(a.partF) + ((size_t)blockIdx.x * WF + warp) * hp;
 #pragma unroll
         for (int kk = 0; kk < KC; ++kk) {
-            const int c = cb + lane + 32 * kk;
+            const int c = lane + 32 * kk;
             if (c < hq) {
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
@@ -935,11 +913,10 @@ __device__ __forceinline__ double shfl_d(double v, int src) { return __shfl_sync
 
 // FUSED selects the pass: fused roles on TF threads, or split row/column
 // roles on T threads.
-// F32: 0 = float-float rows; 1 = FP32 rows, 8 warps; 2 = FP32 rows, 16 warps
-// in column halves (ff_pass_fused_f32)
+// F32: 0 = float-float rows, 1 = FP32 rows (ff_pass_fused_f32)
 template <int KP, int RW, bool FUSED, int F32 = 0>
-__global__ void __launch_bounds__(F32 == 2 ? 2 * TF : (FUSED ? TF : T), 1) lsqr_ff_kernel(Args a) {
-    constexpr int NT = F32 == 2 ? 2 * TF : (FUSED ? TF : T);
+__global__ void __launch_bounds__(FUSED ? TF : T, 1) lsqr_ff_kernel(Args a) {
+    constexpr int NT = FUSED ? TF : T;
     constexpr int NWC = NT / 32;
     extern __shared__ __align__(128) unsigned char dsm[];
     __shared__ __align__(8) uint64_t full[MAX_ST];
@@ -1017,7 +994,7 @@ __global__ void __launch_bounds__(F32 == 2 ? 2 * TF : (FUSED ? TF : T), 1) lsqr_
 #define LSFF_PASS(...)                                                                 \
     do {                                                                               \
         bool pass_ok;                                                                  \
-        if constexpr (F32 != 0) pass_ok = ff_pass_fused_f32<KP / 2, RW, F32>(a, rg, scratch, __VA_ARGS__, err); \
+        if constexpr (F32 != 0) pass_ok = ff_pass_fused_f32<KP / 2, RW>(a, rg, scratch, __VA_ARGS__, err); \
         else if constexpr (FUSED) pass_ok = ff_pass_fused<KP, RW>(a, rg, scratch, __VA_ARGS__, err); \
         else pass_ok = ff_pass<KP, RW>(a, rg, usm, __VA_ARGS__, err);                  \
         if (!pass_ok) {                                                                \
@@ -1415,8 +1392,7 @@ static KernelPick pick_kernel_f32(int64_t hq) {
     if (hq <= 32) return {kernel_kp<2, 8, true, 1>(), WF * 8, TF, true};
     if (hq <= 64) return {kernel_kp<4, 4, true, 1>(), WF * 4, TF, true};
     if (hq <= 128) return {kernel_kp<8, 4, true, 1>(), WF * 4, TF, true};
-    // n > 512: two warps per row (column halves), 16 warps per CTA
-    return {kernel_kp<8, 1, true, 2>(), WF * 1, 2 * TF, true};
+    return {kernel_kp<16, 2, true, 1>(), WF * 2, TF, true};
 }
 
 }  // namespace lsff

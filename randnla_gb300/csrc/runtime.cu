@@ -104,7 +104,7 @@ cudaStream_t worker_stream(int dev, int idx) {
     return st;
 }
 
-int batched_workers() { return 4; }
+int batched_workers() { return 8; }
 
 // The dynamic shared-memory limit of a kernel only ever grows: concurrent
 // callers (the batched solver's workers) launching one kernel with different
