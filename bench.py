@@ -13,12 +13,21 @@ dataset is involved):
   plain_ls                A of 100000 x 500 in FP64, sigma 1 -> 1e-8
                           (kappa 1e8), b = A x* + 1e-6 N(0,1), d = 2000,
                           LSQR to tolerance 1e-12.
-  batched                 many independent problems of mixed shape through
-                          one rnla_solve_batched call per step.
+  precision_svd           rand_svd (RandNLA mode, tensor cores) of A of
+                          65536 x 16384 stored in FP32, sigma_i = exp(-i/64)
+                          on rank 1536 plus a 1e-6 noise floor; k = 256,
+                          p = 32, q = 2.
+  plain_svd               rand_svd of A of 2000 x 1000 (FP64, sigma_i =
+                          10^(-i/100)); k = 50, p = 10, q = 2.
+  batched                 2048 independent least-squares problems of mixed
+                          shape (m in [1000, 50000], n in [16, 256],
+                          m >= 8 n, kappa 1e6) through one rnla_solve_batched
+                          call per step.
 
-One step = one blendenpik solve (sketch S [A b], QR of the sketch, R^-1,
-preconditioned LSQR, x = R^-1 z) through the library's device-pointer entry
-point.  `value` is solves/s with inputs resident in HBM; `e2e` is the same
+One least-squares step = one blendenpik solve (sketch S [A b], factorization
+of the sketch, R^-1, preconditioned LSQR, x = R^-1 z) through the library's
+device-pointer entry point; one rand_svd step = one rand_svd through
+rnla_rand_svd_dev.  `value` is solves/s with inputs resident in HBM; `e2e` is the same
 metric through the host-pointer entry point with pinned host buffers (A and b
 copied in, x copied out inside the timed region).  A is larger than L2 in
 every workload, so no flush is needed between steps.
@@ -29,7 +38,7 @@ sampling, no extrapolation; each CPU solve runs in a subprocess with a
 10-minute cap and is reported as "not finished (cap)" if it exceeds it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload precision_ls|plain_ls|batched]
+                    [--workload precision_ls|plain_ls|precision_svd|plain_svd|batched]
 
 With N > 1 (torchrun) every rank solves its own replica (the path has no
 exchange step); value = all ranks' solves / max-over-ranks time.

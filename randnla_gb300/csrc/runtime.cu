@@ -38,6 +38,11 @@ static cudaMemPool_t device_pool(int dev) {
     RNLA_CUDA(cudaMemPoolCreate(&pool, &props));
     uint64_t thresh = ~0ull;
     RNLA_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thresh));
+    // memory freed on one stream is reused on another only through event
+    // dependencies the library made itself: the pool must not insert waits
+    // between unrelated streams (the batched solver's workers would serialise)
+    int no = 0;
+    RNLA_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no));
     pools[dev] = pool;
     return pool;
 }
@@ -104,7 +109,7 @@ cudaStream_t worker_stream(int dev, int idx) {
     return st;
 }
 
-int batched_workers() { return 8; }
+int batched_workers() { return 4; }
 
 // The dynamic shared-memory limit of a kernel only ever grows: concurrent
 // callers (the batched solver's workers) launching one kernel with different

@@ -224,10 +224,14 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                     }
                     mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YD_BYTES));
                     bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
-#pragma unroll
-                    for (int p = 0; p < P; ++p)
-                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * prm.ypl + p) * YD_BYTES, YD_BYTES,
-                                 &full[slot]);
+                    // the P digit tiles of a stage are adjacent in HBM and in the ring: one copy
+                    bulk_g2s(sY + slot * P * YD_BYTES, yd + (size_t)i * prm.ypl * YD_BYTES, (uint32_t)(P * YD_BYTES),
+                             &full[slot]);
+                    // the tiles one ring depth further on, into L2, so that copy meets L2 rather than DRAM
+                    if (i + STAGES < w.nst) {
+                        bulk_prefetch_l2(sk + (size_t)(i + STAGES) * S_BYTES, S_BYTES);
+                        bulk_prefetch_l2(yd + (size_t)(i + STAGES) * prm.ypl * YD_BYTES, (uint32_t)(P * YD_BYTES));
+                    }
                     ++g;
                 }
             }
