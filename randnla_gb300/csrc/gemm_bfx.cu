@@ -159,11 +159,6 @@ __global__ void __launch_bounds__(THREADS, 1) bfx_gemm_kernel(const Params prm) 
                     mbar_expect_tx(&full[slot], (uint32_t)(XS_BYTES + YS_BYTES));
                     bulk_g2s(sX + slot * XS_BYTES, xs + (size_t)i * prm.px * XT_BYTES, XS_BYTES, &full[slot]);
                     bulk_g2s(sY + slot * YS_BYTES, ys + (size_t)i * prm.py * YT_BYTES, YS_BYTES, &full[slot]);
-                    // one ring depth ahead into L2
-                    if (i + STAGES < w.nst) {
-                        bulk_prefetch_l2(xs + (size_t)(i + STAGES) * prm.px * XT_BYTES, XS_BYTES);
-                        bulk_prefetch_l2(ys + (size_t)(i + STAGES) * prm.py * YT_BYTES, YS_BYTES);
-                    }
                     ++g;
                 }
             }

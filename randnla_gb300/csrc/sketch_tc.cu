@@ -86,7 +86,7 @@ struct Params {
     int64_t M, N, K;          // C is M x N, reduction length K
     int tiles_m, tiles_n, Ks, kc_count, stages_per_kc;
     int units;                // work units of this launch
-    int jt_only;              // >= 0: only column tile jt_only (units = tiles_m * kc_count)
+    int jt0, jt_count;        // the column tiles [jt0, jt0 + jt_count) of this launch
     int it0, it_count;        // the row tiles [it0, it0 + it_count) of this launch
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
     const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
@@ -150,14 +150,8 @@ struct Unit {
 };
 __device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
     Unit w;
-    int rest;
-    if (prm.jt_only >= 0) {
-        w.jt = prm.jt_only;
-        rest = u;
-    } else {
-        w.jt = u % prm.tiles_n;
-        rest = u / prm.tiles_n;
-    }
+    w.jt = prm.jt0 + u % prm.jt_count;
+    const int rest = u / prm.jt_count;
     w.it = prm.it0 + rest % prm.it_count;
     w.kc = rest / prm.it_count;
     w.s_begin = w.kc * prm.stages_per_kc;
@@ -224,14 +218,10 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                     }
                     mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YD_BYTES));
                     bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
-                    // the P digit tiles of a stage are adjacent in HBM and in the ring: one copy
-                    bulk_g2s(sY + slot * P * YD_BYTES, yd + (size_t)i * prm.ypl * YD_BYTES, (uint32_t)(P * YD_BYTES),
-                             &full[slot]);
-                    // the tiles one ring depth further on, into L2, so that copy meets L2 rather than DRAM
-                    if (i + STAGES < w.nst) {
-                        bulk_prefetch_l2(sk + (size_t)(i + STAGES) * S_BYTES, S_BYTES);
-                        bulk_prefetch_l2(yd + (size_t)(i + STAGES) * prm.ypl * YD_BYTES, (uint32_t)(P * YD_BYTES));
-                    }
+#pragma unroll
+                    for (int p = 0; p < P; ++p)
+                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * prm.ypl + p) * YD_BYTES, YD_BYTES,
+                                 &full[slot]);
                     ++g;
                 }
             }
@@ -550,10 +540,14 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     constexpr int WIN_MAX = 32000;
     const int sm = ctx.sm_count;
     const int64_t tiles = (int64_t)tiles_m * tiles_n;
-    // with a feed and a small S, each column tile is its own launch as its
-    // columns arrive (below)
-    const bool per_tile = feed && (double)tiles_m * Ks * S_BYTES * tiles_n <= 4.0e9;
-    const int64_t tiles_launch = per_tile ? (int64_t)tiles_m : tiles;
+    // With a feed (A still arriving from the host) the MMA runs per group of
+    // column tiles as their columns land, so it overlaps the rest of the
+    // upload; every group re-reads S (from L2 when S is small), so a small S
+    // goes tile by tile and a large one in four groups.
+    const double s_bytes = (double)tiles_m * Ks * S_BYTES;
+    const int groups = !feed ? 1 : (s_bytes * tiles_n <= 4.0e9 ? tiles_n : std::min(tiles_n, 4));
+    const int per_group = div_up(tiles_n, groups);
+    const int64_t tiles_launch = (int64_t)tiles_m * per_group;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -581,8 +575,12 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     const cudaStream_t side = (ctx.side ? ctx.side : side_stream(ctx.device));
     stream_wait(side, ctx.stream);                 // the S buffer exists
     {
+        // about four resident blocks per SM in all: the generator is
+        // integer-pipe bound, and the main stream's HBM-bound digit planes
+        // (and the caller's row-major copy) need the remaining SM slots to
+        // run beside it rather than after it
         int gx = div_up((int64_t)Ks * 1024, 256);
-        const int cap = 16 * sm / (tiles_m < 16 ? tiles_m : 16) + 1;
+        const int cap = std::max(1, 4 * sm / tiles_m);
         if (gx > cap) gx = cap;
         sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, 0, sk);
         RNLA_LAUNCH_CHECK();
@@ -591,6 +589,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     prm.M = M; prm.N = N; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
     prm.it0 = 0; prm.it_count = tiles_m;
+    prm.jt0 = 0; prm.jt_count = tiles_n;
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
@@ -623,29 +622,24 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         // the caller's main-stream work that only needs the inputs (the
         // solver's row-major copy) fills the wait for the generator
         if (before_mma) before_mma();
-        prm.jt_only = -1;
         stream_wait(ctx.stream, side);                 // S is written
         kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
         RNLA_LAUNCH_CHECK();
     } else {
-        // Each column tile's digit planes are made as soon as its columns
-        // have landed.  The MMA runs per column tile too (overlapping the
-        // rest of the upload) while re-reading S once per tile stays cheap;
-        // when S is large (every tile re-reads all of it from HBM) one MMA
-        // launch after the last tile keeps S reads to about one.
-        for (int jt = 0; jt < tiles_n; ++jt) {
-            feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
-            digits(jt, 1);
-            if (!per_tile) continue;
-            if (jt == 0) stream_wait(ctx.stream, side);
-            prm.jt_only = jt;
-            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
-            RNLA_LAUNCH_CHECK();
-        }
-        if (!per_tile) {
-            stream_wait(ctx.stream, side);
-            prm.jt_only = -1;
-            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+        // each column tile's digit planes as soon as its columns have
+        // landed, each group's MMA once the group's last tile is in
+        for (int g0 = 0; g0 < tiles_n; g0 += per_group) {
+            const int cnt = std::min(per_group, tiles_n - g0);
+            for (int jt = g0; jt < g0 + cnt; ++jt) {
+                feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
+                digits(jt, 1);
+            }
+            if (g0 == 0) stream_wait(ctx.stream, side);    // S is written
+            prm.jt0 = g0;
+            prm.jt_count = cnt;
+            prm.units = (int)((int64_t)cnt * tiles_m * kc_count);
+            const unsigned gp = (unsigned)(prm.units < sm ? prm.units : sm);
+            kfn<<<gp, THREADS, smem, ctx.stream>>>(prm);
             RNLA_LAUNCH_CHECK();
         }
     }
@@ -833,7 +827,8 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
     Params prm;
     prm.M = MM; prm.N = NN; prm.K = K;
     prm.tiles_m = tiles_m; prm.tiles_n = tiles_n; prm.Ks = Ks;
-    prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units; prm.jt_only = -1;
+    prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
+    prm.jt0 = 0; prm.jt_count = tiles_n;
     prm.it0 = 0; prm.it_count = tiles_m;
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
