@@ -221,11 +221,10 @@ RNLA_API int rnla_lsqr_dev(const double* a_dev, int64_t m, int64_t n, int64_t ld
  * 8 * (10 + 4G + m + 5n + G n) bytes, G <= 4 x (number of SMs), and larger
  * problems return RNLA_ERR_INVALID_DIMENSIONS; n > 4096 returns
  * RNLA_ERR_UNSUPPORTED.  Calls share that array, so calls on one device are
- * serialised (a per-device lock held until the call has synchronised); the
- * first call on a device looks up the array's address and should come
- * before any stream capture.  Every call clears its words with
- * cudaMemsetAsync and synchronises the given stream on its result before it
- * returns. */
+ * serialised (a per-device lock held until the call has synchronised).
+ * Every call clears its words with cudaMemsetAsync and synchronises the
+ * given stream on its result before it returns: it must not be called on a
+ * stream that is being captured into a graph. */
 RNLA_API int rnla_lsqr_noalloc_dev(const double* a_dev, int64_t m, int64_t n, int64_t lda,
                                    const double* b_dev, double damp, double atol, double btol,
                                    double conlim, int64_t iter_lim, const double* x0_dev,

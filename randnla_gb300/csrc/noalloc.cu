@@ -26,11 +26,11 @@
 //   * n is at most 4096 (as for rnla_lsqr_dev); a larger n returns
 //     RNLA_ERR_UNSUPPORTED;
 //   * the first call on a device looks the array's device address up
-//     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture;
+//     (cudaGetSymbolAddress, with that device current) and caches it;
 //   * every call clears its words with cudaMemsetAsync, queries the kernel's
 //     occupancy and synchronises the stream it is given on its result
-//     before it returns.
+//     before it returns, so it must not be called on a stream that is being
+//     captured into a graph.
 #include "rnla_abi.h"
 #include <mutex>
 
