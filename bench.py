@@ -424,7 +424,10 @@ def run_ours(args, rank, local, ws):
         t_e2e = time.perf_counter() - t_start
         t_e2e = max_over_ranks(t_e2e, ws)
         e2e = {"value": ws * ke / t_e2e, "unit": UNIT, "h2d_bytes_per_step": m * n * esz + m * 8,
-               "d2h_bytes_per_step": n * 8, "steps": ke}
+               "d2h_bytes_per_step": n * 8, "steps": ke,
+               # the last call's device-timed stages: the sketch stage includes the wait for the upload
+               "stages_ms": {"sketch_and_upload": st_e.ms_sketch, "factor": st_e.ms_factor,
+                             "solve": st_e.ms_solve}}
         del Ah
 
     # roofline of the dominant kernel
