@@ -456,24 +456,45 @@ __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int6
         const int jt = (int)(j / BN), jl = (int)(j % BN);
         const int Ej = (j < Ntot) ? E[j] : 0;
         uint16_t dg[P][8];
+        const int ksc = 8 - Ej;                      // x 2^(8 - E_j) lies in (-256, 256)
+        if (sizeof(T) == 4 && j < N && ksc >= -126 && ksc <= 127) {
+            // FP32 data in FP32 arithmetic: scaling by a power of two is exact,
+            // each digit is the nearest integer of what the earlier ones leave
+            // (|d| <= 256, balanced), times 256 for the next -- a handful of
+            // FP32 operations per element instead of 64-bit integer work.  The
+            // bf16 of an integer of at most 9 bits is its float's top half.
+            const float scale = __int_as_float((127 + ksc) << 23);
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int64_t k = (int64_t)s * BK + c8 * 8 + t;
-            uint64_t M = 0;
-            int e2 = 0;
-            bool neg = false;
-            if (j < Ntot && k < K) load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
-            uint64_t Tq = 0;
-            if (M) {
-                const int sh = Ej - 8 * P - e2;
-                if (sh <= 0) Tq = M << (-sh);
-                else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
+            for (int t = 0; t < 8; ++t) {
+                const int64_t k = (int64_t)s * BK + c8 * 8 + t;
+                float x = k < K ? (float)Y[k + j * ldy] * scale : 0.f;
+#pragma unroll
+                for (int p = 0; p < P; ++p) {
+                    const float d = rintf(x);
+                    dg[p][t] = (uint16_t)(__float_as_uint(d) >> 16);
+                    x = (x - d) * 256.f;
+                }
             }
+        } else {
 #pragma unroll
-            for (int p = 0; p < P; ++p) {
-                const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (8 * (P - 1)))
-                                            : (uint32_t)((Tq >> (8 * (P - 1 - p))) & 255u);
-                dg[p][t] = digit_bf16(d, neg);
+            for (int t = 0; t < 8; ++t) {
+                const int64_t k = (int64_t)s * BK + c8 * 8 + t;
+                uint64_t M = 0;
+                int e2 = 0;
+                bool neg = false;
+                if (j < Ntot && k < K) load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
+                uint64_t Tq = 0;
+                if (M) {
+                    const int sh = Ej - 8 * P - e2;
+                    if (sh <= 0) Tq = M << (-sh);
+                    else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
+                }
+#pragma unroll
+                for (int p = 0; p < P; ++p) {
+                    const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (8 * (P - 1)))
+                                                : (uint32_t)((Tq >> (8 * (P - 1 - p))) & 255u);
+                    dg[p][t] = digit_bf16(d, neg);
+                }
             }
         }
         const size_t blk = ((size_t)jt * Ks + s) * P;
@@ -673,6 +694,35 @@ __global__ void sdigit_kernel(const T* __restrict__ X, int64_t K, int64_t N, int
         const int st = (int)(cc >> 3), c8 = (int)(cc & 7);
         const int it = (int)(j / BM), r = (int)(j % BM);
         const int Ej = (j < N) ? E[j] : 0;
+        uint8_t* tile = out + ((size_t)it * Ks + st) * S_BYTES + r * ROW_BYTES + ((c8 ^ (r & 7)) << 4);
+        const int ksc = 6 - Ej;                      // x 2^(6 - E_j) lies in (-64, 64)
+        if (sizeof(T) == 4 && j < N && ksc >= -126 && ksc <= 127) {
+            // FP32 data in FP32 arithmetic (as slice_kernel): balanced digits
+            // |d| <= 64, the bf16 of each the top half of its float
+            const float scale = __int_as_float((127 + ksc) << 23);
+            float x[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int64_t k = (int64_t)st * BK + c8 * 8 + t;
+                x[t] = k < K ? (float)X[k + j * ldx] * scale : 0.f;
+            }
+            for (int dig = 0; dig < ND; ++dig) {
+                uint32_t h[8];
+#pragma unroll
+                for (int t = 0; t < 8; ++t) {
+                    const float d = rintf(x[t]);
+                    h[t] = __float_as_uint(d) >> 16;
+                    x[t] = (x[t] - d) * 64.f;
+                }
+                uint4 v;
+                v.x = h[0] | (h[1] << 16);
+                v.y = h[2] | (h[3] << 16);
+                v.z = h[4] | (h[5] << 16);
+                v.w = h[6] | (h[7] << 16);
+                *(uint4*)(tile + (size_t)dig * digit_stride) = v;
+            }
+            continue;
+        }
         uint64_t Tq[8];
         bool neg[8];
 #pragma unroll
@@ -694,7 +744,6 @@ __global__ void sdigit_kernel(const T* __restrict__ X, int64_t K, int64_t N, int
                 else if (sh < 64) Tq[t] = (M + (1ull << (sh - 1))) >> sh;
             }
         }
-        uint8_t* tile = out + ((size_t)it * Ks + st) * S_BYTES + r * ROW_BYTES + ((c8 ^ (r & 7)) << 4);
         for (int dig = 0; dig < ND; ++dig) {
             uint16_t dg[8];
 #pragma unroll
