@@ -568,9 +568,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     const double s_bytes = (double)tiles_m * Ks * S_BYTES;
     const int groups = !feed ? 1 : (s_bytes * tiles_n <= 4.0e9 ? tiles_n : std::min(tiles_n, 4));
     const int per_group = div_up(tiles_n, groups);
-    // without a feed and with a large S, two launches over the row halves (below)
-    const bool two_halves = !feed && tiles_m >= 2 && s_bytes >= 1.0e9;
-    const int64_t tiles_launch = two_halves ? (int64_t)(tiles_m / 2) * tiles_n : (int64_t)tiles_m * per_group;
+    const int64_t tiles_launch = (int64_t)tiles_m * per_group;
     const double t_stage = 0.09 * P;                 // us per stage per SM (tensor bound)
     const double t_unit = 0.02;                      // us of partial traffic per unit
     int best_kc = div_up(wins, WIN_MAX);
@@ -593,34 +591,20 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * (YD_BYTES / 2), ctx.stream);
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
     DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
-    // The sketch generator (integer-pipe bound) runs on the side stream while
-    // the main stream makes the digit planes (HBM bound).  Without a feed and
-    // with a large S, the rows of S come in two halves: the MMA over the first
-    // half starts once it is written, and the second half is generated beside
-    // that MMA by about one 128-thread block per SM -- which fits next to an
-    // MMA CTA (registers, shared memory) and uses the CUDA cores the tensor
-    // pipe leaves idle.
+    // the sketch generator (integer ALU bound) runs on the side stream while
+    // the main stream makes the digit planes (HBM bound)
     const cudaStream_t side = (ctx.side ? ctx.side : side_stream(ctx.device));
     stream_wait(side, ctx.stream);                 // the S buffer exists
-    const bool halves = !feed && tiles_m >= 2 && s_bytes >= 1.0e9;
-    const int h = halves ? tiles_m / 2 : tiles_m;
-    auto gen = [&](int it0, int cnt, bool beside) {
-        // four 256-thread blocks per SM leave the digit planes SM slots beside
-        // it; beside the MMA, about one 128-thread block per SM (even three on
-        // one SM leave room for an MMA CTA's registers)
-        const int bt = beside ? 128 : 256;
-        int gx = div_up((int64_t)Ks * 1024, bt);
-        const int cap = std::max(1, (beside ? 1 : 4) * sm / cnt);
+    {
+        // about four resident blocks per SM in all: the generator is
+        // integer-pipe bound, and the main stream's HBM-bound digit planes
+        // (and the caller's row-major copy) need the remaining SM slots to
+        // run beside it rather than after it
+        int gx = div_up((int64_t)Ks * 1024, 256);
+        const int cap = std::max(1, 4 * sm / tiles_m);
         if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)cnt), bt, 0, side>>>(key, dist, M, K, Ks, it0, sk);
+        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, 0, sk);
         RNLA_LAUNCH_CHECK();
-    };
-    cudaEvent_t first_half = nullptr;
-    gen(0, h, false);
-    if (halves) {
-        RNLA_CUDA(cudaEventCreateWithFlags(&first_half, cudaEventDisableTiming));
-        RNLA_CUDA(cudaEventRecord(first_half, side));
-        gen(h, tiles_m - h, true);
     }
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
@@ -659,23 +643,9 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         // the caller's main-stream work that only needs the inputs (the
         // solver's row-major copy) fills the wait for the generator
         if (before_mma) before_mma();
-        if (halves) {
-            for (int part = 0; part < 2; ++part) {
-                if (part == 0) RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, first_half, 0));
-                else stream_wait(ctx.stream, side);         // all of S is written
-                prm.it0 = part == 0 ? 0 : h;
-                prm.it_count = part == 0 ? h : tiles_m - h;
-                prm.units = (int)((int64_t)prm.it_count * tiles_n * kc_count);
-                const unsigned gp = (unsigned)(prm.units < sm ? prm.units : sm);
-                kfn<<<gp, THREADS, smem, ctx.stream>>>(prm);
-                RNLA_LAUNCH_CHECK();
-            }
-            RNLA_CUDA(cudaEventDestroy(first_half));
-        } else {
-            stream_wait(ctx.stream, side);             // S is written
-            kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
-            RNLA_LAUNCH_CHECK();
-        }
+        stream_wait(ctx.stream, side);                 // S is written
+        kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
+        RNLA_LAUNCH_CHECK();
     } else {
         // each column tile's digit planes as soon as its columns have
         // landed, each group's MMA once the group's last tile is in
