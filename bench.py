@@ -29,8 +29,11 @@ of the sketch, R^-1, preconditioned LSQR, x = R^-1 z) through the library's
 device-pointer entry point; one rand_svd step = one rand_svd through
 rnla_rand_svd_dev.  `value` is solves/s with inputs resident in HBM; `e2e` is the same
 metric through the host-pointer entry point with pinned host buffers (A and b
-copied in, x copied out inside the timed region).  A is larger than L2 in
-every workload, so no flush is needed between steps.
+copied in, x copied out inside the timed region), over max(5, K) calls after
+max(3, W) untimed ones, with the per-call median / min / max and the plain
+pinned-copy bandwidth of A beside it (the host link of a shared machine
+slows single copies by 2-3x at times, and the total includes those calls).
+A is larger than L2 in every workload, so no flush is needed between steps.
 
 The CPU legs (`cpu_baseline` and `--impl reference`) run the oracle's
 restatement of the reference path at the FULL size of the workload: no row
@@ -171,6 +174,44 @@ def max_over_ranks(x, ws):
     t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def time_host_calls(call, steps, warmup, ws):
+    """End-to-end leg: `warmup` (at least 3) untimed calls, then `steps`
+    calls timed one by one on the host clock (each call returns only once
+    its results are in host memory).  Returns the max-over-ranks total
+    seconds and the per-call milliseconds: the total gives `e2e.value`,
+    the spread shows calls slowed by the host link."""
+    for _ in range(max(3, warmup)):
+        call()
+    barrier(ws)
+    per = []
+    t_start = time.perf_counter()
+    for _ in range(steps):
+        t = time.perf_counter()
+        call()
+        per.append((time.perf_counter() - t) * 1e3)
+    total = max_over_ranks(time.perf_counter() - t_start, ws)
+    per.sort()
+    return total, {"median": per[len(per) // 2], "min": per[0], "max": per[-1]}
+
+
+def pinned_h2d_gbs(host, dev, reps=5):
+    """Bandwidth of plain copies of a pinned host tensor to the device (the
+    same bytes the end-to-end call uploads): median and slowest of `reps`
+    copies, for reading the end-to-end figure against the host link."""
+    import torch
+    d = torch.empty(host.shape, dtype=host.dtype, device=dev)
+    rates = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        d.copy_(host, non_blocking=True)
+        torch.cuda.synchronize()
+        rates.append(host.numel() * host.element_size() / (time.perf_counter() - t) / 1e9)
+    del d
+    rates.sort()
+    return {"median": rates[len(rates) // 2], "min": rates[0]}
 
 
 # ---------------------------------------------------------------------------
@@ -414,20 +455,14 @@ def run_ours(args, rank, local, ws):
             if rc != 0:
                 raise RuntimeError(lib.rnla_last_error_message().decode())
 
-        for _ in range(2):
-            e2e_call()
-        barrier(ws)
-        t_start = time.perf_counter()
-        ke = max(2, args.steps // 2)
-        for _ in range(ke):
-            e2e_call()
-        t_e2e = time.perf_counter() - t_start
-        t_e2e = max_over_ranks(t_e2e, ws)
+        ke = max(5, args.steps)
+        t_e2e, call_ms = time_host_calls(e2e_call, ke, args.warmup, ws)
         e2e = {"value": ws * ke / t_e2e, "unit": UNIT, "h2d_bytes_per_step": m * n * esz + m * 8,
-               "d2h_bytes_per_step": n * 8, "steps": ke,
+               "d2h_bytes_per_step": n * 8, "steps": ke, "call_ms": call_ms,
                # the last call's device-timed stages: the sketch stage includes the wait for the upload
                "stages_ms": {"sketch_and_upload": st_e.ms_sketch, "factor": st_e.ms_factor,
-                             "solve": st_e.ms_solve}}
+                             "solve": st_e.ms_solve},
+               "pinned_h2d_gbs_of_A": pinned_h2d_gbs(Ah, dev)}
         del Ah
 
     # roofline of the dominant kernel
@@ -649,15 +684,12 @@ def run_svd(args, rank, local, ws):
             Vh.copy_(Vd, non_blocking=True)
             torch.cuda.synchronize()
 
-        e2e_call()
-        t0 = time.perf_counter()
-        ke = max(2, args.steps // 2)
-        for _ in range(ke):
-            e2e_call()
-        t = max_over_ranks(time.perf_counter() - t0, ws)
+        ke = max(5, args.steps)
+        t, call_ms = time_host_calls(e2e_call, ke, args.warmup, ws)
         line["e2e"] = {"value": ws * ke / t, "unit": UNIT, "h2d_bytes_per_step": m * n * esz,
-                       "d2h_bytes_per_step": 8 * (m * l + l + l * n), "steps": ke,
-                       "api": "rnla_rand_svd_dev with pinned host copies in and out on the same stream"}
+                       "d2h_bytes_per_step": 8 * (m * l + l + l * n), "steps": ke, "call_ms": call_ms,
+                       "api": "rnla_rand_svd_dev with pinned host copies in and out on the same stream",
+                       "pinned_h2d_gbs_of_A": pinned_h2d_gbs(Ah, dev)}
     return line
 
 

@@ -1216,10 +1216,11 @@ int rnla_lsrn_overdetermined_dev(const void* a_dev, int32_t a_is_f32, int64_t m,
     RNLA_API_END
 }
 
-// Problems run one after another on the caller's stream, each through the
-// single-problem pipeline, so every x matches its own _dev call bit for bit.
-// A failing problem (bad shape, singular sketch, a device wait that gave
-// up) is recorded and the batch goes on; a CUDA error ends it.
+// Every problem goes through the single-problem pipeline on one of the
+// workers' streams (grids sized for that worker's share of the SMs), so x
+// matches its own _dev call to the solver's accuracy, not bit for bit.  A
+// failing problem (bad shape, singular sketch, a device wait that gave up)
+// is recorded and the batch goes on; a CUDA error ends it.
 int rnla_solve_batched(const rnla_ls_problem* probs, int64_t count, double epsilon, int64_t l,
                        double sampling_factor, const rnla_options* opt, int32_t* status_out,
                        rnla_stats* stats_out, void* stream) {
