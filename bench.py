@@ -201,7 +201,7 @@ def pinned_h2d_gbs(host, dev, reps=5):
     same bytes the end-to-end call uploads): median and slowest of `reps`
     copies, for reading the end-to-end figure against the host link."""
     import torch
-    d = torch.empty(host.shape, dtype=host.dtype, device=dev)
+    d = torch.empty_like(host, device=dev)      # same strides: one contiguous copy
     rates = []
     for _ in range(reps):
         torch.cuda.synchronize()

@@ -677,8 +677,11 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // of the MMA that waits for it; with a feed, on the side stream after
         // the sketch
         const bool ffp = o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n);
-        std::function<void()> before_mma;
-        if (ffp && !feed) before_mma = [&]() { lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in, true); };
+        std::function<void(cudaStream_t)> before_mma;
+        if (ffp && !feed) {
+            lsqr_ff_alloc(ctx, Av, a_f32, m, n, lsqr_in);
+            before_mma = [&](cudaStream_t st) { lsqr_ff_build(ctx, lsqr_in, lda, b, st, 0); };
+        }
         // S [a b] in one pass: b rides along as column n of the digit planes
         tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed, DIST_GAUSSIAN, before_mma);
         if (feed) feed->wait_all(ctx.stream);

@@ -142,8 +142,11 @@ void gram_ff(Ctx& ctx, const double* X, int64_t ldx, int64_t N1, const double* Y
     const int sym = (X == Y && ldx == ldy && N1 == N2) ? 1 : 0;
     const int tiles1 = div_up(N1, TM), tiles2 = div_up(N2, TM);
     const int tiles = sym ? tiles1 * (tiles1 + 1) / 2 : tiles1 * tiles2;
-    // about two CTAs per SM over (tile, K chunk), chunks a multiple of 32 rows
-    int chunks = div_up(2 * ctx.sm_count, tiles);
+    // about eight CTAs per SM over (tile, K chunk), chunks a multiple of 32
+    // rows: with ~2 per SM a tile count just above the SM count (153
+    // symmetric tiles of a 1025-column Gram on 152 SMs) leaves a few SMs
+    // with half again the work of the rest
+    int chunks = div_up(8 * ctx.sm_count, tiles);
     const int64_t max_chunks = div_up(K, KC);
     if (chunks > max_chunks) chunks = (int)max_chunks;
     if (chunks > 4096) chunks = 4096;

@@ -1305,12 +1305,11 @@ __global__ void rowmajor_split_kernel(const TA* __restrict__ A, int64_t m, int64
     }
 }
 
-// Row-major FP32 copy: row i is ldq floats (n rounded up to a multiple of 4,
-// zero beyond n), so a 16-byte chunk holds 4 consecutive columns.  32 x 32
-// tiles through shared memory.
-// Row-major FP32 copy of a column-major FP32 A, 64 x 64 tiles through shared
-// memory (256-byte column segments in, 256-byte row segments out), eight
-// persistent blocks per SM walking the tiles.
+// Row-major FP32 copy of a column-major FP32 A: row i is ldq floats (n
+// rounded up to a multiple of 4, zero beyond n), so a 16-byte chunk holds 4
+// consecutive columns.  64 x 64 tiles through shared memory (256-byte column
+// segments in, 256-byte row segments out), eight persistent blocks per SM
+// walking the tiles.
 __global__ void __launch_bounds__(256) rowmajor_f32_kernel(const float* __restrict__ A, int64_t m, int64_t n,
                                                            int64_t lda, float* __restrict__ AQ, int64_t ldq) {
     __shared__ float tile[64][65];
@@ -1409,13 +1408,14 @@ void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm) {
 // Float-float copies of A (row-major, column-pair order) and b, enqueued on
 // `st`.
 static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32, int64_t m, int64_t n,
-                           int64_t lda, const double* b, int64_t ldf, float2* AF, float2* bF) {
+                           int64_t lda, const double* b, int64_t ldf, float2* AF, float2* bF, int grid_cap = 0) {
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
-    if (a_f32)
-        rowmajor_f32_kernel<<<(unsigned)std::min<int64_t>(div_up(m, 64) * div_up(ldf, 64), 8 * ctx.sm_count), 256, 0,
-                              st>>>(static_cast<const float*>(A), m, n, lda, reinterpret_cast<float*>(AF), ldf);
-    else
+    if (a_f32) {
+        const int64_t cap = grid_cap > 0 ? grid_cap : 8 * ctx.sm_count;
+        rowmajor_f32_kernel<<<(unsigned)std::min<int64_t>(div_up(m, 64) * div_up(ldf, 64), cap), 256, 0, st>>>(
+            static_cast<const float*>(A), m, n, lda, reinterpret_cast<float*>(AF), ldf);
+    } else
         rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,
                                                                     reinterpret_cast<float*>(AF), ldf);
     RNLA_LAUNCH_CHECK();
@@ -1425,8 +1425,7 @@ static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32,
     RNLA_LAUNCH_CHECK();
 }
 
-void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
-                     LsqrFFInput& in, bool on_main) {
+void lsqr_ff_alloc(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in) {
     if (!lsqr_ff_supported(n)) fail(RNLA_ERR_UNSUPPORTED, "lsqr (float-float): n must be in [1, 1024]");
     in.A = A; in.m = m; in.n = n;
     in.f32 = a_f32;
@@ -1435,12 +1434,21 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
     in.ldf = a_f32 ? (n + 3) & ~3LL : (n + 1) & ~1LL;
     in.AF.alloc(a_f32 ? (size_t)m * in.ldf / 2 : (size_t)m * in.ldf, ctx.stream);
     in.bF.alloc(m, ctx.stream);
-    const cudaStream_t st = on_main ? ctx.stream : (ctx.side ? ctx.side : side_stream(ctx.device));
-    if (!on_main) stream_wait(st, ctx.stream);     // buffers allocated, A and b written
-    build_ff_input(ctx, st, A, a_f32, m, n, lda, b, in.ldf, in.AF, in.bF);
-    RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     in.owner = ctx.stream;
+}
+
+void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap) {
+    build_ff_input(ctx, st, in.A, in.f32, in.m, in.n, lda, b, in.ldf, in.AF, in.bF, grid_cap);
+    RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     RNLA_CUDA(cudaEventRecord(in.ready, st));
+}
+
+void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
+                     LsqrFFInput& in) {
+    lsqr_ff_alloc(ctx, A, a_f32, m, n, in);
+    const cudaStream_t st = ctx.side ? ctx.side : side_stream(ctx.device);
+    stream_wait(st, ctx.stream);                   // buffers allocated, A and b written
+    lsqr_ff_build(ctx, in, lda, b, st, 0);
 }
 
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,

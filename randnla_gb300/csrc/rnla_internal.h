@@ -143,9 +143,11 @@ int64_t cgls_solve(Ctx& ctx, const double* a64, const float* a32, int64_t m, int
                    int64_t lda, const double* M, const double* b, const double* x0,
                    double tolerance, int64_t num_iterations, double* x, bool* converged);
 // Float-float LSQR (lsqr_ff.cu) on FP64 or FP32 data, 1 <= n <= 1024; same contract
-// as lsqr_solve.  lsqr_ff_prepare builds the float-float copies of A and b
-// on the side stream (so they overlap earlier work on ctx.stream);
-// lsqr_ff_solve waits for them (or builds them itself when `pre` is null).
+// as lsqr_solve.  lsqr_ff_prepare builds the solver's copies of A and b on
+// the side stream (so they overlap later work on ctx.stream); lsqr_ff_alloc
+// + lsqr_ff_build do the same in two steps, the build on a stream of the
+// caller's choosing; lsqr_ff_solve waits for them (or builds them itself
+// when `pre` is null).
 struct LsqrFFInput {
     DevBuf<float2> AF, bF;
     const void* A = nullptr;
@@ -169,10 +171,13 @@ bool lsqr_ff_supported(int64_t n);
 // M (n x n upper) <- the FP64 value of its float-float split, so that the
 // float-float LSQR operator A M and a later FP64 product M z use the same M.
 void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm);
-// on_main: build on ctx.stream itself (filling a wait of the main stream)
-// instead of the side stream.
 void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* b,
-                     LsqrFFInput& in, bool on_main = false);
+                     LsqrFFInput& in);
+// Allocates the copies on ctx.stream (no kernels).
+void lsqr_ff_alloc(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in);
+// Builds them on `st`, which the caller has ordered after the allocation and
+// after A and b are written; grid_cap > 0 caps the copy kernel's blocks.
+void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
                          double* arnorms_dev, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
@@ -229,7 +234,8 @@ bool tc_available(Ctx& ctx);
 // of the product is started as soon as its columns are on the device.
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN, const std::function<void()>& before_mma = {});
+                     const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN,
+                     const std::function<void(cudaStream_t)>& before_mma = {});
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
 // ---- float-float tall-skinny products (gram_ff.cu) ----

@@ -143,6 +143,69 @@ __global__ void __launch_bounds__(256) sketch_gen_kernel(RngKey key, int dist, i
     }
 }
 
+// The same S tile images for Gaussian entries of a Philox key, bit for bit,
+// with fewer instructions on the integer ALU pipe, which bounds the
+// generator (and which the digit-plane kernels running beside it need too):
+//  * block x takes the whole stages x, x + gridDim.x, ... of m tile it, so a
+//    thread keeps its K pair kp and row groups igq + 8 q (q = 0..3) from
+//    stage to stage, and with them the swizzled store offsets;
+//  * the alias table sits in shared memory as 64-bit entries
+//    {threshold << 7, bf16(own t) | bf16(alias t) << 16}: an entry is a
+//    shift, a 64-bit load, a masked compare and a select -- the masked word
+//    (u & 0x01FFFF80) < threshold << 7 is the x < threshold of qgauss_t --
+//    and no integer-to-float conversion; two entries pack with one byte
+//    permute.
+__device__ __forceinline__ void gauss_block_bf16(const RngKey& key, uint64_t g, const uint2* qt, uint32_t r[4]) {
+    uint32_t w[4] = {(uint32_t)g, (uint32_t)(g >> 32), 0u, 0u};
+    philox4x32_10(w, (uint32_t)key.k0, (uint32_t)(key.k0 >> 32));
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const uint2 e = qt[w[i] >> 25];
+        r[i] = ((w[i] & 0x01FFFF80u) < e.x) ? e.y : (e.y >> 16);     // low 16 bits: bf16 of t
+    }
+}
+
+__global__ void __launch_bounds__(256) sketch_gen_gauss_kernel(RngKey key, int64_t M, int64_t K, int Ks, int it0,
+                                                               uint8_t* __restrict__ S) {
+    __shared__ uint2 qt[128];
+    if (threadIdx.x < 128) {
+        const uint32_t e = k_qgauss_table[threadIdx.x];
+        const float own = (float)((int)((e >> 18) & 0x7Fu) - 63), ali = (float)((int)(e >> 25) - 63);
+        qt[threadIdx.x] = make_uint2((e & 0x3FFFFu) << 7, pack_bf16(own, ali));
+    }
+    __syncthreads();
+    const int it = it0 + blockIdx.y;
+    const uint64_t gstride = (uint64_t)(((M + 3) & ~3LL) >> 2);
+    const int kp = threadIdx.x & 31, igq = threadIdx.x >> 5;
+    // rows 4 igq + t of the first 32-row slab; slab q adds 32 rows (4096 bytes)
+    // and leaves the swizzle (row & 7) unchanged
+    uint32_t off[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int r = 4 * igq + t;
+        off[t] = (uint32_t)(r * ROW_BYTES + ((((kp >> 2) ^ (r & 7))) << 4) + ((kp & 3) << 2));
+    }
+    // block counter of (row group igq, K column 2 kp) in stage 0
+    const uint64_t g0 = (uint64_t)it * (BM / 4) + (uint64_t)igq + (uint64_t)(2 * kp) * gstride;
+    for (int s = blockIdx.x; s < Ks; s += gridDim.x) {
+        uint8_t* tile = S + ((size_t)it * Ks + (size_t)s) * S_BYTES;
+        const int64_t k0 = (int64_t)s * BK + 2 * kp;
+        const uint64_t gs = g0 + (uint64_t)s * BK * gstride;
+#pragma unroll 1
+        for (int q = 0; q < 4; ++q) {
+            const int64_t row0 = (int64_t)it * BM + 4 * (igq + 8 * q);
+            uint32_t r0[4] = {0u, 0u, 0u, 0u}, r1[4] = {0u, 0u, 0u, 0u};
+            if (row0 < M) {
+                if (k0 < K) gauss_block_bf16(key, gs + 8 * q, qt, r0);
+                if (k0 + 1 < K) gauss_block_bf16(key, gs + 8 * q + gstride, qt, r1);
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                *(uint32_t*)(tile + 4096 * q + off[t]) = (row0 + t < M) ? __byte_perm(r0[t], r1[t], 0x5410) : 0u;
+        }
+    }
+}
+
 // Work unit u: C tile (it, jt) partial over K chunk kc, with jt fastest:
 // the column tiles sharing an S tile are processed side by side.
 struct Unit {
@@ -547,7 +610,7 @@ static size_t smem_bytes() {
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32, int64_t K, int64_t N0,
                 int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed,
-                const std::function<void()>& before_mma) {
+                const std::function<void(cudaStream_t)>& before_mma) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
     const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
     const size_t smem = smem_bytes<P>();
@@ -595,16 +658,23 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     // the main stream makes the digit planes (HBM bound)
     const cudaStream_t side = (ctx.side ? ctx.side : side_stream(ctx.device));
     stream_wait(side, ctx.stream);                 // the S buffer exists
+    cudaEvent_t s_done;
+    RNLA_CUDA(cudaEventCreateWithFlags(&s_done, cudaEventDisableTiming));
     {
         // about four resident blocks per SM in all: the generator is
         // integer-pipe bound, and the main stream's HBM-bound digit planes
-        // (and the caller's row-major copy) need the remaining SM slots to
-        // run beside it rather than after it
-        int gx = div_up((int64_t)Ks * 1024, 256);
+        // need the remaining SM slots
         const int cap = std::max(1, 4 * sm / tiles_m);
-        if (gx > cap) gx = cap;
-        sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, 0, sk);
+        if (dist == DIST_GAUSSIAN && key.gen == GEN_PHILOX4X32) {
+            const int gx = std::min(Ks, cap);
+            sketch_gen_gauss_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, M, K, Ks, 0, sk);
+        } else {
+            int gx = div_up((int64_t)Ks * 1024, 256);
+            if (gx > cap) gx = cap;
+            sketch_gen_kernel<<<dim3((unsigned)gx, (unsigned)tiles_m), 256, 0, side>>>(key, dist, M, K, Ks, 0, sk);
+        }
         RNLA_LAUNCH_CHECK();
+        RNLA_CUDA(cudaEventRecord(s_done, side));
     }
     Params prm;
     prm.M = M; prm.N = N; prm.K = K;
@@ -640,10 +710,11 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     };
     if (!feed) {
         digits(0, tiles_n);
-        // the caller's main-stream work that only needs the inputs (the
-        // solver's row-major copy) fills the wait for the generator
-        if (before_mma) before_mma();
-        stream_wait(ctx.stream, side);                 // S is written
+        // the caller's main-stream work that needs only the inputs (the
+        // solver's row-major copy) goes before the MMA: beside the MMA, its
+        // HBM traffic slows the L2-bound MMA by more than it saves
+        if (before_mma) before_mma(ctx.stream);
+        RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, s_done, 0));     // S is written
         kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
         RNLA_LAUNCH_CHECK();
     } else {
@@ -655,7 +726,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
                 feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
                 digits(jt, 1);
             }
-            if (g0 == 0) stream_wait(ctx.stream, side);    // S is written
+            if (g0 == 0) RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, s_done, 0));   // S is written
             prm.jt0 = g0;
             prm.jt_count = cnt;
             prm.units = (int)((int64_t)cnt * tiles_m * kc_count);
@@ -670,6 +741,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 8 * P + quant_shift(dist),
                                                  exact_sum, C, ldc);
     RNLA_LAUNCH_CHECK();
+    RNLA_CUDA(cudaEventDestroy(s_done));
     ctx.check_status("tensor-core sketch");
 }
 
@@ -914,7 +986,7 @@ bool tc_available(Ctx& ctx) {
 
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed, int dist, const std::function<void()>& before_mma) {
+                     const ColumnFeed* feed, int dist, const std::function<void(cudaStream_t)>& before_mma) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
     // default digits: 4 for FP64 data (32 bits below each column's maximum),
     // 3 for FP32 data (its 24-bit significands)
