@@ -672,20 +672,28 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
         // synchronisation; the device status is checked once at the end
         ctx.deferred = true;
         // BF16X + LSQR: the solver's row-major (FP32 or float-float) copies of
-        // A and b.  With A on the device they are built on the main stream
-        // while the sketch generator (side stream) is still running, ahead
-        // of the MMA that waits for it; with a feed, on the side stream after
-        // the sketch
+        // A and b.  FP32 A: the sketch's digit-plane kernel writes the
+        // row-major copy from the same reads of A (also column tile by column
+        // tile as a feed lands).  FP64 A on the device: the float-float rows
+        // are built on the main stream while the sketch generator (side
+        // stream) is still running, ahead of the MMA that waits for it; with
+        // a feed, on the side stream after the sketch.
         const bool ffp = o.inner_solver != RNLA_SOLVER_CGLS && lsqr_ff_supported(n);
         std::function<void(cudaStream_t)> before_mma;
-        if (ffp && !feed) {
-            lsqr_ff_alloc(ctx, Av, a_f32, m, n, lsqr_in);
+        SketchRowMajor rm;
+        if (ffp && (a_f32 || !feed)) lsqr_ff_alloc(ctx, Av, a_f32, m, n, lsqr_in);
+        if (ffp && a_f32) {
+            rm.dst = reinterpret_cast<float*>(lsqr_in.AF.get());
+            rm.ld = lsqr_in.ldf;
+        } else if (ffp && !feed) {
             before_mma = [&](cudaStream_t st) { lsqr_ff_build(ctx, lsqr_in, lda, b, st, 0); };
         }
         // S [a b] in one pass: b rides along as column n of the digit planes
-        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed, DIST_GAUSSIAN, before_mma);
+        tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed, DIST_GAUSSIAN, before_mma,
+                        rm);
         if (feed) feed->wait_all(ctx.stream);
-        if (ffp && feed) lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
+        if (ffp && a_f32) lsqr_ff_build(ctx, lsqr_in, lda, b, ctx.stream, 0, true);
+        else if (ffp && feed) lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     }
     tm.mark();
     // QR of S a with S b carried as an extra column: R and z0 = (Q^T S b)[:n] (lines 53-54)

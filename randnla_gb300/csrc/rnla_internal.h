@@ -176,8 +176,10 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
 // Allocates the copies on ctx.stream (no kernels).
 void lsqr_ff_alloc(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in);
 // Builds them on `st`, which the caller has ordered after the allocation and
-// after A and b are written; grid_cap > 0 caps the copy kernel's blocks.
-void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap);
+// after A and b are written; grid_cap > 0 caps the copy kernel's blocks;
+// a_done: the copy of A is already written (tc_sketch_apply's rm), only b's.
+void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap,
+                   bool a_done = false);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
                          double* arnorms_dev, const LsqrFFInput* pre = nullptr, LsqrPending* pend = nullptr);
@@ -232,10 +234,18 @@ bool tc_available(Ctx& ctx);
 // and the optional double column `extra` (K values) appended as column N.
 // With a feed, X arrives from the host in column chunks and each column tile
 // of the product is started as soon as its columns are on the device.
+// before_mma: the caller's work on the main stream ahead of the MMA (after
+// the digit planes); rm: for FP32 X, a row-major FP32 copy of X (rows of
+// rm.ld floats, zero from column N on) written by the digit-plane kernel
+// from the same reads.
+struct SketchRowMajor {
+    float* dst = nullptr;
+    int64_t ld = 0;
+};
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
                      const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN,
-                     const std::function<void(cudaStream_t)>& before_mma = {});
+                     const std::function<void(cudaStream_t)>& before_mma = {}, const SketchRowMajor& rm = {});
 // Column tile width of the tensor-core sketch (the natural feed chunk).
 constexpr int64_t TC_TILE_COLS = 64;
 // ---- float-float tall-skinny products (gram_ff.cu) ----

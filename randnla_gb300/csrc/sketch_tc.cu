@@ -505,6 +505,83 @@ __device__ __forceinline__ uint16_t digit_bf16(uint32_t d, bool neg) {
 
 // One thread per (column j, 8 consecutive k): reads 8 values, writes P 16-byte
 // chunks into the SW128 images [jt][stage][p][BN][64].  Ntot = N (+1 with extra).
+// The P bf16 digits of the 8 values k = s BK + 8 c8 .. + 7 of column j
+// (zeros beyond K or Ntot) and, for the row-major copy, the 8 FP32 values of
+// A's columns (zero for the appended column and beyond N).
+template <typename T, int P>
+__device__ __forceinline__ void slice_unit(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
+                                           const double* __restrict__ extra, int64_t Ntot,
+                                           const int* __restrict__ E, int64_t j, int s, int c8,
+                                           uint16_t dg[P][8], float xs[8]) {
+    const int Ej = (j < Ntot) ? E[j] : 0;
+    const int ksc = 8 - Ej;                      // x 2^(8 - E_j) lies in (-256, 256)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) xs[t] = 0.f;
+    if (sizeof(T) == 4 && j < N && ksc >= -126 && ksc <= 127) {
+        // FP32 data in FP32 arithmetic: scaling by a power of two is exact,
+        // each digit is the nearest integer of what the earlier ones leave
+        // (|d| <= 256, balanced), times 256 for the next -- a handful of
+        // FP32 operations per element instead of 64-bit integer work.  The
+        // bf16 of an integer of at most 9 bits is its float's top half.
+        const float scale = __int_as_float((127 + ksc) << 23);
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int64_t k = (int64_t)s * BK + c8 * 8 + t;
+            xs[t] = k < K ? (float)Y[k + j * ldy] : 0.f;
+            float x = xs[t] * scale;
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                const float d = rintf(x);
+                dg[p][t] = (uint16_t)(__float_as_uint(d) >> 16);
+                x = (x - d) * 256.f;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int64_t k = (int64_t)s * BK + c8 * 8 + t;
+            uint64_t M = 0;
+            int e2 = 0;
+            bool neg = false;
+            if (j < Ntot && k < K) {
+                load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
+                if (sizeof(T) == 4 && j < N) xs[t] = (float)Y[k + j * ldy];
+            }
+            uint64_t Tq = 0;
+            if (M) {
+                const int sh = Ej - 8 * P - e2;
+                if (sh <= 0) Tq = M << (-sh);
+                else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
+            }
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+                const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (8 * (P - 1)))
+                                            : (uint32_t)((Tq >> (8 * (P - 1 - p))) & 255u);
+                dg[p][t] = digit_bf16(d, neg);
+            }
+        }
+    }
+}
+
+// The unit's digits into row jl of the P digit tile images of (jt, s).
+template <int P>
+__device__ __forceinline__ void store_digits(uint16_t* __restrict__ out, int Ks, int jt, int s, int jl, int c8,
+                                             const uint16_t dg[P][8]) {
+    const size_t blk = ((size_t)jt * Ks + s) * P;
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        uint4 v;
+        v.x = dg[p][0] | ((uint32_t)dg[p][1] << 16);
+        v.y = dg[p][2] | ((uint32_t)dg[p][3] << 16);
+        v.z = dg[p][4] | ((uint32_t)dg[p][5] << 16);
+        v.w = dg[p][6] | ((uint32_t)dg[p][7] << 16);
+        uint8_t* base = (uint8_t*)out + (blk + p) * (size_t)YD_BYTES;
+        *(uint4*)(base + jl * ROW_BYTES + ((c8 ^ (jl & 7)) << 4)) = v;
+    }
+}
+
+// Digit planes of column tiles [jt0, jt0 + jt_count): a thread per (column j,
+// 8 consecutive k); consecutive threads take consecutive k of one column.
 template <typename T, int P>
 __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
                              const double* __restrict__ extra, int64_t Ntot, const int* __restrict__ E,
@@ -516,61 +593,53 @@ __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int6
         const int64_t j = (int64_t)jt0 * BN + u / chunks_per_col;
         const int64_t cc = u % chunks_per_col;
         const int s = (int)(cc >> 3), c8 = (int)(cc & 7);
-        const int jt = (int)(j / BN), jl = (int)(j % BN);
-        const int Ej = (j < Ntot) ? E[j] : 0;
         uint16_t dg[P][8];
-        const int ksc = 8 - Ej;                      // x 2^(8 - E_j) lies in (-256, 256)
-        if (sizeof(T) == 4 && j < N && ksc >= -126 && ksc <= 127) {
-            // FP32 data in FP32 arithmetic: scaling by a power of two is exact,
-            // each digit is the nearest integer of what the earlier ones leave
-            // (|d| <= 256, balanced), times 256 for the next -- a handful of
-            // FP32 operations per element instead of 64-bit integer work.  The
-            // bf16 of an integer of at most 9 bits is its float's top half.
-            const float scale = __int_as_float((127 + ksc) << 23);
+        float xs[8];
+        slice_unit<T, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
+        store_digits<P>(out, Ks, (int)(j / BN), s, (int)(j % BN), c8, dg);
+    }
+}
+
+// The same digit planes for FP32 data together with the solver's row-major
+// FP32 copy of A (rows of ldq floats, zero from column N on), so that A is
+// read once for both: a block per (column tile, stage) tile of 64 x 64
+// values (tiles column-tile fastest), each thread two (column, 8 k) units,
+// the values transposed through shared memory and written as 256-byte row
+// segments.
+template <int P>
+__global__ void __launch_bounds__(256) slice_rowmajor_kernel(const float* __restrict__ Y, int64_t K, int64_t N,
+                                                             int64_t ldy, const double* __restrict__ extra,
+                                                             int64_t Ntot, const int* __restrict__ E, int Ks,
+                                                             int jt0, int jt_count, uint16_t* __restrict__ out,
+                                                             float* __restrict__ AQ, int64_t ldq) {
+    static_assert(BN == 64 && BK == 64, "64 x 64 tiles");
+    __shared__ float tile[BK][BN + 1];
+    const int tid = threadIdx.x;
+    const int64_t tiles = (int64_t)jt_count * Ks;
+    for (int64_t u = blockIdx.x; u < tiles; u += gridDim.x) {
+        const int jt = jt0 + (int)(u % jt_count);
+        const int s = (int)(u / jt_count);
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int64_t k = (int64_t)s * BK + c8 * 8 + t;
-                float x = k < K ? (float)Y[k + j * ldy] * scale : 0.f;
+        for (int h = 0; h < 2; ++h) {
+            const int v = tid + 256 * h;
+            const int c8 = v & 7, jl = v >> 3;
+            const int64_t j = (int64_t)jt * BN + jl;
+            uint16_t dg[P][8];
+            float xs[8];
+            slice_unit<float, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
+            store_digits<P>(out, Ks, jt, s, jl, c8, dg);
 #pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const float d = rintf(x);
-                    dg[p][t] = (uint16_t)(__float_as_uint(d) >> 16);
-                    x = (x - d) * 256.f;
-                }
-            }
-        } else {
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int64_t k = (int64_t)s * BK + c8 * 8 + t;
-                uint64_t M = 0;
-                int e2 = 0;
-                bool neg = false;
-                if (j < Ntot && k < K) load_elem(Y, ldy, N, extra, k, j, M, e2, neg);
-                uint64_t Tq = 0;
-                if (M) {
-                    const int sh = Ej - 8 * P - e2;
-                    if (sh <= 0) Tq = M << (-sh);
-                    else if (sh < 64) Tq = (M + (1ull << (sh - 1))) >> sh;
-                }
-#pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const uint32_t d = (p == 0) ? (uint32_t)(Tq >> (8 * (P - 1)))
-                                                : (uint32_t)((Tq >> (8 * (P - 1 - p))) & 255u);
-                    dg[p][t] = digit_bf16(d, neg);
-                }
-            }
+            for (int t = 0; t < 8; ++t) tile[c8 * 8 + t][jl] = xs[t];
         }
-        const size_t blk = ((size_t)jt * Ks + s) * P;
-#pragma unroll
-        for (int p = 0; p < P; ++p) {
-            uint4 v;
-            v.x = dg[p][0] | ((uint32_t)dg[p][1] << 16);
-            v.y = dg[p][2] | ((uint32_t)dg[p][3] << 16);
-            v.z = dg[p][4] | ((uint32_t)dg[p][5] << 16);
-            v.w = dg[p][6] | ((uint32_t)dg[p][7] << 16);
-            uint8_t* base = (uint8_t*)out + (blk + p) * (size_t)YD_BYTES;
-            *(uint4*)(base + jl * ROW_BYTES + ((c8 ^ (jl & 7)) << 4)) = v;
+        __syncthreads();
+        const int64_t k0 = (int64_t)s * BK, j0 = (int64_t)jt * BN;
+#pragma unroll 4
+        for (int q = 0; q < 16; ++q) {
+            const int idx = q * 256 + tid;
+            const int kk = idx >> 6, jj = idx & 63;
+            if (k0 + kk < K && j0 + jj < ldq) AQ[(k0 + kk) * ldq + j0 + jj] = tile[kk][jj];
         }
+        __syncthreads();
     }
 }
 
@@ -610,7 +679,7 @@ static size_t smem_bytes() {
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32, int64_t K, int64_t N0,
                 int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed,
-                const std::function<void(cudaStream_t)>& before_mma) {
+                const std::function<void(cudaStream_t)>& before_mma, const SketchRowMajor& rm) {
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
     const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
     const size_t smem = smem_bytes<P>();
@@ -702,7 +771,12 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         const int64_t su = (int64_t)Ks * 8 * cnt * BN;
         int g = div_up(su, 256);
         if (g > 32 * sm) g = 32 * sm;
-        if (y_f32)
+        if (y_f32 && rm.dst) {
+            const int64_t tl = (int64_t)cnt * Ks;
+            const int gr = (int)std::min<int64_t>(tl, 8 * sm);
+            slice_rowmajor_kernel<P><<<gr, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt,
+                                                                 dig, rm.dst, rm.ld);
+        } else if (y_f32)
             slice_kernel<float, P><<<g, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
         else
             slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
@@ -986,16 +1060,17 @@ bool tc_available(Ctx& ctx) {
 
 void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int64_t K, int64_t N,
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
-                     const ColumnFeed* feed, int dist, const std::function<void(cudaStream_t)>& before_mma) {
+                     const ColumnFeed* feed, int dist, const std::function<void(cudaStream_t)>& before_mma,
+                     const SketchRowMajor& rm) {
     if (K <= 0 || (N <= 0 && !extra) || M <= 0) return;
     // default digits: 4 for FP64 data (32 bits below each column's maximum),
     // 3 for FP32 data (its 24-bit significands)
     if (digits <= 0) digits = x_f32 ? 3 : 4;
     switch (digits) {
-        case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
-        case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
-        case 3: tc::run<3>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
-        case 4: tc::run<4>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma); break;
+        case 1: tc::run<1>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma, rm); break;
+        case 2: tc::run<2>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma, rm); break;
+        case 3: tc::run<3>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma, rm); break;
+        case 4: tc::run<4>(ctx, key, dist, X, x_f32, K, N, ldx, extra, M, C, ldc, feed, before_mma, rm); break;
         default: fail(RNLA_ERR_INVALID_PARAMETERS, "digits must be 1..4");
     }
 }
