@@ -246,7 +246,9 @@ void tc_sketch_apply(Ctx& ctx, const RngKey& key, const void* X, bool x_f32, int
                      int64_t ldx, const double* extra, int64_t M, int digits, double* C, int64_t ldc,
                      const ColumnFeed* feed = nullptr, int dist = DIST_GAUSSIAN,
                      const std::function<void(cudaStream_t)>& before_mma = {}, const SketchRowMajor& rm = {});
-// Column tile width of the tensor-core sketch (the natural feed chunk).
+// Columns per host-to-device copy of the host-buffer entry points (the
+// tensor-core sketch starts each column tile once its chunks have landed);
+// also the width of the 64-column digit tiles.
 constexpr int64_t TC_TILE_COLS = 64;
 // ---- float-float tall-skinny products (gram_ff.cu) ----
 // C (N1 x N2, FP64, ldc) = X^T Y for column-major FP64 X (K x N1, ldx) and

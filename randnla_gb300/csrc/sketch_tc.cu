@@ -66,14 +66,21 @@ constexpr int BK = 64;            // K per pipeline stage (one 128-byte bf16 row
 constexpr int WIN = 16;           // stages per exact window (1024 K values)
 constexpr int MAXP = 4;           // digits
 constexpr int ACC_COLS = MAXP * BN;                  // TMEM columns of one accumulator set
-// ring depth: as many 16 KB + P x 8 KB stages as fit in ~200 KB (4 for P = 4,
-// 5 for P <= 3), the operand stream from L2 being latency-bound
-__host__ __device__ constexpr int stages_for(int P) { return P >= 4 ? 4 : 5; }
+// Column tile width of a launch's digit planes: one MMA covers the P planes
+// of a tile (N = P x width), so the sketch's own launches use 80 columns for
+// P <= 3 (N = 240: fewer operand bytes per MMA flop than 64-column tiles, and
+// 13 tiles for 1025 columns instead of 17 with 6% padding) and 64 for P = 4
+// (N = 256); the exact X^T Y product keeps 64-column planes for every P.
+__host__ __device__ constexpr int bn_for(int P) { return P <= 3 ? 80 : 64; }
+// ring depth: as many 16 KB + P x (width x 128 B) stages as fit in ~200 KB
+// (4 for P = 4 at 64 columns and for every P at 80, 5 for P <= 3 at 64), the
+// operand stream from L2 being latency-bound
+__host__ __device__ constexpr int stages_for(int P, int BNT) { return BNT == 64 ? (P >= 4 ? 4 : 5) : 4; }
 constexpr int DRAIN_WARPS = 4;
 constexpr int THREADS = 64 + 32 * DRAIN_WARPS;       // loader warp + MMA warp + drain warps
 constexpr int S_BYTES = BM * BK * 2;                 // 16 KB sketch tile
 constexpr int ROW_BYTES = BK * 2;                    // 128
-constexpr int YD_BYTES = BN * ROW_BYTES;             // one digit tile, 8 KB
+constexpr int YD_BYTES = BN * ROW_BYTES;             // one 64-column digit tile, 8 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 // acc += (integer value of the FP32 word f) * 2^sh, exact in int64 (sh < 31)
@@ -89,9 +96,9 @@ struct Params {
     int jt0, jt_count;        // the column tiles [jt0, jt0 + jt_count) of this launch
     int it0, it_count;        // the row tiles [it0, it0 + it_count) of this launch
     const uint8_t* sk;        // sketch tiles [it][stage] (SW128 images, 16 KB)
-    const uint16_t* ydig;     // digit planes [jt][stage][p][BN rows][64] bf16 (SW128 images)
+    const uint16_t* ydig;     // digit planes [jt][stage][p][width rows][64] bf16 (SW128 images)
     int ypl;                  // planes stored per stage in ydig (>= P; the first P are used)
-    long long* partial;       // [kc][tile][BN][BM] exact integer sums (row fastest)
+    long long* partial;       // [kc][tile][width][BM] exact integer sums (row fastest)
     unsigned int* status;
 };
 
@@ -222,14 +229,16 @@ __device__ __forceinline__ Unit unit_of(const Params& prm, int u) {
     return w;
 }
 
-template <int P>
+template <int P, int BNT>
 __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm) {
-    constexpr int STAGES = stages_for(P);
+    static_assert(P * BNT <= ACC_COLS && BNT % 16 == 0, "accumulator width");
+    constexpr int STAGES = stages_for(P, BNT);
+    constexpr int YDB = BNT * ROW_BYTES;                           // one digit tile
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t* sS = smem;                                           // STAGES x 16 KB
-    uint8_t* sY = smem + STAGES * S_BYTES;                        // STAGES x P x 8 KB
-    uint64_t* bars = (uint64_t*)(sY + STAGES * P * YD_BYTES);
+    uint8_t* sY = smem + STAGES * S_BYTES;                        // STAGES x P digit tiles
+    uint64_t* bars = (uint64_t*)(sY + STAGES * P * YDB);
     uint64_t* full = bars;                                        // stage landed (tx)
     uint64_t* empty = bars + STAGES;                              // MMAs done with the stage
     uint64_t* accFull = bars + 2 * STAGES;                        // [2] window accumulated
@@ -272,18 +281,18 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
             for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
                 const Unit w = unit_of(prm, u);
                 const uint8_t* sk = prm.sk + ((size_t)w.it * prm.Ks + w.s_begin) * S_BYTES;
-                const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)w.jt * prm.Ks + w.s_begin) * (size_t)(prm.ypl * YD_BYTES);
+                const uint8_t* yd = (const uint8_t*)prm.ydig + ((size_t)w.jt * prm.Ks + w.s_begin) * (size_t)(prm.ypl * YDB);
                 for (int i = 0; i < w.nst; ++i) {
                     const int slot = g % STAGES;
                     if (g >= STAGES && !mbar_wait(&empty[slot], (uint32_t)((g / STAGES) - 1) & 1u, err)) {
                         ok = false;
                         break;
                     }
-                    mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YD_BYTES));
+                    mbar_expect_tx(&full[slot], (uint32_t)(S_BYTES + P * YDB));
                     bulk_g2s(sS + slot * S_BYTES, sk + (size_t)i * S_BYTES, S_BYTES, &full[slot]);
 #pragma unroll
                     for (int p = 0; p < P; ++p)
-                        bulk_g2s(sY + (slot * P + p) * YD_BYTES, yd + ((size_t)i * prm.ypl + p) * YD_BYTES, YD_BYTES,
+                        bulk_g2s(sY + (slot * P + p) * YDB, yd + ((size_t)i * prm.ypl + p) * YDB, YDB,
                                  &full[slot]);
                     ++g;
                 }
@@ -303,9 +312,9 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
             // the P digit tiles of a stage are contiguous rows of one K-major
-            // operand, so one MMA of N = P * BN covers every digit: the S tile
+            // operand, so one MMA of N = P * BNT covers every digit: the S tile
             // is read from shared memory once per K step, not P times
-            constexpr uint32_t idesc = idesc_bf16(BM, P * BN);
+            constexpr uint32_t idesc = idesc_bf16(BM, P * BNT);
             int g = 0, slot = 0;          // stages consumed; ring slot
             uint32_t fph = 0;             // full-barrier parity of slot
             int win = 0;                  // windows started
@@ -326,7 +335,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                     if (!mbar_wait(&full[slot], fph, err)) { ok = false; break; }
                     tc_after();
                     const uint32_t a0 = smem_u32(sS + slot * S_BYTES);
-                    const uint32_t b0 = smem_u32(sY + slot * P * YD_BYTES);
+                    const uint32_t b0 = smem_u32(sY + slot * P * YDB);
 #pragma unroll
                     for (int kk = 0; kk < BK / 16; ++kk)
                         mma_bf16(acc, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), idesc,
@@ -347,7 +356,7 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                 if (globaltimer_ns() - t0 > WAIT_NS) { *err = 1; break; }
         }
     } else {
-        // ---------------- drain: TMEM lane quarter (warp & 3), all BN columns ----------------
+        // ---------------- drain: TMEM lane quarter (warp & 3), all BNT columns ----------------
         const int q = warp & 3;
         const int row = 32 * q + lane;
         int win = 0;
@@ -355,9 +364,9 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
         for (int u = blockIdx.x; u < prm.units && ok; u += gridDim.x) {
             const Unit w = unit_of(prm, u);
             const int tile = w.it + prm.tiles_m * w.jt;
-            long long v[BN];
+            long long v[BNT];
 #pragma unroll
-            for (int c = 0; c < BN; ++c) v[c] = 0;
+            for (int c = 0; c < BNT; ++c) v[c] = 0;
             const int nwin = (w.nst + WIN - 1) / WIN;
             for (int wi = 0; wi < nwin; ++wi, ++win) {
                 const int b = win & 1;
@@ -367,12 +376,12 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                 // two digit planes per TMEM round trip (registers: v holds the
                 // unit's int64 tile row)
 #pragma unroll
-                for (int c16 = 0; c16 < BN; c16 += 16) {
+                for (int c16 = 0; c16 < BNT; c16 += 16) {
 #pragma unroll
                     for (int p0 = 0; p0 < P; p0 += 2) {
                         uint32_t r0[16], r1[16];
-                        tmem_ld16(base + (uint32_t)(p0 * BN + c16), r0);
-                        if (p0 + 1 < P) tmem_ld16(base + (uint32_t)((p0 + 1) * BN + c16), r1);
+                        tmem_ld16(base + (uint32_t)(p0 * BNT + c16), r0);
+                        if (p0 + 1 < P) tmem_ld16(base + (uint32_t)((p0 + 1) * BNT + c16), r1);
                         tmem_ld_wait();
 #pragma unroll
                         for (int c = 0; c < 16; ++c) {
@@ -386,9 +395,9 @@ __global__ void __launch_bounds__(THREADS, 1) sketch_mma_kernel(const Params prm
                 if (lane == 0) mbar_arrive(&accEmpty[b]);
             }
             if (!ok) break;
-            long long* out = prm.partial + ((size_t)w.kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BN);
+            long long* out = prm.partial + ((size_t)w.kc * prm.tiles_m * prm.tiles_n + tile) * (size_t)(BM * BNT);
 #pragma unroll
-            for (int c = 0; c < BN; ++c) out[(size_t)c * BM + row] = v[c];
+            for (int c = 0; c < BNT; ++c) out[(size_t)c * BM + row] = v[c];
         }
     }
     tc_before();
@@ -563,8 +572,9 @@ __device__ __forceinline__ void slice_unit(const T* __restrict__ Y, int64_t K, i
     }
 }
 
-// The unit's digits into row jl of the P digit tile images of (jt, s).
-template <int P>
+// The unit's digits into row jl of the P digit tile images (BNT rows each)
+// of (jt, s).
+template <int P, int BNT>
 __device__ __forceinline__ void store_digits(uint16_t* __restrict__ out, int Ks, int jt, int s, int jl, int c8,
                                              const uint16_t dg[P][8]) {
     const size_t blk = ((size_t)jt * Ks + s) * P;
@@ -575,68 +585,71 @@ __device__ __forceinline__ void store_digits(uint16_t* __restrict__ out, int Ks,
         v.y = dg[p][2] | ((uint32_t)dg[p][3] << 16);
         v.z = dg[p][4] | ((uint32_t)dg[p][5] << 16);
         v.w = dg[p][6] | ((uint32_t)dg[p][7] << 16);
-        uint8_t* base = (uint8_t*)out + (blk + p) * (size_t)YD_BYTES;
+        uint8_t* base = (uint8_t*)out + (blk + p) * (size_t)(BNT * ROW_BYTES);
         *(uint4*)(base + jl * ROW_BYTES + ((c8 ^ (jl & 7)) << 4)) = v;
     }
 }
 
-// Digit planes of column tiles [jt0, jt0 + jt_count): a thread per (column j,
-// 8 consecutive k); consecutive threads take consecutive k of one column.
-template <typename T, int P>
+// Digit planes of column tiles [jt0, jt0 + jt_count) of width BNT: a thread
+// per (column j, 8 consecutive k); consecutive threads take consecutive k of
+// one column.
+template <typename T, int P, int BNT>
 __global__ void slice_kernel(const T* __restrict__ Y, int64_t K, int64_t N, int64_t ldy,
                              const double* __restrict__ extra, int64_t Ntot, const int* __restrict__ E,
                              int Ks, int jt0, int jt_count, uint16_t* __restrict__ out) {
     const int64_t chunks_per_col = (int64_t)Ks * 8;
-    const int64_t total = chunks_per_col * (int64_t)jt_count * BN;
+    const int64_t total = chunks_per_col * (int64_t)jt_count * BNT;
     for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < total;
          u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t j = (int64_t)jt0 * BN + u / chunks_per_col;
+        const int64_t j = (int64_t)jt0 * BNT + u / chunks_per_col;
         const int64_t cc = u % chunks_per_col;
         const int s = (int)(cc >> 3), c8 = (int)(cc & 7);
         uint16_t dg[P][8];
         float xs[8];
         slice_unit<T, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
-        store_digits<P>(out, Ks, (int)(j / BN), s, (int)(j % BN), c8, dg);
+        store_digits<P, BNT>(out, Ks, (int)(j / BNT), s, (int)(j % BNT), c8, dg);
     }
 }
 
 // The same digit planes for FP32 data together with the solver's row-major
 // FP32 copy of A (rows of ldq floats, zero from column N on), so that A is
-// read once for both: a block per (column tile, stage) tile of 64 x 64
-// values (tiles column-tile fastest), each thread two (column, 8 k) units,
-// the values transposed through shared memory and written as 256-byte row
-// segments.
-template <int P>
+// read once for both: a block per (column tile, stage) tile of 64 x BNT
+// values (tiles column-tile fastest), the BNT x 8 (column, 8 k) units spread
+// over the threads, the values transposed through shared memory and written
+// as row segments of BNT floats.
+template <int P, int BNT>
 __global__ void __launch_bounds__(256) slice_rowmajor_kernel(const float* __restrict__ Y, int64_t K, int64_t N,
                                                              int64_t ldy, const double* __restrict__ extra,
                                                              int64_t Ntot, const int* __restrict__ E, int Ks,
                                                              int jt0, int jt_count, uint16_t* __restrict__ out,
                                                              float* __restrict__ AQ, int64_t ldq) {
-    static_assert(BN == 64 && BK == 64, "64 x 64 tiles");
-    __shared__ float tile[BK][BN + 1];
+    static_assert(BK == 64 && (BK * BNT) % 256 == 0, "tile shape");
+    __shared__ float tile[BK][BNT + 1];
     const int tid = threadIdx.x;
     const int64_t tiles = (int64_t)jt_count * Ks;
     for (int64_t u = blockIdx.x; u < tiles; u += gridDim.x) {
         const int jt = jt0 + (int)(u % jt_count);
         const int s = (int)(u / jt_count);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < (BNT * 8 + 255) / 256; ++h) {
             const int v = tid + 256 * h;
-            const int c8 = v & 7, jl = v >> 3;
-            const int64_t j = (int64_t)jt * BN + jl;
-            uint16_t dg[P][8];
-            float xs[8];
-            slice_unit<float, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
-            store_digits<P>(out, Ks, jt, s, jl, c8, dg);
+            if (v < BNT * 8) {
+                const int c8 = v & 7, jl = v >> 3;
+                const int64_t j = (int64_t)jt * BNT + jl;
+                uint16_t dg[P][8];
+                float xs[8];
+                slice_unit<float, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
+                store_digits<P, BNT>(out, Ks, jt, s, jl, c8, dg);
 #pragma unroll
-            for (int t = 0; t < 8; ++t) tile[c8 * 8 + t][jl] = xs[t];
+                for (int t = 0; t < 8; ++t) tile[c8 * 8 + t][jl] = xs[t];
+            }
         }
         __syncthreads();
-        const int64_t k0 = (int64_t)s * BK, j0 = (int64_t)jt * BN;
+        const int64_t k0 = (int64_t)s * BK, j0 = (int64_t)jt * BNT;
 #pragma unroll 4
-        for (int q = 0; q < 16; ++q) {
+        for (int q = 0; q < BK * BNT / 256; ++q) {
             const int idx = q * 256 + tid;
-            const int kk = idx >> 6, jj = idx & 63;
+            const int kk = idx / BNT, jj = idx % BNT;
             if (k0 + kk < K && j0 + jj < ldq) AQ[(k0 + kk) * ldq + j0 + jj] = tile[kk][jj];
         }
         __syncthreads();
@@ -646,17 +659,17 @@ __global__ void __launch_bounds__(256) slice_rowmajor_kernel(const float* __rest
 // C[i, j] = 2^(E_j - shift) * sum over kc of partial[kc][tile][col][row].
 // The chunk sums are exact integers; they are added in int64 when the
 // caller guarantees no overflow (exact_sum), else in FP64, in a fixed order.
-__global__ void splitk_sum_kernel(const long long* __restrict__ part, int kc_count, int tiles_m, int tiles_n,
+__global__ void splitk_sum_kernel(const long long* __restrict__ part, int kc_count, int tiles_m, int tiles_n, int bn,
                                   int64_t M, int64_t N, const int* __restrict__ colexp, int shift, int exact_sum,
                                   double* __restrict__ C, int64_t ldc) {
     const int64_t total = M * N;
-    const size_t tile_elems = (size_t)BM * BN;
+    const size_t tile_elems = (size_t)BM * bn;
     const size_t kc_stride = (size_t)tiles_m * tiles_n * tile_elems;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t i = e % M, j = e / M;
-        const int it = (int)(i / BM), jt = (int)(j / BN);
-        const size_t off = (size_t)(it + (int64_t)tiles_m * jt) * tile_elems + (size_t)(j % BN) * BM + (i % BM);
+        const int it = (int)(i / BM), jt = (int)(j / bn);
+        const size_t off = (size_t)(it + (int64_t)tiles_m * jt) * tile_elems + (size_t)(j % bn) * BM + (i % BM);
         double s;
         if (exact_sum) {
             long long t = 0;
@@ -670,19 +683,20 @@ __global__ void splitk_sum_kernel(const long long* __restrict__ part, int kc_cou
     }
 }
 
-template <int P>
+template <int P, int BNT>
 static size_t smem_bytes() {
-    constexpr int STAGES = stages_for(P);
-    return 1024 + (size_t)STAGES * S_BYTES + (size_t)STAGES * P * YD_BYTES + 512;
+    constexpr int STAGES = stages_for(P, BNT);
+    return 1024 + (size_t)STAGES * S_BYTES + (size_t)STAGES * P * (BNT * ROW_BYTES) + 512;
 }
 
 template <int P>
 static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32, int64_t K, int64_t N0,
                 int64_t ldy, const double* extra, int64_t M, double* C, int64_t ldc, const ColumnFeed* feed,
                 const std::function<void(cudaStream_t)>& before_mma, const SketchRowMajor& rm) {
+    constexpr int BNR = bn_for(P);               // column tile width of this launch
     const int64_t N = N0 + (extra ? 1 : 0);      // the extra column is appended as column N0
-    const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BN);
-    const size_t smem = smem_bytes<P>();
+    const int tiles_m = div_up(M, BM), tiles_n = div_up(N, BNR);
+    const size_t smem = smem_bytes<P, BNR>();
     const int Ks = div_up(K, BK);
     const int wins = div_up(Ks, WIN);
     // choose the K split for the persistent walk: about
@@ -717,12 +731,12 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     const int kc_count = div_up(Ks, spk);
     const int64_t units = tiles_launch * kc_count;
 
-    DevBuf<int> E((size_t)tiles_n * BN, ctx.stream);
-    exp_init_kernel<<<(unsigned)div_up((int64_t)tiles_n * BN, 256), 256, 0, ctx.stream>>>(E, (int64_t)tiles_n * BN);
+    DevBuf<int> E((size_t)tiles_n * BNR, ctx.stream);
+    exp_init_kernel<<<(unsigned)div_up((int64_t)tiles_n * BNR, 256), 256, 0, ctx.stream>>>(E, (int64_t)tiles_n * BNR);
     RNLA_LAUNCH_CHECK();
-    DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * (YD_BYTES / 2), ctx.stream);
+    DevBuf<uint16_t> dig((size_t)tiles_n * Ks * P * BNR * (ROW_BYTES / 2), ctx.stream);
     DevBuf<uint8_t> sk((size_t)tiles_m * Ks * S_BYTES, ctx.stream);
-    DevBuf<long long> part((size_t)kc_count * tiles * BM * BN, ctx.stream);
+    DevBuf<long long> part((size_t)kc_count * tiles * BM * BNR, ctx.stream);
     // the sketch generator (integer ALU bound) runs on the side stream while
     // the main stream makes the digit planes (HBM bound)
     const cudaStream_t side = (ctx.side ? ctx.side : side_stream(ctx.device));
@@ -753,13 +767,13 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     prm.kc_count = kc_count; prm.stages_per_kc = spk; prm.units = (int)units;
     prm.sk = sk; prm.ydig = dig; prm.ypl = P; prm.partial = part; prm.status = ctx.status;
     ctx.clear_status();
-    auto kfn = sketch_mma_kernel<P>;
+    auto kfn = sketch_mma_kernel<P, BNR>;
     set_smem_limit((const void*)kfn, smem);
     const unsigned grid = (unsigned)(units < sm ? units : sm);
     // exponents and digit planes of column tiles [jt0, jt0 + cnt)
     auto digits = [&](int jt0, int cnt) {
-        const int64_t j0 = (int64_t)jt0 * BN;
-        const int64_t j1 = std::min((int64_t)N, (int64_t)(jt0 + cnt) * BN);
+        const int64_t j0 = (int64_t)jt0 * BNR;
+        const int64_t j1 = std::min((int64_t)N, (int64_t)(jt0 + cnt) * BNR);
         // about 16 values per thread: K / 4096 blocks per column
         const int64_t rpb = 4096;
         const dim3 cg((unsigned)div_up(K, rpb), (unsigned)(j1 - j0));
@@ -768,18 +782,18 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         else
             colexp_kernel<double><<<cg, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, E, j0, rpb);
         RNLA_LAUNCH_CHECK();
-        const int64_t su = (int64_t)Ks * 8 * cnt * BN;
+        const int64_t su = (int64_t)Ks * 8 * cnt * BNR;
         int g = div_up(su, 256);
         if (g > 32 * sm) g = 32 * sm;
         if (y_f32 && rm.dst) {
             const int64_t tl = (int64_t)cnt * Ks;
             const int gr = (int)std::min<int64_t>(tl, 8 * sm);
-            slice_rowmajor_kernel<P><<<gr, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt,
+            slice_rowmajor_kernel<P, BNR><<<gr, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt,
                                                                  dig, rm.dst, rm.ld);
         } else if (y_f32)
-            slice_kernel<float, P><<<g, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
+            slice_kernel<float, P, BNR><<<g, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
         else
-            slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
+            slice_kernel<double, P, BNR><<<g, 256, 0, ctx.stream>>>((const double*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt, dig);
         RNLA_LAUNCH_CHECK();
     };
     if (!feed) {
@@ -797,7 +811,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         for (int g0 = 0; g0 < tiles_n; g0 += per_group) {
             const int cnt = std::min(per_group, tiles_n - g0);
             for (int jt = g0; jt < g0 + cnt; ++jt) {
-                feed->wait_cols(ctx.stream, (int64_t)jt * BN, std::min(N0, (int64_t)(jt + 1) * BN));
+                feed->wait_cols(ctx.stream, (int64_t)jt * BNR, std::min(N0, (int64_t)(jt + 1) * BNR));
                 digits(jt, 1);
             }
             if (g0 == 0) RNLA_CUDA(cudaStreamWaitEvent(ctx.stream, s_done, 0));   // S is written
@@ -812,7 +826,7 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
     int g = div_up(M * N, 256);
     if (g > 8 * sm) g = 8 * sm;
     const int exact_sum = (int64_t)wins + kc_count <= WIN_MAX ? 1 : 0;   // all windows together fit int64
-    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, M, N, E, 8 * P + quant_shift(dist),
+    splitk_sum_kernel<<<g, 256, 0, ctx.stream>>>(part, kc_count, tiles_m, tiles_n, BNR, M, N, E, 8 * P + quant_shift(dist),
                                                  exact_sum, C, ldc);
     RNLA_LAUNCH_CHECK();
     RNLA_CUDA(cudaEventDestroy(s_done));
@@ -948,8 +962,8 @@ __global__ void exact_tn_sum_kernel(const long long* __restrict__ part, int kc_c
 template <int P>
 static void launch_mma(Ctx& ctx, const tc::Params& prm, unsigned grid) {
     using namespace tc;
-    const size_t smem = smem_bytes<P>();
-    auto kfn = sketch_mma_kernel<P>;
+    const size_t smem = smem_bytes<P, BN>();
+    auto kfn = sketch_mma_kernel<P, BN>;
     set_smem_limit((const void*)kfn, smem);
     kfn<<<grid, THREADS, smem, ctx.stream>>>(prm);
     RNLA_LAUNCH_CHECK();
@@ -1001,7 +1015,7 @@ void tc_exact_tn(Ctx& ctx, const void* X, bool x_f32, int64_t K, int64_t MM, int
         const int64_t su = (int64_t)Ks * 8 * tiles_n * BN;
         int g = div_up(su, 256);
         if (g > 32 * sm) g = 32 * sm;
-        slice_kernel<double, P><<<g, 256, 0, ctx.stream>>>(Y, K, NN, ldy, nullptr, NN, Ey, Ks, 0, tiles_n, dig);
+        slice_kernel<double, P, BN><<<g, 256, 0, ctx.stream>>>(Y, K, NN, ldy, nullptr, NN, Ey, Ks, 0, tiles_n, dig);
         RNLA_LAUNCH_CHECK();
     }
     const size_t digit_bytes = (size_t)tiles_m * Ks * S_BYTES;
