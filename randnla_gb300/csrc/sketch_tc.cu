@@ -198,7 +198,10 @@ __global__ void __launch_bounds__(256) sketch_gen_gauss_kernel(RngKey key, int64
         uint8_t* tile = S + ((size_t)it * Ks + (size_t)s) * S_BYTES;
         const int64_t k0 = (int64_t)s * BK + 2 * kp;
         const uint64_t gs = g0 + (uint64_t)s * BK * gstride;
-#pragma unroll 1
+        // all four slabs unrolled: eight independent Philox chains per thread
+        // (4.47 ms at the full precision least-squares sketch against 4.68
+        // one slab at a time)
+#pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int64_t row0 = (int64_t)it * BM + 4 * (igq + 8 * q);
             uint32_t r0[4] = {0u, 0u, 0u, 0u}, r1[4] = {0u, 0u, 0u, 0u};
