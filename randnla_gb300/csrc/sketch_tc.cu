@@ -626,31 +626,42 @@ __global__ void __launch_bounds__(256) slice_rowmajor_kernel(const float* __rest
                                                              int64_t Ntot, const int* __restrict__ E, int Ks,
                                                              int jt0, int jt_count, uint16_t* __restrict__ out,
                                                              float* __restrict__ AQ, int64_t ldq) {
-    static_assert(BK == 64 && (BK * BNT) % 256 == 0, "tile shape");
-    __shared__ float tile[BK][BNT + 1];
+    // SPI stages per iteration, so that the iteration's (column, 8 k) units
+    // are a whole number per thread (two stages of 80 columns: 1280 units,
+    // five each)
+    constexpr int SPI = (BNT * 8) % 256 == 0 ? 1 : 2;
+    constexpr int UNITS = SPI * BNT * 8;
+    static_assert(BK == 64 && UNITS % 256 == 0 && (SPI * BK * BNT) % 256 == 0, "tile shape");
+    __shared__ float tile[SPI * BK][BNT + 1];
     const int tid = threadIdx.x;
-    const int64_t tiles = (int64_t)jt_count * Ks;
+    const int pairs = (Ks + SPI - 1) / SPI;
+    const int64_t tiles = (int64_t)jt_count * pairs;
     for (int64_t u = blockIdx.x; u < tiles; u += gridDim.x) {
         const int jt = jt0 + (int)(u % jt_count);
-        const int s = (int)(u / jt_count);
+        const int s0 = (int)(u / jt_count) * SPI;
 #pragma unroll
-        for (int h = 0; h < (BNT * 8 + 255) / 256; ++h) {
+        for (int h = 0; h < UNITS / 256; ++h) {
             const int v = tid + 256 * h;
-            if (v < BNT * 8) {
-                const int c8 = v & 7, jl = v >> 3;
+            const int ss = v / (BNT * 8), w = v % (BNT * 8);
+            const int c8 = w & 7, jl = w >> 3;
+            const int s = s0 + ss;
+            float xs[8];
+            if (s < Ks) {
                 const int64_t j = (int64_t)jt * BNT + jl;
                 uint16_t dg[P][8];
-                float xs[8];
                 slice_unit<float, P>(Y, K, N, ldy, extra, Ntot, E, j, s, c8, dg, xs);
                 store_digits<P, BNT>(out, Ks, jt, s, jl, c8, dg);
+            } else {
 #pragma unroll
-                for (int t = 0; t < 8; ++t) tile[c8 * 8 + t][jl] = xs[t];
+                for (int t = 0; t < 8; ++t) xs[t] = 0.f;
             }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) tile[ss * BK + c8 * 8 + t][jl] = xs[t];
         }
         __syncthreads();
-        const int64_t k0 = (int64_t)s * BK, j0 = (int64_t)jt * BNT;
+        const int64_t k0 = (int64_t)s0 * BK, j0 = (int64_t)jt * BNT;
 #pragma unroll 4
-        for (int q = 0; q < BK * BNT / 256; ++q) {
+        for (int q = 0; q < SPI * BK * BNT / 256; ++q) {
             const int idx = q * 256 + tid;
             const int kk = idx / BNT, jj = idx % BNT;
             if (k0 + kk < K && j0 + jj < ldq) AQ[(k0 + kk) * ldq + j0 + jj] = tile[kk][jj];
@@ -789,8 +800,14 @@ static void run(Ctx& ctx, const RngKey& key, int dist, const void* Y, bool y_f32
         int g = div_up(su, 256);
         if (g > 32 * sm) g = 32 * sm;
         if (y_f32 && rm.dst) {
-            const int64_t tl = (int64_t)cnt * Ks;
-            const int gr = (int)std::min<int64_t>(tl, 8 * sm);
+            // every block resident at once (a grid of whole waves)
+            static const int occ = [] {
+                int o = 0;
+                RNLA_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, slice_rowmajor_kernel<P, bn_for(P)>, 256, 0));
+                return o;
+            }();
+            const int64_t tl = (int64_t)cnt * div_up(Ks, (BNR * 8) % 256 == 0 ? 1 : 2);
+            const int gr = (int)std::min<int64_t>(tl, (int64_t)std::max(occ, 1) * sm);
             slice_rowmajor_kernel<P, BNR><<<gr, 256, 0, ctx.stream>>>((const float*)Y, K, N0, ldy, extra, N, E, Ks, jt0, cnt,
                                                                  dig, rm.dst, rm.ld);
         } else if (y_f32)
