@@ -39,6 +39,21 @@ def test_integer_data_bit_exact(rnla, d, m, n):
     assert torch.equal(C, ref), (C - ref).abs().max().item()
 
 
+@pytest.mark.parametrize("digits,vmax", [(3, 1000), (2, 1000), (1, 127)])
+@pytest.mark.parametrize("n", [1, 79, 80, 81, 159, 161])
+def test_integer_fp32_data_80_column_tiles_bit_exact(rnla, digits, vmax, n):
+    """FP32 data with up to three digits runs on 80-column digit tiles (one
+    MMA of N = 80 x digits); integers that the digits hold exactly give the
+    exact product, for column counts on both sides of the tile edges."""
+    import torch
+    d, m = 136, 3001
+    g = torch.Generator(device="cuda").manual_seed(31 * n + digits)
+    Y = torch.randint(-vmax, vmax + 1, (n, m), generator=g, device="cuda").float().t()
+    C = _tc(Y, d, seed=21, digits=digits)
+    ref = _quantized_sketch(d, m, 21) @ Y.double()
+    assert torch.equal(C, ref), (C - ref).abs().max().item()
+
+
 @pytest.mark.parametrize("dist", [1, 2])
 @pytest.mark.parametrize("d,m,n", [(200, 5000, 100), (37, 4099, 5)])
 def test_uniform_and_rademacher_bit_exact(rnla, dist, d, m, n):
