@@ -22,24 +22,29 @@
 // entry of Y) and the final conversion to FP64; S is applied exactly.
 //
 // Pipeline.
-//   sketch_gen_kernel  writes S once as bf16 tile images [m tile][K stage]
-//                      (128 x 64, the exact SWIZZLE_128B K-major shared-memory
-//                      layout), 16 KB each: 2 bytes per entry of HBM traffic
-//                      instead of generating S inside the GEMM;
+//   sketch_gen_gauss_kernel (sketch_gen_kernel for the other distributions
+//                      and ThreeFry keys) writes S once as bf16 tile images
+//                      [m tile][K stage] (128 x 64, the exact SWIZZLE_128B
+//                      K-major shared-memory layout), 16 KB each: 2 bytes per
+//                      entry of HBM traffic instead of generating S inside
+//                      the GEMM;
+//   colexp_kernel      the column exponents E_j;
 //   slice_kernel       writes the digit planes of Y as tile images
-//                      [n tile][K stage][digit] (64 x 64 bf16, 8 KB);
+//                      [n tile][K stage][digit] (W x 64 bf16, W = 80 for
+//                      P <= 3 and 64 for P = 4); slice_rowmajor_kernel the
+//                      same for FP32 data together with the solver's
+//                      row-major copy of Y from the same reads;
 //   sketch_mma_kernel  persistent: one CTA per SM walks the work units
 //                      (m tile, n tile, K chunk) u = blockIdx.x, + gridDim.x,
 //                      ...; 192 threads: warp 0 streams the S tile and the P
 //                      digit tiles of each stage with cp.async.bulk into a
-//                      4-stage (P = 4) or 5-stage (P <= 3) mbarrier ring that
-//                      runs on across units;
+//                      4- or 5-stage mbarrier ring that runs on across units;
 //                      warp 1 allocates TMEM and issues tcgen05.mma
-//                      (M = 128, N = 64 P, K = 16, bf16 x bf16 -> f32: the
+//                      (M = 128, N = W P, K = 16, bf16 x bf16 -> f32: the
 //                      P digit tiles are one operand, so digit p accumulates
-//                      in TMEM columns [64 p, 64 p + 64); two sets so the
-//                      MMAs of a window overlap the drain of the previous
-//                      one) from one lane; warps 2-5 drain TMEM after each
+//                      in TMEM columns [W p, W p + W); two sets so the MMAs
+//                      of a window overlap the drain of the previous one)
+//                      from one lane; warps 2-5 drain TMEM after each
 //                      window.  Units that share an S tile are adjacent in
 //                      the walk, so S is read from HBM about once and served
 //                      from L2 to the other column tiles;
