@@ -686,13 +686,13 @@ static void blendenpik_impl(Ctx& ctx, const void* Av, bool a_f32, int64_t m, int
             rm.dst = reinterpret_cast<float*>(lsqr_in.AF.get());
             rm.ld = lsqr_in.ldf;
         } else if (ffp && !feed) {
-            before_mma = [&](cudaStream_t st) { lsqr_ff_build(ctx, lsqr_in, lda, b, st, 0); };
+            before_mma = [&](cudaStream_t st) { lsqr_ff_build(ctx, lsqr_in, lda, b, st); };
         }
         // S [a b] in one pass: b rides along as column n of the digit planes
         tc_sketch_apply(ctx, key, Av, a_f32, m, n, lda, b, d, o.digits_a, SK, d, feed, DIST_GAUSSIAN, before_mma,
                         rm);
         if (feed) feed->wait_all(ctx.stream);
-        if (ffp && a_f32) lsqr_ff_build(ctx, lsqr_in, lda, b, ctx.stream, 0, true);
+        if (ffp && a_f32) lsqr_ff_build(ctx, lsqr_in, lda, b, ctx.stream, true);
         else if (ffp && feed) lsqr_ff_prepare(ctx, Av, a_f32, m, n, lda, b, lsqr_in);
     }
     tm.mark();

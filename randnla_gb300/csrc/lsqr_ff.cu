@@ -1408,19 +1408,19 @@ void ff_round_upper(Ctx& ctx, double* M, int64_t n, int64_t ldm) {
 // Float-float copies of A (row-major, column-pair order) and b, enqueued on
 // `st`.
 static void build_ff_input(Ctx& ctx, cudaStream_t st, const void* A, bool a_f32, int64_t m, int64_t n,
-                           int64_t lda, const double* b, int64_t ldf, float2* AF, float2* bF, int grid_cap = 0,
+                           int64_t lda, const double* b, int64_t ldf, float2* AF, float2* bF,
                            bool a_done = false) {
     using namespace lsff;
     dim3 grid((unsigned)div_up(m, 32), (unsigned)div_up(ldf, 32));
-    if (a_done) {
-    } else if (a_f32) {
-        const int64_t cap = grid_cap > 0 ? grid_cap : 8 * ctx.sm_count;
-        rowmajor_f32_kernel<<<(unsigned)std::min<int64_t>(div_up(m, 64) * div_up(ldf, 64), cap), 256, 0, st>>>(
-            static_cast<const float*>(A), m, n, lda, reinterpret_cast<float*>(AF), ldf);
-    } else
+    if (a_f32 && !a_done) {
+        rowmajor_f32_kernel<<<(unsigned)std::min<int64_t>(div_up(m, 64) * div_up(ldf, 64), 8 * ctx.sm_count), 256, 0,
+                              st>>>(static_cast<const float*>(A), m, n, lda, reinterpret_cast<float*>(AF), ldf);
+        RNLA_LAUNCH_CHECK();
+    } else if (!a_done) {
         rowmajor_split_kernel<double><<<grid, dim3(32, 8), 0, st>>>(static_cast<const double*>(A), m, n, lda,
                                                                     reinterpret_cast<float*>(AF), ldf);
-    RNLA_LAUNCH_CHECK();
+        RNLA_LAUNCH_CHECK();
+    }
     int g = (int)div_up(m, 256);
     if (g > 8 * ctx.sm_count) g = 8 * ctx.sm_count;
     vec_split_kernel<<<g, 256, 0, st>>>(b, m, bF);
@@ -1439,9 +1439,9 @@ void lsqr_ff_alloc(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, Ls
     in.owner = ctx.stream;
 }
 
-void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap,
+void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st,
                    bool a_done) {
-    build_ff_input(ctx, st, in.A, in.f32, in.m, in.n, lda, b, in.ldf, in.AF, in.bF, grid_cap, a_done);
+    build_ff_input(ctx, st, in.A, in.f32, in.m, in.n, lda, b, in.ldf, in.AF, in.bF, a_done);
     RNLA_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming));
     RNLA_CUDA(cudaEventRecord(in.ready, st));
 }
@@ -1451,7 +1451,7 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
     lsqr_ff_alloc(ctx, A, a_f32, m, n, in);
     const cudaStream_t st = ctx.side ? ctx.side : side_stream(ctx.device);
     stream_wait(st, ctx.stream);                   // buffers allocated, A and b written
-    lsqr_ff_build(ctx, in, lda, b, st, 0);
+    lsqr_ff_build(ctx, in, lda, b, st);
 }
 
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,

@@ -176,9 +176,9 @@ void lsqr_ff_prepare(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, 
 // Allocates the copies on ctx.stream (no kernels).
 void lsqr_ff_alloc(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, LsqrFFInput& in);
 // Builds them on `st`, which the caller has ordered after the allocation and
-// after A and b are written; grid_cap > 0 caps the copy kernel's blocks;
-// a_done: the copy of A is already written (tc_sketch_apply's rm), only b's.
-void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st, int grid_cap,
+// after A and b are written; a_done: the copy of A is already written
+// (tc_sketch_apply's rm), only b's is built.
+void lsqr_ff_build(Ctx& ctx, LsqrFFInput& in, int64_t lda, const double* b, cudaStream_t st,
                    bool a_done = false);
 LsqrResult lsqr_ff_solve(Ctx& ctx, const void* A, bool a_f32, int64_t m, int64_t n, int64_t lda, const double* M,
                          const double* b, const double* x0, const LsqrParams& prm, double* x, double* var,
