@@ -339,7 +339,7 @@ RNLA_API int rnla_blendenpik_overdetermined_ex(const double* a, int64_t m, int64
 /* The same with A stored in FP32 on the host (b and x stay FP64): the
  * reference takes &DMatrix<f64> only; FP32 storage halves the bytes of A
  * moved and streamed for large problems.  A goes up in 64-column chunks and
- * the sketch starts on each chunk as it lands. */
+ * the sketch starts on each of its column tiles as the tile's chunks land. */
 RNLA_API int rnla_blendenpik_overdetermined_f32_ex(const float* a, int64_t m, int64_t n, int64_t lda,
                                           const double* b, double epsilon, int64_t l,
                                           double sampling_factor, const rnla_options* opt, double* x,
