@@ -117,6 +117,34 @@ def test_qgauss_lookup_matches_restatement():
     assert np.array_equal(got, o)
 
 
+def test_qgauss_64bit_entries_select_the_same_sample():
+    """The tensor-core generator holds the alias table as 64-bit entries
+    {threshold << 7, bf16(own t) | bf16(alias t) << 16} and selects with the
+    masked word, (u & 0x01FFFF80) < threshold << 7, keeping the low or high
+    half: a restatement of that rule gives the bf16 bits of qgauss_t(u) for
+    every bucket and threshold edge."""
+    tab = np.array(_qgauss_table(), dtype=np.uint64)
+    thr, own, ali = tab & 0x3FFFF, ((tab >> 18) & 127).astype(np.int64) - 63, (tab >> 25).astype(np.int64) - 63
+
+    def bf16_bits(t):
+        return (np.asarray(t, dtype=np.float32).view(np.uint32) >> 16).astype(np.uint64)
+
+    lo = thr << np.uint64(7)
+    hi = bf16_bits(own) | (bf16_bits(ali) << np.uint64(16))
+    rng = np.random.default_rng(9)
+    u = rng.integers(0, 2 ** 32, size=20000, dtype=np.uint64)
+    # the words at each bucket's threshold edge (x = thr - 1, thr) as well
+    b = np.arange(128, dtype=np.uint64)
+    for dx in (0, 1):
+        x = np.maximum(thr.astype(np.int64) - dx, 0).astype(np.uint64)
+        u = np.concatenate([u, (b << np.uint64(25)) | (x << np.uint64(7)) | np.uint64(0x55)])
+    idx = (u >> np.uint64(25)).astype(np.int64)
+    sel = np.where((u & np.uint64(0x01FFFF80)) < lo[idx], hi[idx], hi[idx] >> np.uint64(16)) & np.uint64(0xFFFF)
+    x = (u >> np.uint64(7)) & np.uint64(0x3FFFF)
+    t = np.where(x < thr[idx], own[idx], ali[idx])
+    assert np.array_equal(sel, bf16_bits(t))
+
+
 def test_quantized_sketch_grid():
     Q = O.sketch(O.DIST_GAUSSIAN, 64, 2000, key0=1, quantized=True)
     assert np.all(np.abs(Q * 8 - np.rint(Q * 8)) == 0) and np.abs(Q).max() <= 63 / 8
