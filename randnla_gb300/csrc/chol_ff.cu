@@ -118,13 +118,34 @@ __global__ void __launch_bounds__(CT) chol_ff_kernel(float2* __restrict__ F, int
                 Rjs[q][t] = t < kb ? F[(k0 + t) + (jfirst + (int64_t)q * Gc) * n] : z2;
             }
             const int r = tid & 63, cg = tid >> 6;
+            // the panel rows of the next 64 columns are loaded into registers
+            // while the current block is applied (their L2 round trip
+            // overlaps the multiply-adds), then staged into shared memory
+            constexpr int PRE = CB * 64 / CT;
+            float2 pre[PRE];
+#pragma unroll
+            for (int u = 0; u < PRE; ++u) {
+                const int e = tid + u * CT;
+                const int t = e % CB, rr = e / CB;
+                pre[u] = (t < kb && k1 + rr < n) ? F[(k0 + t) + (k1 + rr) * n] : z2;
+            }
             for (int64_t i0 = k1; i0 <= jlast; i0 += 64) {
                 __syncthreads();
-                for (int e = tid; e < CB * 64; e += CT) {
-                    const int t = e % CB, rr = e / CB;
-                    Ps[t][rr] = (t < kb && i0 + rr < n) ? F[(k0 + t) + (i0 + rr) * n] : z2;
+#pragma unroll
+                for (int u = 0; u < PRE; ++u) {
+                    const int e = tid + u * CT;
+                    Ps[e % CB][e / CB] = pre[u];
                 }
                 __syncthreads();
+                const int64_t i1 = i0 + 64;
+                if (i1 <= jlast) {
+#pragma unroll
+                    for (int u = 0; u < PRE; ++u) {
+                        const int e = tid + u * CT;
+                        const int t = e % CB, rr = e / CB;
+                        pre[u] = (t < kb && i1 + rr < n) ? F[(k0 + t) + (i1 + rr) * n] : z2;
+                    }
+                }
                 const int64_t i = i0 + r;
                 const int q0 = i0 > jfirst ? (int)((i0 - jfirst + Gc - 1) / Gc) : 0;
                 for (int q = q0 + cg; q < nq; q += 4) {
